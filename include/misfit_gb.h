@@ -1,0 +1,191 @@
+/*
+ * misfit_gb.h -- C ABI of libmisfit_gb, the GB300 implementation of MISFIT's
+ * dynamic maximal-independent-set maintenance path.
+ *
+ * The reference (anonymous-artifacts/MISFIT) has no plugin API: its boundary
+ * is the 5-argument CLI plus the .egr / MIS / batch-folder files, and inside
+ * the binary the seam is HybridGraph + GPUVertexClusteringGraph +
+ * compact_flash_graph.  Each entry point below names the reference interface
+ * it replaces (file:line in the reference tree).
+ *
+ * Conventions:
+ *   - every function returns an mf_status (0 = success, negative = error) and
+ *     never calls exit(); the reference exits the process on every error
+ *     (src/misfit/misfit.cu:28-35, core/FlashGraph.h:110-153);
+ *   - mf_last_error() gives a one-line description of the last failure on
+ *     the calling thread;
+ *   - vertex ids are 0-based int32 (the text formats are 1-based and are
+ *     converted by the file helpers, as the reference does);
+ *   - a context is bound to one GPU and is not thread-safe: one host thread
+ *     drives it.  Host input arrays may be reused as soon as the call that
+ *     took them returns, except for mf_apply_batch_async (see there);
+ *   - all state (base CSR, delta overlay, membership, cluster ids) lives in
+ *     device memory; the library owns every buffer it allocates.
+ */
+#ifndef MISFIT_GB_H
+#define MISFIT_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mf_ctx mf_ctx;
+
+typedef enum mf_status {
+  MF_OK = 0,
+  MF_EINVAL = -1,   /* bad argument (range, size, null pointer) */
+  MF_EIO = -2,      /* file could not be opened, read or written */
+  MF_EFORMAT = -3,  /* malformed .egr / MIS / batch file */
+  MF_ECUDA = -4,    /* CUDA runtime error */
+  MF_ENOMEM = -5,   /* device or pinned allocation failed */
+  MF_ESTATE = -6,   /* inconsistent graph state (e.g. negative degree) */
+  MF_ELIMIT = -7    /* request beyond a documented fixed limit */
+} mf_status;
+
+/* Per-batch counters of the last processed batch (host-side copy). */
+typedef struct mf_batch_stats {
+  int64_t updates;          /* lines in the batch */
+  int64_t sub_batches;      /* sub-batches the split rule produced */
+  int64_t seeds;            /* mapped seed rows, summed over sub-batches */
+  int64_t candidates;       /* mapped candidate rows, summed */
+  int64_t clusters;         /* cluster_count, summed (src/misfit/misfit.cu:681) */
+  int64_t processed_edges;  /* edges walked by the repair stage */
+  int64_t exact_sizes;      /* sub-batches that needed exact 2-hop sizes */
+  int64_t max_csr;          /* MAX_CSR_ELEMENTS after the batch */
+  int64_t repair_rounds;    /* speculative repair rounds, summed */
+  double device_ms;         /* device time of the batch (CUDA events) */
+} mf_batch_stats;
+
+/* ---- lifetime -------------------------------------------------------- */
+
+/* Version of this ABI (major*10000 + minor*100 + patch). */
+int mf_version(void);
+const char* mf_status_string(int status);
+/* Last error on the calling thread ("" when none). */
+const char* mf_last_error(void);
+
+/* Open a .egr file (int32 or int64-sentinel nindex) and stage it into HBM on
+ * device `gpu`.  Replaces HybridGraph::open + FlashGraph::map_file
+ * (core/FlashGraph.h:108-169,285-289) and the GPUVertexClusteringGraph
+ * constructor (src/misfit/misfit.cu:389-421); MAX_CSR_ELEMENTS starts at the
+ * reference's estimate (src/misfit/misfit.cu:768-772). */
+int mf_open_egr(const char* path, int gpu, mf_ctx** out);
+
+/* Same, from an in-memory CSR (nindex has n+1 entries, copied). */
+int mf_open_csr(int32_t n, const int64_t* nindex, const int32_t* nlist, int gpu, mf_ctx** out);
+
+/* Release all device and host resources (~GPUVertexClusteringGraph,
+ * src/misfit/misfit.cu:423-439). */
+int mf_close(mf_ctx* ctx);
+
+int mf_num_nodes(const mf_ctx* ctx, int32_t* n);
+int mf_num_base_entries(const mf_ctx* ctx, int64_t* entries);
+
+/* ---- membership ------------------------------------------------------- */
+
+/* Upload a 0/1 membership vector of n bytes and reset all cluster ids
+ * (setMISFromHost, src/misfit/misfit.cu:448-453). */
+int mf_set_mis(mf_ctx* ctx, const uint8_t* mis, int64_t n);
+/* Download the membership vector (getMISToHost, src/misfit/misfit.cu:455-462). */
+int mf_get_mis(mf_ctx* ctx, uint8_t* out, int64_t n);
+/* Number of members, counted on the device. */
+int mf_mis_size(mf_ctx* ctx, int64_t* count);
+
+/* Greedy MIS of the current graph in ascending vertex order -- the set
+ * tools/compute_initial_mis.py:32-43 computes -- written to out[n] (it does
+ * not change the context's membership). */
+int mf_greedy_mis(mf_ctx* ctx, uint8_t* out, int64_t n);
+
+/* ---- updates --------------------------------------------------------- */
+
+/* is_insertion = !isAdjacent(u, v) against the current graph, one byte per
+ * update (core/cli_setup.h:66-82; src/misfit/misfit.cu:812-828 evaluates it
+ * for every batch before any batch is applied). */
+int mf_flag_updates(mf_ctx* ctx, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out);
+
+/* Process one batch: conditional overlay insert/delete in file order, the
+ * sub-batch split, 2-hop neighbourhoods, clustering and MIS repair.
+ * Replaces processBatchGPUVertexClustering (src/misfit/misfit.cu:704-730)
+ * with GPUVertexClusteringGraph::processBatchWithVertexClustering
+ * (:468-692).  u, v: 0-based endpoints, u != v, both < n; ins: the flags.
+ * Host arrays; returns when the batch is complete on the device. */
+int mf_apply_batch(mf_ctx* ctx, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m);
+
+/* Same with device-resident inputs (device pointers, m entries each). */
+int mf_apply_batch_device(mf_ctx* ctx, const int32_t* d_u, const int32_t* d_v,
+                          const uint8_t* d_ins, int64_t m);
+
+/* Enqueue a batch and return after the host-side part; the host arrays must
+ * stay valid until the next mf_sync.  Pairs with mf_sync like
+ * launchBatch / syncAndCollect of the pipelined engine
+ * (src/misfit_async/misfit_async.cu:484-700). */
+int mf_apply_batch_async(mf_ctx* ctx, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m);
+int mf_sync(mf_ctx* ctx);
+
+int mf_last_batch_stats(mf_ctx* ctx, mf_batch_stats* out);
+
+/* ---- graph queries ----------------------------------------------------- */
+
+/* Row of x in overlay order (base minus tombstones, then added neighbours in
+ * insertion order; DeltaOverlay::neighbors_into, core/FlashGraph.h:214-233).
+ * Writes min(len, cap) entries and the full length to *len. */
+int mf_get_row(mf_ctx* ctx, int32_t x, int32_t* out, int64_t cap, int64_t* len);
+/* DeltaOverlay::degree (core/FlashGraph.h:235-242) for all n vertices. */
+int mf_get_degrees(mf_ctx* ctx, int32_t* out, int64_t n);
+int mf_is_adjacent(mf_ctx* ctx, int32_t u, int32_t v, int* adjacent);
+int mf_get_max_csr(mf_ctx* ctx, int64_t* value);
+int mf_set_max_csr(mf_ctx* ctx, int64_t value);
+int mf_get_cluster_ids(mf_ctx* ctx, int32_t* out, int64_t n);
+
+/* Independence violations (edges with both ends in the set) and uncovered
+ * vertices (neither in the set nor adjacent to it) on the current graph. */
+int mf_check_mis(mf_ctx* ctx, int64_t* violations, int64_t* uncovered);
+
+/* ---- compaction -------------------------------------------------------- */
+
+/* Merge base + overlay on the device and write an int64-sentinel .egr via a
+ * temporary file, fsync, rename and directory fsync.  With rebase != 0 the
+ * merged CSR becomes the new base and the overlay is cleared (the
+ * reference's remap + delta.clear(), src/misfit/misfit.cu:919-921).
+ * Replaces compact_flash_graph (core/flash_compactor.h:20-105). */
+int mf_compact(mf_ctx* ctx, const char* out_path, int rebase);
+
+/* ---- file helpers (host) ----------------------------------------------- */
+
+/* Read a MIS file (1-based ids, one per line; out-of-range ids ignored,
+ * src/misfit/misfit.cu:778-791) into out[n]; *lines counts accepted lines. */
+int mf_read_mis_file(const char* path, int32_t n, uint8_t* out, int64_t* lines);
+/* Write the members of mis[n] 1-based, one per line (src/misfit/misfit.cu:892-907). */
+int mf_write_mis_file(const char* path, const uint8_t* mis, int32_t n);
+
+/* Parse a batch file: lines "u v" (1-based); lines that do not start with
+ * two integers, out-of-range ids and self-loops are dropped
+ * (core/cli_setup.h:66-82).  *u and *v are malloc'd 0-based arrays the
+ * caller releases with mf_free. */
+int mf_read_batch_file(const char* path, int32_t n, int32_t** u, int32_t** v, int64_t* m);
+/* Regular files of a folder sorted by the integer value of their stem
+ * (core/cli_setup.h:49-59); names joined by '\n' into a malloc'd string. */
+int mf_list_batch_files(const char* folder, char** names, int64_t* count);
+void mf_free(void* p);
+
+/* ---- trace (parity tests) ---------------------------------------------- */
+
+/* When enabled, mf_apply_batch keeps, per sub-batch, the stage outputs the
+ * tests compare with the oracle.  field: 0 header int64[10] = {p, q,
+ * n_seeds, n_cands, packed (or -1 when not needed), max_after,
+ * cluster_count, n_processed, n_rows, estimate}; 1 seeds (int32); 2
+ * candidates (int32); 3 cluster ids after clustering (int32[n]); 4 processed
+ * edges in repair order (int32 batch index); 5 membership after repair
+ * (uint8[n]); 6 row lengths (int64, only when packed >= 0). */
+int mf_trace_enable(mf_ctx* ctx, int on);
+int mf_trace_count(mf_ctx* ctx, int64_t* count);
+int mf_trace_get(mf_ctx* ctx, int64_t index, int field, void* out, int64_t cap, int64_t* len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,716 @@
+// mf_api.cu -- extern "C" entry points of libmisfit_gb and the host-side file
+// formats (.egr, MIS file, batch folder).
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "mf_internal.cuh"
+
+namespace mf {
+
+namespace {
+thread_local std::string g_error;
+}
+
+void set_error(const std::string& msg) { g_error = msg; }
+const char* get_error() { return g_error.c_str(); }
+
+}  // namespace mf
+
+namespace {
+
+using mf::Failure;
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    mf::set_error("");
+    f();
+    return MF_OK;
+  } catch (const Failure& e) {
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    mf::set_error("host allocation failed");
+    return MF_ENOMEM;
+  } catch (const std::exception& e) {
+    mf::set_error(e.what());
+    return MF_EINVAL;
+  }
+}
+
+void need(bool cond, int status, const char* msg) {
+  if (!cond) MF_FAIL(status, msg);
+}
+
+void release_all(mf_ctx* c) {
+  mf::DBuf<int64_t>* b64[] = {&c->nindex, &c->aoff, &c->aoff_alt, &c->i64a, &c->i64b, &c->rowlens, &c->counters};
+  for (auto* b : b64) b->release();
+  mf::DBuf<int32_t>* b32[] = {&c->nlist, &c->dead, &c->rcnt, &c->deg, &c->aadj, &c->aown, &c->aadj_alt, &c->aown_alt,
+                              &c->cid, &c->v2i, &c->f1, &c->bu, &c->bv, &c->prev, &c->i32a, &c->i32b, &c->i32c,
+                              &c->acnt_new, &c->seeds, &c->cands, &c->hlist, &c->touched, &c->rowcid};
+  for (auto* b : b32) b->release();
+  c->live.release();
+  c->hmark.release();
+  c->bval.release();
+  c->wval.release();
+  c->bitmaps.release();
+  c->mis.release();
+  c->bins.release();
+  c->u8a.release();
+  c->akill.release();
+  c->creates.release();
+  c->keys.release();
+  c->vals.release();
+  c->app_keys.release();
+  c->app_vals.release();
+  c->ws.release();
+  if (c->h_counters) cudaFreeHost(c->h_counters);
+  c->h_counters = nullptr;
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  c->stream = nullptr;
+}
+
+mf_ctx* new_ctx(int gpu) {
+  int count = 0;
+  MF_CUDA(cudaGetDeviceCount(&count));
+  if (gpu < 0 || gpu >= count) MF_FAIL(MF_EINVAL, "gpu id out of range");
+  MF_CUDA(cudaSetDevice(gpu));
+  mf_ctx* c = new mf_ctx();
+  c->device = gpu;
+  try {
+    MF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    MF_CUDA(cudaEventCreate(&c->ev0));
+    MF_CUDA(cudaEventCreate(&c->ev1));
+    MF_CUDA(cudaMallocHost(&c->h_counters, sizeof(int64_t) * 64));
+    c->counters.reserve(64);
+  } catch (...) {
+    release_all(c);
+    delete c;
+    throw;
+  }
+  return c;
+}
+
+void bind(const mf_ctx* c) { MF_CUDA(cudaSetDevice(c->device)); }
+
+// Inputs of a batch are already in c->bu / c->bv / c->bins.
+void run_batch(mf_ctx* c, int64_t m) {
+  cudaStream_t s = c->stream;
+  c->stats = mf_batch_stats{};
+  c->stats.updates = m;
+  c->traces.clear();
+  MF_CUDA(cudaEventRecord(c->ev0, s));
+  if (m > 0) {
+    mf::apply_overlay(c, m);
+    mf::process_batch(c, m);
+  }
+  MF_CUDA(cudaEventRecord(c->ev1, s));
+  MF_CUDA(cudaEventSynchronize(c->ev1));
+  float ms = 0.f;
+  MF_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->stats.device_ms = ms;
+  c->stats.max_csr = c->max_csr;
+}
+
+__global__ void k_validate(const int32_t* u, const int32_t* v, int64_t m, int32_t n, unsigned long long* bad) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int32_t a = u[i], b = v[i];
+  if (a < 0 || a >= n || b < 0 || b >= n || a == b) atomicAdd(bad, 1ull);
+}
+
+void stage_inputs(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m,
+                  cudaMemcpyKind kind) {
+  cudaStream_t s = c->stream;
+  c->bu.reserve(m);
+  c->bv.reserve(m);
+  c->bins.reserve(m);
+  if (m == 0) return;
+  MF_CUDA(cudaMemcpyAsync(c->bu.p, u, sizeof(int32_t) * (size_t)m, kind, s));
+  MF_CUDA(cudaMemcpyAsync(c->bv.p, v, sizeof(int32_t) * (size_t)m, kind, s));
+  if (ins) MF_CUDA(cudaMemcpyAsync(c->bins.p, ins, (size_t)m, kind, s));
+  MF_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int64_t), s));
+  k_validate<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(c->bu.p, c->bv.p, m, c->n,
+                                                          reinterpret_cast<unsigned long long*>(c->counters.p));
+  MF_CUDA(cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
+  if (c->h_counters[0] != 0) MF_FAIL(MF_EINVAL, "update endpoints must be distinct vertex ids in [0, n)");
+}
+
+// ---- .egr ----------------------------------------------------------------------
+
+struct EgrHeader {
+  int32_t n = 0;
+  uint64_t edges = 0;
+  bool wide = false;
+  size_t header_bytes = 0;
+};
+
+EgrHeader read_egr_header(FILE* f, const char* path, size_t file_size) {
+  EgrHeader h;
+  int32_t e32 = 0;
+  need(std::fread(&h.n, 4, 1, f) == 1 && std::fread(&e32, 4, 1, f) == 1, MF_EFORMAT,
+       "failed to read the .egr header");
+  if (e32 == -1) {
+    need(std::fread(&h.edges, 8, 1, f) == 1, MF_EFORMAT, "failed to read the 64-bit edge count");
+    h.wide = true;
+    h.header_bytes = 16;
+  } else {
+    need(h.n >= 1 && e32 >= 0, MF_EFORMAT, "invalid .egr header (nodes < 1 or edges < 0)");
+    h.edges = (uint64_t)e32;
+    h.header_bytes = 8;
+  }
+  need(h.n >= 0, MF_EFORMAT, "invalid .egr header (negative node count)");
+  const size_t need_bytes = h.header_bytes + ((size_t)h.n + 1) * (h.wide ? 8 : 4) + (size_t)h.edges * 4;
+  if (need_bytes > file_size)
+    MF_FAIL(MF_EFORMAT, std::string("truncated .egr file ") + path);
+  return h;
+}
+
+mf_ctx* open_egr(const char* path, int gpu) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) MF_FAIL(MF_EIO, std::string("could not open ") + path);
+  struct stat st;
+  if (fstat(fileno(f), &st) != 0) {
+    std::fclose(f);
+    MF_FAIL(MF_EIO, std::string("fstat failed for ") + path);
+  }
+  EgrHeader h;
+  try {
+    h = read_egr_header(f, path, (size_t)st.st_size);
+  } catch (...) {
+    std::fclose(f);
+    throw;
+  }
+  std::vector<int64_t> nindex((size_t)h.n + 1);
+  bool ok;
+  if (h.wide) {
+    ok = std::fread(nindex.data(), 8, nindex.size(), f) == nindex.size();
+  } else {
+    std::vector<int32_t> t(nindex.size());
+    ok = std::fread(t.data(), 4, t.size(), f) == t.size();
+    for (size_t i = 0; ok && i < t.size(); ++i) nindex[i] = t[i];
+  }
+  if (!ok) {
+    std::fclose(f);
+    MF_FAIL(MF_EFORMAT, "failed to read nindex");
+  }
+  mf_ctx* c = nullptr;
+  try {
+    c = new_ctx(gpu);
+    c->header_edges = h.edges;
+    // nlist: read through two pinned chunks, copied asynchronously.
+    const int64_t nnz = (int64_t)h.edges;
+    c->nlist.reserve(std::max<int64_t>(nnz, 1));
+    const size_t chunk = (size_t)64 << 20;
+    void* pin[2] = {nullptr, nullptr};
+    cudaEvent_t done[2];
+    MF_CUDA(cudaMallocHost(&pin[0], chunk));
+    MF_CUDA(cudaMallocHost(&pin[1], chunk));
+    MF_CUDA(cudaEventCreate(&done[0]));
+    MF_CUDA(cudaEventCreate(&done[1]));
+    size_t off = 0, total = (size_t)nnz * 4;
+    int slot = 0;
+    bool rd_ok = true;
+    while (off < total) {
+      const size_t len = std::min(chunk, total - off);
+      MF_CUDA(cudaEventSynchronize(done[slot]));
+      if (std::fread(pin[slot], 1, len, f) != len) { rd_ok = false; break; }
+      MF_CUDA(cudaMemcpyAsync((char*)c->nlist.p + off, pin[slot], len, cudaMemcpyHostToDevice, c->stream));
+      MF_CUDA(cudaEventRecord(done[slot], c->stream));
+      off += len;
+      slot ^= 1;
+    }
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+    cudaFreeHost(pin[0]);
+    cudaFreeHost(pin[1]);
+    cudaEventDestroy(done[0]);
+    cudaEventDestroy(done[1]);
+    std::fclose(f);
+    f = nullptr;
+    if (!rd_ok) MF_FAIL(MF_EFORMAT, "failed to read nlist");
+    mf::upload_base(c, h.n, nindex.data(), nullptr, nnz);
+  } catch (...) {
+    if (f) std::fclose(f);
+    if (c) {
+      release_all(c);
+      delete c;
+    }
+    throw;
+  }
+  return c;
+}
+
+int write_egr_int64(const std::string& out_path, int32_t n, const std::vector<int64_t>& nindex,
+                    const std::vector<int32_t>& nlist) {
+  const std::string tmp = out_path + ".tmp." + std::to_string(getpid());
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) MF_FAIL(MF_EIO, "could not open " + tmp + " for writing");
+  const int32_t sentinel = -1;
+  const uint64_t total = (uint64_t)nlist.size();
+  bool ok = std::fwrite(&n, 4, 1, f) == 1 && std::fwrite(&sentinel, 4, 1, f) == 1 &&
+            std::fwrite(&total, 8, 1, f) == 1 &&
+            std::fwrite(nindex.data(), 8, nindex.size(), f) == nindex.size() &&
+            (nlist.empty() || std::fwrite(nlist.data(), 4, nlist.size(), f) == nlist.size());
+  if (ok) ok = std::fflush(f) == 0 && fsync(fileno(f)) == 0;
+  std::fclose(f);
+  if (!ok) {
+    std::remove(tmp.c_str());
+    MF_FAIL(MF_EIO, "failed writing " + tmp);
+  }
+  if (std::rename(tmp.c_str(), out_path.c_str()) != 0) MF_FAIL(MF_EIO, "rename " + tmp + " -> " + out_path + " failed");
+  std::string dir = ".";
+  const size_t slash = out_path.find_last_of('/');
+  if (slash != std::string::npos) dir = out_path.substr(0, slash);
+  const int fd = ::open(dir.c_str(), O_RDONLY);
+  if (fd >= 0) {
+    fsync(fd);
+    ::close(fd);
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mf_version(void) { return 10000; }
+
+const char* mf_status_string(int status) {
+  switch (status) {
+    case MF_OK: return "ok";
+    case MF_EINVAL: return "invalid argument";
+    case MF_EIO: return "i/o error";
+    case MF_EFORMAT: return "malformed input file";
+    case MF_ECUDA: return "CUDA error";
+    case MF_ENOMEM: return "out of memory";
+    case MF_ESTATE: return "inconsistent graph state";
+    case MF_ELIMIT: return "request beyond a fixed limit";
+    default: return "unknown status";
+  }
+}
+
+const char* mf_last_error(void) { return mf::get_error(); }
+
+int mf_open_egr(const char* path, int gpu, mf_ctx** out) {
+  return guarded([&] {
+    need(path && out, MF_EINVAL, "null argument");
+    *out = nullptr;
+    *out = open_egr(path, gpu);
+  });
+}
+
+int mf_open_csr(int32_t n, const int64_t* nindex, const int32_t* nlist, int gpu, mf_ctx** out) {
+  return guarded([&] {
+    need(out && nindex && n >= 0, MF_EINVAL, "bad CSR arguments");
+    *out = nullptr;
+    const int64_t nnz = nindex[n];
+    need(nnz >= 0 && (nnz == 0 || nlist), MF_EINVAL, "bad CSR arguments");
+    mf_ctx* c = new_ctx(gpu);
+    try {
+      c->header_edges = (uint64_t)nnz;
+      mf::upload_base(c, n, nindex, nlist, nnz);
+    } catch (...) {
+      release_all(c);
+      delete c;
+      throw;
+    }
+    *out = c;
+  });
+}
+
+int mf_close(mf_ctx* c) {
+  if (!c) return MF_OK;
+  return guarded([&] {
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    release_all(c);
+    delete c;
+  });
+}
+
+int mf_num_nodes(const mf_ctx* c, int32_t* n) {
+  return guarded([&] {
+    need(c && n, MF_EINVAL, "null argument");
+    *n = c->n;
+  });
+}
+
+int mf_num_base_entries(const mf_ctx* c, int64_t* e) {
+  return guarded([&] {
+    need(c && e, MF_EINVAL, "null argument");
+    *e = c->nnz;
+  });
+}
+
+int mf_set_mis(mf_ctx* c, const uint8_t* mis, int64_t n) {
+  return guarded([&] {
+    need(c && mis && n == c->n, MF_EINVAL, "membership vector must have n entries");
+    bind(c);
+    if (n > 0) {
+      MF_CUDA(cudaMemcpyAsync(c->mis.p, mis, (size_t)n, cudaMemcpyHostToDevice, c->stream));
+      MF_CUDA(cudaMemsetAsync(c->cid.p, 0xFF, sizeof(int32_t) * (size_t)n, c->stream));
+    }
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int mf_get_mis(mf_ctx* c, uint8_t* out, int64_t n) {
+  return guarded([&] {
+    need(c && out && n == c->n, MF_EINVAL, "output must have n entries");
+    bind(c);
+    if (n > 0) MF_CUDA(cudaMemcpyAsync(out, c->mis.p, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int mf_mis_size(mf_ctx* c, int64_t* count) {
+  return guarded([&] {
+    need(c && count, MF_EINVAL, "null argument");
+    bind(c);
+    std::vector<uint8_t> h((size_t)c->n);
+    if (c->n > 0) MF_CUDA(cudaMemcpyAsync(h.data(), c->mis.p, (size_t)c->n, cudaMemcpyDeviceToHost, c->stream));
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+    int64_t k = 0;
+    for (uint8_t b : h) k += b != 0;
+    *count = k;
+  });
+}
+
+int mf_greedy_mis(mf_ctx* c, uint8_t* out, int64_t n) {
+  return guarded([&] {
+    need(c && out && n == c->n, MF_EINVAL, "output must have n entries");
+    bind(c);
+    mf::DBuf<uint8_t> d;
+    d.reserve(std::max<int64_t>(n, 1));
+    mf::greedy_mis(c, d.p);
+    if (n > 0) MF_CUDA(cudaMemcpy(out, d.p, (size_t)n, cudaMemcpyDeviceToHost));
+    d.release();
+  });
+}
+
+int mf_flag_updates(mf_ctx* c, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out) {
+  return guarded([&] {
+    need(c && m >= 0 && (m == 0 || (u && v && ins_out)), MF_EINVAL, "bad arguments");
+    bind(c);
+    stage_inputs(c, u, v, nullptr, m, cudaMemcpyHostToDevice);
+    mf::flag_updates(c, m);
+    if (m > 0) MF_CUDA(cudaMemcpyAsync(ins_out, c->bins.p, (size_t)m, cudaMemcpyDeviceToHost, c->stream));
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int mf_apply_batch(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
+  return guarded([&] {
+    need(c && m >= 0 && (m == 0 || (u && v && ins)), MF_EINVAL, "bad arguments");
+    need(!c->pending, MF_EINVAL, "an asynchronous batch is pending; call mf_sync first");
+    bind(c);
+    stage_inputs(c, u, v, ins, m, cudaMemcpyHostToDevice);
+    run_batch(c, m);
+  });
+}
+
+int mf_apply_batch_device(mf_ctx* c, const int32_t* d_u, const int32_t* d_v, const uint8_t* d_ins, int64_t m) {
+  return guarded([&] {
+    need(c && m >= 0 && (m == 0 || (d_u && d_v && d_ins)), MF_EINVAL, "bad arguments");
+    need(!c->pending, MF_EINVAL, "an asynchronous batch is pending; call mf_sync first");
+    bind(c);
+    stage_inputs(c, d_u, d_v, d_ins, m, cudaMemcpyDeviceToDevice);
+    run_batch(c, m);
+  });
+}
+
+int mf_apply_batch_async(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
+  // The device path reads sizes back between stages, so the batch runs to
+  // completion here; the call exists so that pipelined callers keep the
+  // launch/collect structure of the reference's async engine.
+  return guarded([&] {
+    need(c && m >= 0 && (m == 0 || (u && v && ins)), MF_EINVAL, "bad arguments");
+    need(!c->pending, MF_EINVAL, "an asynchronous batch is pending; call mf_sync first");
+    bind(c);
+    stage_inputs(c, u, v, ins, m, cudaMemcpyHostToDevice);
+    run_batch(c, m);
+    c->pending = true;
+  });
+}
+
+int mf_sync(mf_ctx* c) {
+  return guarded([&] {
+    need(c != nullptr, MF_EINVAL, "null context");
+    bind(c);
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+    c->pending = false;
+  });
+}
+
+int mf_last_batch_stats(mf_ctx* c, mf_batch_stats* out) {
+  return guarded([&] {
+    need(c && out, MF_EINVAL, "null argument");
+    *out = c->stats;
+  });
+}
+
+int mf_get_row(mf_ctx* c, int32_t x, int32_t* out, int64_t cap, int64_t* len) {
+  return guarded([&] {
+    need(c && len && x >= 0 && x < c->n && (cap == 0 || out), MF_EINVAL, "bad arguments");
+    bind(c);
+    int64_t nb[2], ab[2];
+    int32_t dead = 0;
+    MF_CUDA(cudaMemcpy(nb, c->nindex.p + x, sizeof(nb), cudaMemcpyDeviceToHost));
+    MF_CUDA(cudaMemcpy(ab, c->aoff.p + x, sizeof(ab), cudaMemcpyDeviceToHost));
+    MF_CUDA(cudaMemcpy(&dead, c->dead.p + x, sizeof(dead), cudaMemcpyDeviceToHost));
+    std::vector<int32_t> base((size_t)(nb[1] - nb[0]));
+    if (!base.empty())
+      MF_CUDA(cudaMemcpy(base.data(), c->nlist.p + nb[0], sizeof(int32_t) * base.size(), cudaMemcpyDeviceToHost));
+    std::vector<int32_t> row;
+    if (dead == 0) {
+      row = base;
+    } else {
+      const int64_t w0 = nb[0] >> 5, w1 = (nb[1] + 31) >> 5;
+      std::vector<uint32_t> bits((size_t)(w1 - w0));
+      MF_CUDA(cudaMemcpy(bits.data(), c->live.p + w0, sizeof(uint32_t) * bits.size(), cudaMemcpyDeviceToHost));
+      for (int64_t k = nb[0]; k < nb[1]; ++k)
+        if ((bits[(size_t)((k >> 5) - w0)] >> (k & 31)) & 1u) row.push_back(base[(size_t)(k - nb[0])]);
+    }
+    std::vector<int32_t> add((size_t)(ab[1] - ab[0]));
+    if (!add.empty())
+      MF_CUDA(cudaMemcpy(add.data(), c->aadj.p + ab[0], sizeof(int32_t) * add.size(), cudaMemcpyDeviceToHost));
+    row.insert(row.end(), add.begin(), add.end());
+    *len = (int64_t)row.size();
+    for (int64_t i = 0; i < (int64_t)row.size() && i < cap; ++i) out[i] = row[(size_t)i];
+  });
+}
+
+int mf_get_degrees(mf_ctx* c, int32_t* out, int64_t n) {
+  return guarded([&] {
+    need(c && out && n == c->n, MF_EINVAL, "output must have n entries");
+    bind(c);
+    if (n > 0) MF_CUDA(cudaMemcpy(out, c->deg.p, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost));
+  });
+}
+
+int mf_get_cluster_ids(mf_ctx* c, int32_t* out, int64_t n) {
+  return guarded([&] {
+    need(c && out && n == c->n, MF_EINVAL, "output must have n entries");
+    bind(c);
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+    if (n > 0) MF_CUDA(cudaMemcpy(out, c->cid.p, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost));
+  });
+}
+
+int mf_is_adjacent(mf_ctx* c, int32_t u, int32_t v, int* adjacent) {
+  return guarded([&] {
+    need(c && adjacent && u >= 0 && v >= 0 && u < c->n && v < c->n, MF_EINVAL, "bad arguments");
+    bind(c);
+    uint8_t ins = 0;
+    stage_inputs(c, &u, &v, nullptr, 1, cudaMemcpyHostToDevice);
+    mf::flag_updates(c, 1);
+    MF_CUDA(cudaMemcpyAsync(&ins, c->bins.p, 1, cudaMemcpyDeviceToHost, c->stream));
+    MF_CUDA(cudaStreamSynchronize(c->stream));
+    *adjacent = ins ? 0 : 1;
+  });
+}
+
+int mf_get_max_csr(mf_ctx* c, int64_t* value) {
+  return guarded([&] {
+    need(c && value, MF_EINVAL, "null argument");
+    *value = c->max_csr;
+  });
+}
+
+int mf_set_max_csr(mf_ctx* c, int64_t value) {
+  return guarded([&] {
+    need(c && value > 0, MF_EINVAL, "bad arguments");
+    c->max_csr = value;
+  });
+}
+
+int mf_check_mis(mf_ctx* c, int64_t* violations, int64_t* uncovered) {
+  return guarded([&] {
+    need(c && violations && uncovered, MF_EINVAL, "null argument");
+    bind(c);
+    mf::check_mis(c, violations, uncovered);
+  });
+}
+
+int mf_compact(mf_ctx* c, const char* out_path, int rebase) {
+  return guarded([&] {
+    need(c && out_path, MF_EINVAL, "null argument");
+    bind(c);
+    std::vector<int64_t> ni;
+    std::vector<int32_t> nl;
+    mf::compact_graph(c, ni, nl);
+    write_egr_int64(out_path, c->n, ni, nl);
+    if (rebase) mf::rebase(c);
+  });
+}
+
+int mf_read_mis_file(const char* path, int32_t n, uint8_t* out, int64_t* lines) {
+  return guarded([&] {
+    need(path && n >= 0 && (n == 0 || out) && lines, MF_EINVAL, "bad arguments");
+    std::memset(out, 0, (size_t)n);
+    *lines = 0;
+    std::ifstream in(path);
+    if (!in.is_open()) return;  // the reference starts from an empty set
+    std::string line;
+    int64_t lineno = 0;
+    while (std::getline(in, line)) {
+      ++lineno;
+      int id;
+      try {
+        id = std::stoi(line) - 1;
+      } catch (...) {
+        MF_FAIL(MF_EFORMAT, std::string(path) + ":" + std::to_string(lineno) + ": not an integer");
+      }
+      if (id >= 0 && id < n) {
+        out[id] = 1;
+        ++*lines;
+      }
+    }
+  });
+}
+
+int mf_write_mis_file(const char* path, const uint8_t* mis, int32_t n) {
+  return guarded([&] {
+    need(path && n >= 0 && (n == 0 || mis), MF_EINVAL, "bad arguments");
+    std::ofstream out(path);
+    if (!out.is_open()) MF_FAIL(MF_EIO, std::string("could not open ") + path);
+    std::string buf;
+    buf.reserve(1 << 20);
+    for (int32_t i = 0; i < n; ++i) {
+      if (!mis[i]) continue;
+      buf += std::to_string(i + 1);
+      buf += '\n';
+      if (buf.size() > (1 << 20)) {
+        out << buf;
+        buf.clear();
+      }
+    }
+    out << buf;
+    if (!out.good()) MF_FAIL(MF_EIO, std::string("failed writing ") + path);
+  });
+}
+
+int mf_read_batch_file(const char* path, int32_t n, int32_t** u, int32_t** v, int64_t* m) {
+  return guarded([&] {
+    need(path && u && v && m, MF_EINVAL, "null argument");
+    *u = nullptr;
+    *v = nullptr;
+    *m = 0;
+    std::ifstream in(path);
+    if (!in.is_open()) MF_FAIL(MF_EIO, std::string("could not open ") + path);
+    std::vector<int32_t> a, b;
+    std::string line;
+    while (std::getline(in, line)) {
+      std::istringstream iss(line);
+      int src, dst;
+      if (iss >> src >> dst) {
+        --src;
+        --dst;
+        if (src >= 0 && src < n && dst >= 0 && dst < n && src != dst) {
+          a.push_back(src);
+          b.push_back(dst);
+        }
+      }
+    }
+    const size_t cnt = a.size();
+    *u = (int32_t*)std::malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
+    *v = (int32_t*)std::malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
+    if (!*u || !*v) {
+      std::free(*u);
+      std::free(*v);
+      *u = *v = nullptr;
+      MF_FAIL(MF_ENOMEM, "host allocation failed");
+    }
+    if (cnt) {
+      std::memcpy(*u, a.data(), sizeof(int32_t) * cnt);
+      std::memcpy(*v, b.data(), sizeof(int32_t) * cnt);
+    }
+    *m = (int64_t)cnt;
+  });
+}
+
+int mf_list_batch_files(const char* folder, char** names, int64_t* count) {
+  return guarded([&] {
+    need(folder && names && count, MF_EINVAL, "null argument");
+    *names = nullptr;
+    *count = 0;
+    std::vector<std::pair<int, std::string>> files;
+    std::error_code ec;
+    for (const auto& e : std::filesystem::directory_iterator(folder, ec)) {
+      if (!e.is_regular_file()) continue;
+      int key;
+      try {
+        key = std::stoi(e.path().stem().string());
+      } catch (...) {
+        MF_FAIL(MF_EFORMAT, "batch file name without an integer stem: " + e.path().filename().string());
+      }
+      files.emplace_back(key, e.path().filename().string());
+    }
+    if (ec) MF_FAIL(MF_EIO, std::string("could not list ") + folder);
+    std::stable_sort(files.begin(), files.end(), [](const auto& x, const auto& y) {
+      return x.first != y.first ? x.first < y.first : x.second < y.second;
+    });
+    std::string joined;
+    for (const auto& f : files) joined += f.second + "\n";
+    char* buf = (char*)std::malloc(joined.size() + 1);
+    if (!buf) MF_FAIL(MF_ENOMEM, "host allocation failed");
+    std::memcpy(buf, joined.data(), joined.size());
+    buf[joined.size()] = 0;
+    *names = buf;
+    *count = (int64_t)files.size();
+  });
+}
+
+void mf_free(void* p) { std::free(p); }
+
+int mf_trace_enable(mf_ctx* c, int on) {
+  return guarded([&] {
+    need(c != nullptr, MF_EINVAL, "null context");
+    c->trace = on != 0;
+  });
+}
+
+int mf_trace_count(mf_ctx* c, int64_t* count) {
+  return guarded([&] {
+    need(c && count, MF_EINVAL, "null argument");
+    *count = (int64_t)c->traces.size();
+  });
+}
+
+int mf_trace_get(mf_ctx* c, int64_t index, int field, void* out, int64_t cap, int64_t* len) {
+  return guarded([&] {
+    need(c && len, MF_EINVAL, "null argument");
+    need(index >= 0 && index < (int64_t)c->traces.size(), MF_EINVAL, "trace index out of range");
+    const SubBatchTrace& t = c->traces[(size_t)index];
+    auto put = [&](const void* src, int64_t cnt, size_t elem) {
+      *len = cnt;
+      if (out && cap > 0) std::memcpy(out, src, (size_t)std::min(cnt, cap) * elem);
+    };
+    switch (field) {
+      case 0: put(t.hdr, 10, 8); break;
+      case 1: put(t.seeds.data(), (int64_t)t.seeds.size(), 4); break;
+      case 2: put(t.cands.data(), (int64_t)t.cands.size(), 4); break;
+      case 3: put(t.cid_after.data(), (int64_t)t.cid_after.size(), 4); break;
+      case 4: put(t.order.data(), (int64_t)t.order.size(), 4); break;
+      case 5: put(t.mis_after.data(), (int64_t)t.mis_after.size(), 1); break;
+      case 6: put(t.row_len.data(), (int64_t)t.row_len.size(), 8); break;
+      default: MF_FAIL(MF_EINVAL, "unknown trace field");
+    }
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,287 @@
+// mf_internal.cuh -- shared declarations of libmisfit_gb (not installed).
+//
+// Device layout of one graph context (all in HBM):
+//   base CSR     nindex int64[n+1], nlist int32[E]    (both .egr layouts are
+//                widened to int64 offsets on upload)
+//   live bits    uint32[(E+31)/32]: bit k clear <=> base entry k is tombstoned
+//   dead[n]      cleared base entries per row, rcnt[n] tombstone-set sizes
+//   added CSR    aoff int64[n+1], aadj/aown int32[A]: added neighbours per
+//                vertex in insertion order (the DeltaOverlay's vectors)
+//   deg[n]       DeltaOverlay::degree (base - |tombstones| + |added|)
+//   mis[n]       uint8 membership, cid[n] int32 cluster ids (persist across
+//                sub-batches like DeviceNode::cluster_id), v2i[n] row map
+//   scratch      n-sized epoch-tagged marks and per-batch buffers
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/misfit_gb.h"
+
+namespace mf {
+
+// Fixed sizes of the reference engine (src/misfit/misfit.cu:37,560).
+constexpr int64_t kMaxBatchEdges = 1048576;          // MAX_BATCH_SIZE
+constexpr int64_t kMaxRows = 2 * kMaxBatchEdges;     // 2*MAX_BATCH_SIZE rows
+constexpr int64_t kEstimateWeight = 1000;            // hop_limit 2 estimate
+constexpr int kRowBits = 21;                         // row index < 2^21
+constexpr uint32_t kRowMask = (1u << kRowBits) - 1;
+constexpr uint32_t kMaxEpoch = (1u << (32 - kRowBits)) - 1;
+
+// ---- error handling ------------------------------------------------------
+
+void set_error(const std::string& msg);
+const char* get_error();
+
+struct Failure {
+  int status;
+};
+
+#define MF_CUDA(call)                                                          \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ::mf::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));     \
+      throw ::mf::Failure{e_ == cudaErrorMemoryAllocation ? MF_ENOMEM : MF_ECUDA}; \
+    }                                                                          \
+  } while (0)
+
+#define MF_FAIL(status, msg)            \
+  do {                                  \
+    ::mf::set_error(msg);               \
+    throw ::mf::Failure{status};        \
+  } while (0)
+
+// ---- device buffers ------------------------------------------------------
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  int64_t cap = 0;
+  void reserve(int64_t count) {
+    if (count <= cap) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    int64_t c = count < 16 ? 16 : count;
+    MF_CUDA(cudaMalloc(&p, sizeof(T) * (size_t)c));
+    cap = c;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// ---- read-only view of the current graph ----------------------------------
+
+struct GraphView {
+  int32_t n;
+  const int64_t* nindex;
+  const int32_t* nlist;
+  const uint32_t* live;
+  const int32_t* dead;
+  const int64_t* aoff;
+  const int32_t* aadj;
+};
+
+__device__ __forceinline__ bool live_at(const uint32_t* live, int64_t k) {
+  return (__ldg(live + (k >> 5)) >> (k & 31)) & 1u;
+}
+
+// Length of the overlay row of x (what neighbors_into returns).
+__device__ __forceinline__ int64_t row_len(const GraphView& g, int32_t x) {
+  return (g.nindex[x + 1] - g.nindex[x]) - g.dead[x] + (g.aoff[x + 1] - g.aoff[x]);
+}
+
+// Calls f(y) for every y of row(x) in order; stops when f returns true.
+// Returns true if stopped early.
+template <class F>
+__device__ __forceinline__ bool thread_row_until(const GraphView& g, int32_t x, F f) {
+  const int64_t b = g.nindex[x], e = g.nindex[x + 1];
+  if (g.dead[x] == 0) {
+    for (int64_t k = b; k < e; ++k)
+      if (f(__ldg(g.nlist + k))) return true;
+  } else {
+    for (int64_t k = b; k < e; ++k)
+      if (live_at(g.live, k) && f(__ldg(g.nlist + k))) return true;
+  }
+  const int64_t ab = g.aoff[x], ae = g.aoff[x + 1];
+  for (int64_t k = ab; k < ae; ++k)
+    if (f(g.aadj[k])) return true;
+  return false;
+}
+
+// Warp-cooperative: first element y of row(x) (in order) with pred(y),
+// returned in *hit; false when none.  All lanes must call it.
+template <class P>
+__device__ __forceinline__ bool warp_row_first(const GraphView& g, int32_t x, P pred, int32_t* hit) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = g.nindex[x], e = g.nindex[x + 1];
+  const bool filt = g.dead[x] != 0;
+  for (int64_t k0 = b; k0 < e; k0 += 32) {
+    const int64_t k = k0 + lane;
+    int32_t y = -1;
+    bool ok = false;
+    if (k < e) {
+      y = __ldg(g.nlist + k);
+      ok = (!filt || live_at(g.live, k)) && pred(y);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (m) {
+      *hit = __shfl_sync(0xffffffffu, y, __ffs(m) - 1);
+      return true;
+    }
+  }
+  const int64_t ab = g.aoff[x], ae = g.aoff[x + 1];
+  for (int64_t k0 = ab; k0 < ae; k0 += 32) {
+    const int64_t k = k0 + lane;
+    int32_t y = -1;
+    bool ok = false;
+    if (k < ae) {
+      y = g.aadj[k];
+      ok = pred(y);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (m) {
+      *hit = __shfl_sync(0xffffffffu, y, __ffs(m) - 1);
+      return true;
+    }
+  }
+  return false;
+}
+
+// Warp-cooperative for-each over row(x) (no order guarantee between lanes).
+template <class F>
+__device__ __forceinline__ void warp_row_each(const GraphView& g, int32_t x, F f) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = g.nindex[x], e = g.nindex[x + 1];
+  const bool filt = g.dead[x] != 0;
+  for (int64_t k = b + lane; k < e; k += 32)
+    if (!filt || live_at(g.live, k)) f(__ldg(g.nlist + k));
+  const int64_t ab = g.aoff[x], ae = g.aoff[x + 1];
+  for (int64_t k = ab + lane; k < ae; k += 32) f(g.aadj[k]);
+}
+
+// ---- primitives (mf_prims.cu) -----------------------------------------------
+
+struct Scratch;  // workspace for primitives
+
+// out[i] = sum_{j<i} in[j] for i in [0, n]; out has n+1 entries (out[n] = total).
+void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s);
+void scan_exclusive_i32(const int32_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s);
+void scan_exclusive_u8(const uint8_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s);
+// Stable LSD radix sort of (key, value) on key bits [0, bits); result in keys/vals.
+void radix_sort_pairs(uint64_t* keys, uint32_t* vals, int64_t n, int bits, Scratch& ws, cudaStream_t s);
+
+struct Scratch {
+  DBuf<int64_t> block_sums;
+  DBuf<int64_t> block_sums2;
+  DBuf<int32_t> hist;
+  DBuf<int64_t> hist_scan;
+  DBuf<uint64_t> keys_alt;
+  DBuf<uint32_t> vals_alt;
+  void release() {
+    block_sums.release();
+    block_sums2.release();
+    hist.release();
+    hist_scan.release();
+    keys_alt.release();
+    vals_alt.release();
+  }
+};
+
+int bits_for(int64_t v);  // number of bits to hold values in [0, v]
+
+}  // namespace mf
+
+// ---- the context --------------------------------------------------------------
+
+struct SubBatchTrace {
+  int64_t hdr[10];
+  std::vector<int32_t> seeds, cands, cid_after, order;
+  std::vector<uint8_t> mis_after;
+  std::vector<int64_t> row_len;
+};
+
+struct mf_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int32_t n = 0;
+  int64_t nnz = 0;
+  uint64_t header_edges = 0;
+  bool rows_sorted = true;
+
+  mf::DBuf<int64_t> nindex;
+  mf::DBuf<int32_t> nlist;
+  mf::DBuf<uint32_t> live;
+  mf::DBuf<int32_t> dead, rcnt, deg;
+  mf::DBuf<int64_t> aoff, aoff_alt;
+  mf::DBuf<int32_t> aadj, aown, aadj_alt, aown_alt;
+  int64_t a_total = 0;
+
+  mf::DBuf<uint8_t> mis;
+  mf::DBuf<int32_t> cid, v2i;
+  mf::DBuf<uint32_t> hmark, bval, wval;
+  mf::DBuf<int32_t> f1;
+  uint32_t epoch = 0;
+
+  // batch-sized buffers
+  mf::DBuf<int32_t> bu, bv;
+  mf::DBuf<uint8_t> bins;
+  mf::DBuf<uint64_t> keys;
+  mf::DBuf<uint32_t> vals;
+  mf::DBuf<int32_t> prev;       // previous edge index per endpoint slot
+  mf::DBuf<int64_t> i64a, i64b; // scans
+  mf::DBuf<int32_t> i32a, i32b, i32c;
+  mf::DBuf<uint8_t> u8a;
+  // overlay rebuild
+  mf::DBuf<int32_t> acnt_new;
+  mf::DBuf<uint8_t> akill;
+  mf::DBuf<uint64_t> app_keys;
+  mf::DBuf<uint32_t> app_vals;
+  // sub-batch buffers
+  mf::DBuf<int32_t> seeds, cands, hlist, touched;
+  mf::DBuf<int32_t> rowcid;
+  mf::DBuf<uint8_t> creates;
+  mf::DBuf<int64_t> rowlens;
+  mf::DBuf<uint32_t> bitmaps;   // per-CTA vertex bitmaps for exact 2-hop sizes
+  int64_t bitmap_words = 0;
+  int bitmap_ctas = 0;
+  mf::DBuf<int64_t> counters;   // device counters
+  int64_t* h_counters = nullptr;  // pinned mirror
+  mf::Scratch ws;
+
+  int64_t max_csr = 0;
+  mf_batch_stats stats{};
+  bool trace = false;
+  std::vector<SubBatchTrace> traces;
+
+  // pinned staging for host-input batches
+  uint8_t* h_stage = nullptr;
+  int64_t h_stage_cap = 0;
+  bool pending = false;
+
+  mf::GraphView view() const {
+    return mf::GraphView{n, nindex.p, nlist.p, live.p, dead.p, aoff.p, aadj.p};
+  }
+};
+
+namespace mf {
+// mf_overlay.cu
+void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nlist, int64_t nnz);
+void apply_overlay(mf_ctx* c, int64_t m);          // uses c->bu/bv/bins
+void flag_updates(mf_ctx* c, int64_t m);           // c->bu/bv -> c->bins
+void compact_graph(mf_ctx* c, std::vector<int64_t>& nindex_out, std::vector<int32_t>& nlist_out);
+void rebase(mf_ctx* c);
+void greedy_mis(mf_ctx* c, uint8_t* d_out);
+void check_mis(mf_ctx* c, int64_t* viol, int64_t* uncovered);
+// mf_repair.cu
+void process_batch(mf_ctx* c, int64_t m);          // everything after the overlay apply
+int64_t initial_max_csr(int32_t n, uint64_t edges);
+}  // namespace mf

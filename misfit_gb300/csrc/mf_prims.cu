@@ -1,0 +1,259 @@
+// mf_prims.cu -- device scans and a stable LSD radix sort.
+//
+// Scans: three passes (tile reduce, scan of tile sums in one block, tile
+// rescan).  Tiles are 256 threads x 8 items, loaded striped for coalescing
+// and scanned per thread out of shared memory.
+// Radix sort: 8-bit digits, per-tile digit histograms, a scan over the
+// digit-major histogram and a stable scatter that ranks items inside a tile
+// with __match_any_sync.  Stability is what the callers rely on: equal keys
+// keep their input (value) order.
+#include "mf_internal.cuh"
+
+namespace mf {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 8;
+constexpr int kTile = kThreads * kItems;
+
+template <typename T>
+struct Loader {
+  const T* p;
+  __device__ __forceinline__ int64_t operator()(int64_t i) const { return (int64_t)p[i]; }
+};
+
+__device__ __forceinline__ int64_t block_sum(int64_t v, int64_t* smem_warp) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) smem_warp[w] = v;
+  __syncthreads();
+  int64_t t = 0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < (blockDim.x >> 5) ? smem_warp[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// Exclusive scan across the block of one value per thread; returns the
+// thread's prefix and writes the block total to *total.
+__device__ __forceinline__ int64_t block_exclusive(int64_t v, int64_t* smem_warp, int64_t* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int64_t inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) smem_warp[w] = inc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = blockDim.x >> 5;
+    int64_t x = threadIdx.x < nw ? smem_warp[threadIdx.x] : 0;
+    int64_t xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t t = __shfl_up_sync(0xffffffffu, xi, o);
+      if (threadIdx.x >= o) xi += t;
+    }
+    if (threadIdx.x < nw) smem_warp[threadIdx.x] = xi - x;
+    if (threadIdx.x == nw - 1) smem_warp[32] = xi;
+  }
+  __syncthreads();
+  const int64_t r = smem_warp[w] + inc - v;
+  *total = smem_warp[32];
+  __syncthreads();
+  return r;
+}
+
+template <typename L>
+__global__ void k_tile_reduce(L load, int64_t n, int64_t* sums) {
+  __shared__ int64_t sw[33];
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+  int64_t acc = 0;
+  for (int k = 0; k < kItems; ++k) {
+    const int64_t i = base + (int64_t)k * kThreads + threadIdx.x;
+    if (i < n) acc += load(i);
+  }
+  const int64_t t = block_sum(acc, sw);
+  if (threadIdx.x == 0) sums[blockIdx.x] = t;
+}
+
+// Single block: exclusive scan of sums[0..nb) in place, total to sums[nb].
+__global__ void k_scan_sums(int64_t* sums, int64_t nb) {
+  __shared__ int64_t sw[33];
+  int64_t carry = 0;
+  for (int64_t base = 0; base < nb; base += kTile) {
+    int64_t v[kItems];
+    int64_t local = 0;
+    for (int k = 0; k < kItems; ++k) {
+      const int64_t i = base + (int64_t)threadIdx.x * kItems + k;
+      v[k] = i < nb ? sums[i] : 0;
+      local += v[k];
+    }
+    int64_t tot;
+    int64_t pre = block_exclusive(local, sw, &tot) + carry;
+    for (int k = 0; k < kItems; ++k) {
+      const int64_t i = base + (int64_t)threadIdx.x * kItems + k;
+      if (i < nb) sums[i] = pre;
+      pre += v[k];
+    }
+    carry += tot;
+  }
+  if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+template <typename L>
+__global__ void k_tile_scan(L load, int64_t n, const int64_t* offs, int64_t* out) {
+  __shared__ int64_t tile[kTile];
+  __shared__ int64_t sw[33];
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+  for (int k = 0; k < kItems; ++k) {
+    const int idx = k * kThreads + threadIdx.x;
+    const int64_t i = base + idx;
+    tile[idx] = i < n ? load(i) : 0;
+  }
+  __syncthreads();
+  int64_t local = 0;
+  for (int k = 0; k < kItems; ++k) local += tile[threadIdx.x * kItems + k];
+  int64_t tot;
+  int64_t pre = block_exclusive(local, sw, &tot) + offs[blockIdx.x];
+  for (int k = 0; k < kItems; ++k) {
+    const int idx = threadIdx.x * kItems + k;
+    const int64_t v = tile[idx];
+    tile[idx] = pre;
+    pre += v;
+  }
+  __syncthreads();
+  for (int k = 0; k < kItems; ++k) {
+    const int idx = k * kThreads + threadIdx.x;
+    const int64_t i = base + idx;
+    if (i < n) out[i] = tile[idx];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = offs[gridDim.x];
+}
+
+template <typename L>
+void scan_exclusive(L load, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s) {
+  if (n <= 0) {
+    MF_CUDA(cudaMemsetAsync(out, 0, sizeof(int64_t), s));
+    return;
+  }
+  const int64_t nb = (n + kTile - 1) / kTile;
+  ws.block_sums.reserve(nb + 1);
+  k_tile_reduce<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p);
+  k_scan_sums<<<1, kThreads, 0, s>>>(ws.block_sums.p, nb);
+  k_tile_scan<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p, out);
+  MF_CUDA(cudaGetLastError());
+}
+
+// ---- radix sort --------------------------------------------------------------
+
+__global__ void k_radix_hist(const uint64_t* keys, int64_t n, int shift, int32_t* hist, int nblocks) {
+  __shared__ int32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+  for (int k = 0; k < kItems; ++k) {
+    const int64_t i = base + (int64_t)k * kThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_radix_scatter(const uint64_t* keys, const uint32_t* vals, int64_t n, int shift,
+                                const int64_t* offs, int nblocks, uint64_t* okeys, uint32_t* ovals) {
+  __shared__ int32_t wcnt[kThreads / 32][256];
+  __shared__ int32_t running[256];
+  __shared__ int32_t itotal[256];
+  __shared__ int64_t base_off[256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  base_off[threadIdx.x] = offs[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+  running[threadIdx.x] = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+  for (int k = 0; k < kItems; ++k) {
+    for (int j = 0; j < kThreads / 32; ++j) wcnt[j][threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t i = base + (int64_t)k * kThreads + threadIdx.x;
+    const bool valid = i < n;
+    uint64_t key = 0;
+    uint32_t val = 0;
+    int d = 256;
+    if (valid) {
+      key = keys[i];
+      val = vals[i];
+      d = (int)((key >> shift) & 255u);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int rank = __popc(peers & lt);
+    if (valid && rank == 0) wcnt[w][d] = __popc(peers);
+    __syncthreads();
+    {
+      int acc = 0;
+      for (int j = 0; j < kThreads / 32; ++j) {
+        const int t = wcnt[j][threadIdx.x];
+        wcnt[j][threadIdx.x] = acc;
+        acc += t;
+      }
+      itotal[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+      const int64_t pos = base_off[d] + running[d] + wcnt[w][d] + rank;
+      okeys[pos] = key;
+      ovals[pos] = val;
+    }
+    __syncthreads();
+    running[threadIdx.x] += itotal[threadIdx.x];
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+int bits_for(int64_t v) {
+  int b = 1;
+  while (b < 63 && (v >> b) != 0) ++b;
+  return b;
+}
+
+void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s) {
+  scan_exclusive(Loader<int64_t>{in}, out, n, ws, s);
+}
+void scan_exclusive_i32(const int32_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s) {
+  scan_exclusive(Loader<int32_t>{in}, out, n, ws, s);
+}
+void scan_exclusive_u8(const uint8_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s) {
+  scan_exclusive(Loader<uint8_t>{in}, out, n, ws, s);
+}
+
+void radix_sort_pairs(uint64_t* keys, uint32_t* vals, int64_t n, int bits, Scratch& ws, cudaStream_t s) {
+  if (n <= 1) return;
+  const int nblocks = (int)((n + kTile - 1) / kTile);
+  ws.keys_alt.reserve(n);
+  ws.vals_alt.reserve(n);
+  ws.hist.reserve((int64_t)256 * nblocks);
+  ws.hist_scan.reserve((int64_t)256 * nblocks + 1);
+  uint64_t* ka = keys;
+  uint32_t* va = vals;
+  uint64_t* kb = ws.keys_alt.p;
+  uint32_t* vb = ws.vals_alt.p;
+  const int passes = (bits + 7) / 8;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int shift = pass * 8;
+    k_radix_hist<<<nblocks, kThreads, 0, s>>>(ka, n, shift, ws.hist.p, nblocks);
+    scan_exclusive_i32(ws.hist.p, ws.hist_scan.p, (int64_t)256 * nblocks, ws, s);
+    k_radix_scatter<<<nblocks, kThreads, 0, s>>>(ka, va, n, shift, ws.hist_scan.p, nblocks, kb, vb);
+    MF_CUDA(cudaGetLastError());
+    uint64_t* tk = ka; ka = kb; kb = tk;
+    uint32_t* tv = va; va = vb; vb = tv;
+  }
+  if (ka != keys) {
+    MF_CUDA(cudaMemcpyAsync(keys, ka, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
+    MF_CUDA(cudaMemcpyAsync(vals, va, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+  }
+}
+
+}  // namespace mf

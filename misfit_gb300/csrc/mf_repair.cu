@@ -1,0 +1,764 @@
+// mf_repair.cu -- the per-sub-batch path on the device.
+//
+// Reference: GPUVertexClusteringGraph::processBatchWithVertexClustering
+// (src/misfit/misfit.cu:468-692) with its host stages (split :490-521,
+// 2-hop lists :527-558, row packing :560-599) and kernels (:211-358).
+//
+// The reference materialises every seed's exact 2-hop list on the host and
+// ships it to the GPU.  Nothing here materialises a 2-hop list: a seed row is
+// the virtual sequence  [s] ++ row(s) ++ row(h1) ++ row(h2) ++ ...  (h over
+// row(s) in order).  The first element with a property is the same in the
+// virtual sequence and in the de-duplicated BFS list, and set-valued queries
+// do not care about repeats, so clustering and repair read rows straight out
+// of the HBM CSR + overlay.  Only the split rule needs exact list lengths
+// (MAX_CSR_ELEMENTS grows when the packed lists overflow it); those are
+// counted exactly, and only when an upper bound says growth is possible.
+//
+// Canonical schedule for the racy kernels (the same the oracle uses):
+//   clustering bulk-synchronous (pre-kernel reads, new ids by ascending row,
+//   highest row writes last); assignment by ascending sub-batch index (lists
+//   walked descending); clusters processed in ascending id.
+#include <algorithm>
+#include <cstring>
+
+#include "mf_internal.cuh"
+
+namespace mf {
+
+int64_t initial_max_csr(int32_t n, uint64_t edges) {
+  // src/misfit/misfit.cu:768-772
+  double avg = n > 0 ? (double)edges / n : 1.0;
+  int64_t est = (int64_t)(kMaxBatchEdges * 2.0 * avg * avg);
+  int64_t v = est > 0 ? std::min<int64_t>(800000000LL, est) : 50000000LL;
+  return std::max<int64_t>(v, 1000000LL);
+}
+
+namespace {
+
+constexpr int kTB = 256;
+constexpr int32_t kSkip = -2;
+
+inline unsigned grid_for(int64_t n, int per = kTB) {
+  int64_t g = (n + per - 1) / per;
+  if (g < 1) g = 1;
+  return (unsigned)std::min<int64_t>(g, (int64_t)1 << 30);
+}
+inline unsigned warps_grid(int64_t items) { return grid_for(items * 32); }
+
+__device__ __forceinline__ int64_t warp_id() {
+  return ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+}
+
+// ---- split ------------------------------------------------------------------
+
+__global__ void k_slot_keys(const int32_t* u, const int32_t* v, int64_t m, int sbits, uint64_t* keys, uint32_t* vals) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * m) return;
+  const int32_t x = (i & 1) ? v[i >> 1] : u[i >> 1];
+  keys[i] = ((uint64_t)x << sbits) | (uint64_t)i;
+  vals[i] = (uint32_t)i;
+}
+
+__global__ void k_prev(const uint64_t* keys, const uint32_t* vals, int64_t cnt, int sbits, int32_t* prev) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cnt) return;
+  const uint32_t slot = vals[j];
+  int32_t pe = -1;
+  if (j > 0 && (keys[j - 1] >> sbits) == (keys[j] >> sbits)) pe = (int32_t)(vals[j - 1] >> 1);
+  prev[slot] = pe;
+}
+
+// Estimate added by each edge of a sub-batch starting at p
+// (src/misfit/misfit.cu:501-507): deg * 1000 for each endpoint not seen yet.
+__global__ void k_contrib(const int32_t* u, const int32_t* v, const int32_t* prev, const int32_t* deg,
+                          int64_t p, int64_t len, int64_t* out) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= len) return;
+  const int64_t j = p + t;
+  int64_t c = 0;
+  if (prev[2 * j] < p) c += (int64_t)deg[u[j]] * kEstimateWeight;
+  if (prev[2 * j + 1] < p) c += (int64_t)deg[v[j]] * kEstimateWeight;
+  out[t] = c;
+}
+
+// First edge t >= 1 whose running estimate reaches MAX_CSR_ELEMENTS
+// (src/misfit/misfit.cu:509-511); pex is the exclusive scan (len+1 entries).
+__global__ void k_find_cut(const int64_t* pex, int64_t len, int64_t maxcsr, unsigned long long* out) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 1 || t >= len) return;
+  if (pex[t + 1] >= maxcsr) atomicMin(out, (unsigned long long)t);
+}
+
+__global__ void k_seed_flags(const int32_t* prev, int64_t p, int64_t q, uint8_t* flags) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * (q - p)) return;
+  flags[i] = prev[2 * p + i] < p ? 1 : 0;
+}
+
+__global__ void k_seed_compact(const int32_t* u, const int32_t* v, const uint8_t* flags, const int64_t* pos,
+                               int64_t p, int64_t q, int32_t* seeds, int32_t* v2i) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * (q - p) || !flags[i]) return;
+  const int64_t slot = 2 * p + i;
+  const int32_t x = (slot & 1) ? v[slot >> 1] : u[slot >> 1];
+  const int64_t k = pos[i];
+  seeds[k] = x;
+  v2i[x] = (int32_t)k;
+}
+
+// ---- hop-1 set and candidates ---------------------------------------------------
+
+__global__ void k_mark_hop1(GraphView g, const int32_t* seeds, int64_t ns, uint32_t epoch, uint32_t* hmark,
+                            int32_t* hlist, unsigned long long* count) {
+  const int64_t w = warp_id();
+  if (w >= ns) return;
+  const int32_t s = seeds[w];
+  warp_row_each(g, s, [&](int32_t y) {
+    if (atomicExch(hmark + y, epoch) != epoch) hlist[atomicAdd(count, 1ull)] = y;
+  });
+}
+
+__global__ void k_cand_flags(const uint32_t* hmark, const int32_t* v2i, int32_t n, uint32_t epoch, uint8_t* flags) {
+  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < n) flags[x] = (hmark[x] == epoch && v2i[x] < 0) ? 1 : 0;
+}
+
+__global__ void k_cand_compact(const uint8_t* flags, const int64_t* pos, int32_t n, int64_t cap, int64_t ns,
+                               int32_t* cands, int32_t* v2i) {
+  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n || !flags[x]) return;
+  const int64_t k = pos[x];
+  if (k >= cap) return;
+  cands[k] = (int32_t)x;
+  v2i[x] = (int32_t)(ns + k);
+}
+
+// ---- packed sizes ---------------------------------------------------------------
+
+// Upper bound of the packed element count: 1 + len(s) + sum of len(h) per seed
+// (capped by n), plus the candidate row lengths.
+__global__ void k_size_bound(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct,
+                             unsigned long long* out) {
+  const int64_t w = warp_id();
+  const int lane = threadIdx.x & 31;
+  if (w < ns) {
+    const int32_t s = seeds[w];
+    int64_t acc = 0;
+    warp_row_each(g, s, [&](int32_t y) { acc += row_len(g, y); });
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      int64_t b = 1 + row_len(g, s) + acc;
+      if (b > g.n) b = g.n;
+      atomicAdd(out, (unsigned long long)b);
+    }
+  } else if (w < ns + nct) {
+    if (lane == 0) atomicAdd(out, (unsigned long long)row_len(g, cands[w - ns]));
+  }
+}
+
+// Exact |2-hop list| of each seed: each CTA owns a bitmap of n bits in global
+// memory, sets the bits of the virtual sequence, counts newly set bits, then
+// clears the words it touched.
+__global__ void __launch_bounds__(512) k_two_hop_sizes(GraphView g, const int32_t* seeds, int64_t ns,
+                                                       uint32_t* bitmaps, int64_t words, int64_t* lens) {
+  uint32_t* bm = bitmaps + (int64_t)blockIdx.x * words;
+  __shared__ unsigned long long s_cnt;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t i = blockIdx.x; i < ns; i += gridDim.x) {
+    const int32_t s = seeds[i];
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    unsigned long long local = 0;
+    auto setbit = [&](int32_t y) {
+      const uint32_t bit = 1u << (y & 31);
+      const uint32_t old = atomicOr(bm + (y >> 5), bit);
+      if (!(old & bit)) ++local;
+    };
+    if (threadIdx.x == 0) setbit(s);
+    const int64_t b = g.nindex[s], e = g.nindex[s + 1];
+    const bool filt = g.dead[s] != 0;
+    const int64_t nb = e - b, na = g.aoff[s + 1] - g.aoff[s];
+    for (int64_t k = threadIdx.x; k < nb + na; k += blockDim.x) {
+      if (k < nb) {
+        if (!filt || live_at(g.live, b + k)) setbit(g.nlist[b + k]);
+      } else {
+        setbit(g.aadj[g.aoff[s] + (k - nb)]);
+      }
+    }
+    for (int64_t k = wid; k < nb + na; k += nw) {
+      int32_t h;
+      if (k < nb) {
+        if (filt && !live_at(g.live, b + k)) continue;
+        h = g.nlist[b + k];
+      } else {
+        h = g.aadj[g.aoff[s] + (k - nb)];
+      }
+      warp_row_each(g, h, setbit);
+    }
+    atomicAdd(&s_cnt, local);
+    __syncthreads();
+    if (threadIdx.x == 0) lens[i] = (int64_t)s_cnt;
+    // clear
+    auto clr = [&](int32_t y) { bm[y >> 5] = 0u; };
+    if (threadIdx.x == 0) clr(s);
+    for (int64_t k = threadIdx.x; k < nb + na; k += blockDim.x) {
+      if (k < nb) clr(g.nlist[b + k]);
+      else clr(g.aadj[g.aoff[s] + (k - nb)]);
+    }
+    for (int64_t k = wid; k < nb + na; k += nw) {
+      int32_t h = k < nb ? g.nlist[b + k] : g.aadj[g.aoff[s] + (k - nb)];
+      warp_row_each(g, h, clr);
+    }
+    (void)lane;
+    __syncthreads();
+  }
+}
+
+__global__ void k_cand_lens(GraphView g, const int32_t* cands, int64_t nct, int64_t* lens) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nct) lens[k] = row_len(g, cands[k]);
+}
+
+// Growth of MAX_CSR_ELEMENTS while packing rows in order
+// (src/misfit/misfit.cu:565-568): whenever a row's end offset reaches the
+// limit, the limit becomes 1.5x that end offset.  io[0] = limit in/out,
+// io[1] = packed total out.
+__global__ void k_growth(const int64_t* pex, int64_t rows, int64_t* io) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t cur = io[0];
+  int64_t start = 0;
+  while (start < rows) {
+    int64_t lo = start, hi = rows;  // first i >= start with pex[i+1] >= cur
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (pex[mid + 1] >= cur) hi = mid; else lo = mid + 1;
+    }
+    if (lo >= rows) break;
+    const int64_t end = pex[lo + 1];
+    cur = (int64_t)((double)(uint64_t)end * 1.5);
+    start = lo + 1;
+  }
+  io[0] = cur;
+  io[1] = pex[rows];
+}
+
+// ---- clustering ------------------------------------------------------------------
+
+// f1[x] = cluster id of the first element of row(x) that has one (-1: none).
+__global__ void k_first_cid(GraphView g, const int32_t* list, int64_t cnt, const int32_t* cid, int32_t* f1) {
+  const int64_t w = warp_id();
+  if (w >= cnt) return;
+  const int32_t x = list[w];
+  int32_t y = -1;
+  const bool hit = warp_row_first(g, x, [&](int32_t z) { return cid[z] != -1; }, &y);
+  if ((threadIdx.x & 31) == 0) f1[x] = hit ? cid[y] : -1;
+}
+
+// Per row: early return when the row's own vertex already has an id
+// (src/misfit/misfit.cu:224), else the first existing id in row order or a
+// new one.  Seeds scan [s] ++ row(s) ++ row(h)...: f1(s), then f1(h) in order.
+__global__ void k_row_decide(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct,
+                             const int32_t* cid, const int32_t* f1, int32_t* rowcid, uint8_t* creates) {
+  const int64_t w = warp_id();
+  const int lane = threadIdx.x & 31;
+  if (w >= ns + nct) return;
+  const bool is_seed = w < ns;
+  const int32_t x = is_seed ? seeds[w] : cands[w - ns];
+  if (cid[x] != -1) {
+    if (lane == 0) { rowcid[w] = kSkip; creates[w] = 0; }
+    return;
+  }
+  int32_t fe = f1[x];
+  if (fe == -1 && is_seed) {
+    int32_t h = -1;
+    if (warp_row_first(g, x, [&](int32_t z) { return f1[z] != -1; }, &h)) fe = f1[h];
+  }
+  if (lane == 0) {
+    rowcid[w] = fe;
+    creates[w] = fe == -1 ? 1 : 0;
+  }
+}
+
+__global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < rows && rowcid[i] == -1) rowcid[i] = (int32_t)pos[i];
+}
+
+// Phase 1: bval[y] = max tag of the non-skipped seed rows with y in {s} u row(s).
+__global__ void k_push_seed(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* rowcid, uint32_t epoch,
+                            uint32_t* bval) {
+  const int64_t w = warp_id();
+  if (w >= ns || rowcid[w] == kSkip) return;
+  const int32_t s = seeds[w];
+  const uint32_t tag = (epoch << kRowBits) | (uint32_t)w;
+  if ((threadIdx.x & 31) == 0) atomicMax(bval + s, tag);
+  warp_row_each(g, s, [&](int32_t y) { atomicMax(bval + y, tag); });
+}
+
+__device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag, uint32_t epoch, int32_t* touched,
+                                       unsigned long long* tcount) {
+  const uint32_t old = atomicMax(wval + y, tag);
+  if ((old >> kRowBits) != epoch) touched[atomicAdd(tcount, 1ull)] = y;
+}
+
+// Phase 2: wval[y] = max over x with y in {x} u row(x) of bval[x] (2-hop reach
+// of the seed rows), then the candidate rows' own tags over row(c).
+__global__ void k_push_hop(GraphView g, const int32_t* list, int64_t cnt, uint32_t epoch, const uint32_t* bval,
+                           uint32_t* wval, int32_t* touched, unsigned long long* tcount) {
+  const int64_t w = warp_id();
+  if (w >= cnt) return;
+  const int32_t x = list[w];
+  const uint32_t t = bval[x];
+  if ((t >> kRowBits) != epoch) return;
+  if ((threadIdx.x & 31) == 0) push_w(wval, x, t, epoch, touched, tcount);
+  warp_row_each(g, x, [&](int32_t y) { push_w(wval, y, t, epoch, touched, tcount); });
+}
+
+__global__ void k_push_cand(GraphView g, const int32_t* cands, int64_t nct, int64_t ns, const int32_t* rowcid,
+                            uint32_t epoch, uint32_t* wval, int32_t* touched, unsigned long long* tcount) {
+  const int64_t w = warp_id();
+  if (w >= nct || rowcid[ns + w] == kSkip) return;
+  const uint32_t tag = (epoch << kRowBits) | (uint32_t)(ns + w);
+  warp_row_each(g, cands[w], [&](int32_t y) { push_w(wval, y, tag, epoch, touched, tcount); });
+}
+
+__global__ void k_finalize_cid(const int32_t* touched, int64_t cnt, const uint32_t* wval, const int32_t* rowcid,
+                               int32_t* cid) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= cnt) return;
+  const int32_t y = touched[k];
+  cid[y] = rowcid[wval[y] & kRowMask];
+}
+
+// ---- assignment and order ------------------------------------------------------------
+
+__global__ void k_assign(const int32_t* u, const int32_t* v, int64_t p, int64_t len, const int32_t* cid,
+                         int64_t limit, uint64_t* keys, uint32_t* vals, unsigned long long* count) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= len) return;
+  const int64_t j = p + t;
+  int32_t c = cid[u[j]];
+  if (c == -1) c = cid[v[j]];
+  if (c < 0 || (int64_t)c >= limit) return;
+  const unsigned long long k = atomicAdd(count, 1ull);
+  keys[k] = ((uint64_t)c << kRowBits) | (uint64_t)(kRowMask - (uint32_t)t);
+  vals[k] = (uint32_t)t;
+}
+
+// ---- repair -------------------------------------------------------------------------------
+
+struct RepairArgs {
+  GraphView g;
+  const int32_t* u;
+  const int32_t* v;
+  const uint8_t* ins;
+  int64_t p;
+  const uint32_t* order;
+  int64_t cnt;
+  int64_t ns;
+  const int32_t* v2i;
+  uint8_t* mis;
+};
+
+__device__ __forceinline__ bool is_seed_row(const RepairArgs& a, int32_t x) {
+  const int32_t i = a.v2i[x];
+  return i >= 0 && (int64_t)i < a.ns;
+}
+
+// any z in row-of(x) with mis[z] and z != except, one thread.
+__device__ bool thread_any_member(const RepairArgs& a, int32_t x, int32_t except) {
+  const GraphView& g = a.g;
+  const uint8_t* mis = a.mis;
+  auto hit = [&](int32_t z) { return z != except && mis[z] != 0; };
+  if (!is_seed_row(a, x)) return thread_row_until(g, x, hit);
+  if (hit(x)) return true;
+  if (thread_row_until(g, x, hit)) return true;
+  return thread_row_until(g, x, [&](int32_t h) { return thread_row_until(g, h, hit); });
+}
+
+// Q(w) of the insertion rule (src/misfit/misfit.cu:300-313).
+__device__ bool eligible(const RepairArgs& a, int32_t w) {
+  if (a.mis[w]) return false;
+  if (a.v2i[w] < 0) return false;
+  return !thread_any_member(a, w, -1);
+}
+
+// Element k of row(x) (base positions first, then added), or -1 if tombstoned.
+__device__ __forceinline__ int32_t row_elem(const GraphView& g, int32_t x, int64_t k, int64_t nb) {
+  if (k < nb) {
+    const int64_t gk = g.nindex[x] + k;
+    if (g.dead[x] != 0 && !live_at(g.live, gk)) return -1;
+    return g.nlist[gk];
+  }
+  return g.aadj[g.aoff[x] + (k - nb)];
+}
+
+// Single CTA walks the repair order; per chunk of 1024 edges it finds the next
+// edge whose endpoint states call for work, evaluates it with the whole block,
+// and repeats.  Exact sequential semantics of the canonical schedule.
+// Shared flags are read into registers between two barriers so that every
+// thread takes the same branch; warp loops exit on warp-uniform votes.
+__global__ void __launch_bounds__(1024) k_repair_sequential(RepairArgs a) {
+  __shared__ int s_first;
+  __shared__ int s_act;        // 1 insert, 2 delete
+  __shared__ int32_t s_x, s_keep;
+  __shared__ unsigned long long s_best;
+  __shared__ int s_flag;
+  const GraphView& g = a.g;
+  uint8_t* mis = a.mis;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  for (int64_t base = 0; base < a.cnt; base += blockDim.x) {
+    const int64_t idx = base + tid;
+    int32_t eu = 0, ev = 0;
+    bool eins = false;
+    const bool valid = idx < a.cnt;
+    if (valid) {
+      const int64_t j = a.p + a.order[idx];
+      eu = a.u[j];
+      ev = a.v[j];
+      eins = a.ins[j] != 0;
+    }
+    int start = 0;
+    while (true) {
+      if (tid == 0) s_first = 1 << 30;
+      __syncthreads();
+      if (valid && tid >= start) {
+        const bool mu = mis[eu] != 0, mv = mis[ev] != 0;
+        if (eins ? (mu && mv) : (mu != mv)) atomicMin(&s_first, tid);
+      }
+      __syncthreads();
+      const int first = s_first;
+      if (first >= (int)blockDim.x) break;
+      if (tid == first) {
+        const bool mu = mis[eu] != 0;
+        if (eins) {
+          const int32_t r = eu > ev ? eu : ev;
+          mis[r] = 0;
+          s_act = 1;
+          s_x = r;
+        } else {
+          s_act = 2;
+          s_x = mu ? ev : eu;     // the endpoint that may join
+          s_keep = mu ? eu : ev;  // the endpoint in the set
+        }
+        s_best = ~0ull;
+        s_flag = 0;
+      }
+      __syncthreads();
+      const int act = s_act;
+      const int32_t x = s_x, keep = s_keep;
+      if (act == 1 && a.v2i[x] >= 0) {
+        // Insertion rule: first eligible w of row-of(r) in order.  Position
+        // keys: 0 = r itself, 1 + k = row(r)[k], hop-2 = 2^62 + (k << 32) + j.
+        const int32_t r = x;
+        const bool seed = is_seed_row(a, r);
+        if (tid == 0 && seed && eligible(a, r)) atomicMin(&s_best, 0ull);
+        const int64_t nb = g.nindex[r + 1] - g.nindex[r];
+        const int64_t nr = nb + (g.aoff[r + 1] - g.aoff[r]);
+        for (int64_t k = tid; k < nr; k += blockDim.x) {
+          const int32_t w = row_elem(g, r, k, nb);
+          if (w >= 0 && eligible(a, w)) atomicMin(&s_best, 1ull + (unsigned long long)k);
+        }
+        __syncthreads();
+        bool done = s_best != ~0ull;
+        __syncthreads();
+        if (!done && seed) {
+          for (int64_t k0 = 0; k0 < nr; k0 += nw) {
+            const int64_t k = k0 + wid;
+            const int32_t h = k < nr ? row_elem(g, r, k, nb) : -1;
+            if (h >= 0) {
+              const int64_t hb = g.nindex[h + 1] - g.nindex[h];
+              const int64_t hn = hb + (g.aoff[h + 1] - g.aoff[h]);
+              for (int64_t j0 = 0; j0 < hn; j0 += 32) {
+                const int64_t jj = j0 + lane;
+                bool ok = false;
+                if (jj < hn) {
+                  const int32_t w = row_elem(g, h, jj, hb);
+                  ok = w >= 0 && eligible(a, w);
+                }
+                const unsigned msk = __ballot_sync(0xffffffffu, ok);
+                if (msk) {
+                  if (lane == 0)
+                    atomicMin(&s_best, (1ull << 62) + ((unsigned long long)k << 32) +
+                                           (unsigned long long)(j0 + __ffs(msk) - 1));
+                  break;
+                }
+              }
+            }
+            __syncthreads();
+            done = s_best != ~0ull;
+            __syncthreads();
+            if (done) break;
+          }
+        }
+        if (tid == 0 && s_best != ~0ull) {
+          const unsigned long long key = s_best;
+          int32_t w;
+          if (key == 0) {
+            w = r;
+          } else if (key < (1ull << 62)) {
+            w = row_elem(g, r, (int64_t)(key - 1), nb);
+          } else {
+            const int64_t k = (int64_t)((key - (1ull << 62)) >> 32);
+            const int64_t jj = (int64_t)(key & 0xffffffffull);
+            const int32_t h = row_elem(g, r, k, nb);
+            w = row_elem(g, h, jj, g.nindex[h + 1] - g.nindex[h]);
+          }
+          mis[w] = 1;
+        }
+      } else if (act == 2) {
+        // Deletion rule: y joins unless row-of(y) holds a member other than keep.
+        const int32_t y = x;
+        if (a.v2i[y] < 0) {
+          if (tid == 0) mis[y] = 1;
+        } else {
+          const bool seed = is_seed_row(a, y);
+          auto hit = [&](int32_t z) { return z != keep && mis[z] != 0; };
+          bool found = tid == 0 && seed && hit(y);
+          const int64_t nb = g.nindex[y + 1] - g.nindex[y];
+          const int64_t ny = nb + (g.aoff[y + 1] - g.aoff[y]);
+          for (int64_t k = tid; k < ny && !found; k += blockDim.x) {
+            const int32_t z = row_elem(g, y, k, nb);
+            if (z >= 0 && hit(z)) found = true;
+          }
+          if (found) s_flag = 1;
+          __syncthreads();
+          const bool done = s_flag != 0;
+          __syncthreads();
+          if (!done && seed) {
+            for (int64_t k = wid; k < ny; k += nw) {
+              const int32_t h = row_elem(g, y, k, nb);
+              bool f = false;
+              if (h >= 0) {
+                const int64_t hb = g.nindex[h + 1] - g.nindex[h];
+                const int64_t hn = hb + (g.aoff[h + 1] - g.aoff[h]);
+                for (int64_t j0 = 0; j0 < hn; j0 += 32) {
+                  const int64_t jj = j0 + lane;
+                  bool ok = false;
+                  if (jj < hn) {
+                    const int32_t z = row_elem(g, h, jj, hb);
+                    ok = z >= 0 && hit(z);
+                  }
+                  if (__any_sync(0xffffffffu, ok)) { f = true; break; }
+                  if (__any_sync(0xffffffffu, *(volatile int*)&s_flag != 0)) break;
+                }
+              }
+              if (f && lane == 0) s_flag = 1;
+              if (__any_sync(0xffffffffu, f || *(volatile int*)&s_flag != 0)) break;
+            }
+          }
+          __syncthreads();
+          if (tid == 0 && !s_flag) mis[y] = 1;
+        }
+      }
+      __syncthreads();
+      start = first + 1;
+    }
+  }
+}
+
+__global__ void k_clear(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, int32_t* cid,
+                        int32_t* v2i) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns + nct) return;
+  const int32_t x = i < ns ? seeds[i] : cands[i - ns];
+  cid[x] = -1;
+  v2i[x] = -1;
+}
+
+template <typename T>
+std::vector<T> fetch(const T* d, int64_t cnt, cudaStream_t s) {
+  std::vector<T> h((size_t)std::max<int64_t>(cnt, 0));
+  if (cnt > 0) MF_CUDA(cudaMemcpyAsync(h.data(), d, sizeof(T) * (size_t)cnt, cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
+  return h;
+}
+
+void next_epoch(mf_ctx* c) {
+  if (c->epoch >= kMaxEpoch) {
+    cudaStream_t s = c->stream;
+    MF_CUDA(cudaMemsetAsync(c->hmark.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
+    MF_CUDA(cudaMemsetAsync(c->bval.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
+    MF_CUDA(cudaMemsetAsync(c->wval.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
+    c->epoch = 0;
+  }
+  ++c->epoch;
+}
+
+}  // namespace
+
+void process_batch(mf_ctx* c, int64_t m) {
+  cudaStream_t s = c->stream;
+  const int32_t n = c->n;
+  const GraphView g = c->view();
+  int64_t* cnt = c->counters.p;
+  unsigned long long* ucnt = reinterpret_cast<unsigned long long*>(cnt);
+  int64_t* h = c->h_counters;
+
+  // previous occurrence of every endpoint slot (for "not seen in this sub-batch")
+  const int sbits = bits_for(std::max<int64_t>(2 * m - 1, 1));
+  const int nbits = bits_for(std::max<int32_t>(n - 1, 1));
+  c->keys.reserve(2 * m);
+  c->vals.reserve(2 * m);
+  c->prev.reserve(2 * m);
+  k_slot_keys<<<grid_for(2 * m), kTB, 0, s>>>(c->bu.p, c->bv.p, m, sbits, c->keys.p, c->vals.p);
+  radix_sort_pairs(c->keys.p, c->vals.p, 2 * m, sbits + nbits, c->ws, s);
+  k_prev<<<grid_for(2 * m), kTB, 0, s>>>(c->keys.p, c->vals.p, 2 * m, sbits, c->prev.p);
+  MF_CUDA(cudaGetLastError());
+
+  const int64_t big = 2 * std::min<int64_t>(m, kMaxBatchEdges) + (int64_t)n + 2;
+  c->i64a.reserve(big);
+  c->i64b.reserve(big);
+  c->u8a.reserve(big);
+  c->seeds.reserve(2 * std::min<int64_t>(m, kMaxBatchEdges));
+  c->cands.reserve(kMaxRows);
+  c->rowcid.reserve(kMaxRows + 2 * std::min<int64_t>(m, kMaxBatchEdges));
+  c->creates.reserve(kMaxRows + 2 * std::min<int64_t>(m, kMaxBatchEdges));
+  c->rowlens.reserve(kMaxRows + 2 * std::min<int64_t>(m, kMaxBatchEdges) + 1);
+
+  int64_t p = 0;
+  while (p < m) {
+    const int64_t len = std::min<int64_t>(m - p, kMaxBatchEdges);
+    // ---- split
+    k_contrib<<<grid_for(len), kTB, 0, s>>>(c->bu.p, c->bv.p, c->prev.p, c->deg.p, p, len, c->i64a.p);
+    scan_exclusive_i64(c->i64a.p, c->i64b.p, len, c->ws, s);
+    const int64_t lenv = len;
+    MF_CUDA(cudaMemcpyAsync(cnt, &lenv, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    k_find_cut<<<grid_for(len), kTB, 0, s>>>(c->i64b.p, len, c->max_csr, ucnt);
+    MF_CUDA(cudaMemcpyAsync(h, cnt, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t q = p + h[0];
+    int64_t est = 0;
+    MF_CUDA(cudaMemcpyAsync(&est, c->i64b.p + (q - p), sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+
+    // ---- seeds (first appearance)
+    const int64_t nslots = 2 * (q - p);
+    k_seed_flags<<<grid_for(nslots), kTB, 0, s>>>(c->prev.p, p, q, c->u8a.p);
+    scan_exclusive_u8(c->u8a.p, c->i64a.p, nslots, c->ws, s);
+    k_seed_compact<<<grid_for(nslots), kTB, 0, s>>>(c->bu.p, c->bv.p, c->u8a.p, c->i64a.p, p, q, c->seeds.p, c->v2i.p);
+    MF_CUDA(cudaMemcpyAsync(h + 1, c->i64a.p + nslots, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t ns = h[1];
+
+    // ---- hop-1 set, candidates in ascending id
+    next_epoch(c);
+    const uint32_t ep = c->epoch;
+    MF_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int64_t), s));
+    k_mark_hop1<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->hmark.p, c->hlist.p, ucnt + 2);
+    k_cand_flags<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->v2i.p, n, ep, c->u8a.p);
+    scan_exclusive_u8(c->u8a.p, c->i64a.p, n, c->ws, s);
+    const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
+    k_cand_compact<<<grid_for(n), kTB, 0, s>>>(c->u8a.p, c->i64a.p, n, capc, ns, c->cands.p, c->v2i.p);
+    MF_CUDA(cudaMemcpyAsync(h + 3, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaMemcpyAsync(h + 2, cnt + 2, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t nh = h[2];
+    const int64_t nct = std::min<int64_t>(h[3], capc);
+    const int64_t rows = ns + nct;
+
+    // ---- packed sizes and MAX_CSR_ELEMENTS growth
+    MF_CUDA(cudaMemsetAsync(cnt + 4, 0, sizeof(int64_t), s));
+    k_size_bound<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, ucnt + 4);
+    MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    int64_t packed = -1;
+    const bool exact = h[4] >= c->max_csr;
+    if (exact) {
+      if (c->bitmap_ctas == 0 || c->bitmap_words != ((int64_t)n + 31) / 32) {
+        c->bitmap_words = ((int64_t)n + 31) / 32;
+        int sms = 0;
+        MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+        const int64_t budget = (int64_t)1 << 31;  // bytes for the per-CTA bitmaps
+        int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 2, budget / (c->bitmap_words * 4)));
+        c->bitmap_ctas = (int)ctas;
+        c->bitmaps.release();
+        c->bitmaps.reserve(ctas * c->bitmap_words);
+        MF_CUDA(cudaMemsetAsync(c->bitmaps.p, 0, sizeof(uint32_t) * (size_t)(ctas * c->bitmap_words), s));
+      }
+      if (ns > 0)
+        k_two_hop_sizes<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ns), 512, 0, s>>>(
+            g, c->seeds.p, ns, c->bitmaps.p, c->bitmap_words, c->rowlens.p);
+      k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns);
+      scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
+      h[5] = c->max_csr;
+      MF_CUDA(cudaMemcpyAsync(cnt + 5, h + 5, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+      k_growth<<<1, 32, 0, s>>>(c->i64a.p, rows, cnt + 5);
+      MF_CUDA(cudaMemcpyAsync(h + 5, cnt + 5, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaStreamSynchronize(s));
+      c->max_csr = h[5];
+      packed = h[6];
+      c->stats.exact_sizes += 1;
+    }
+    MF_CUDA(cudaGetLastError());
+
+    // ---- clustering (bulk-synchronous)
+    k_first_cid<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->cid.p, c->f1.p);
+    k_first_cid<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, c->cid.p, c->f1.p);
+    k_row_decide<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->f1.p,
+                                                  c->rowcid.p, c->creates.p);
+    scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
+    k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p);
+    MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    k_push_seed<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->rowcid.p, ep, c->bval.p);
+    MF_CUDA(cudaMemsetAsync(cnt + 8, 0, sizeof(int64_t), s));
+    k_push_hop<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8);
+    k_push_hop<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8);
+    k_push_cand<<<warps_grid(nct), kTB, 0, s>>>(g, c->cands.p, nct, ns, c->rowcid.p, ep, c->wval.p, c->touched.p,
+                                                ucnt + 8);
+    MF_CUDA(cudaMemcpyAsync(h + 8, cnt + 8, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t cc = h[7];
+    const int64_t ntouched = h[8];
+    k_finalize_cid<<<grid_for(ntouched), kTB, 0, s>>>(c->touched.p, ntouched, c->wval.p, c->rowcid.p, c->cid.p);
+    MF_CUDA(cudaGetLastError());
+
+    SubBatchTrace* tr = nullptr;
+    if (c->trace) {
+      c->traces.emplace_back();
+      tr = &c->traces.back();
+      tr->hdr[0] = p; tr->hdr[1] = q; tr->hdr[2] = ns; tr->hdr[3] = nct; tr->hdr[4] = packed;
+      tr->hdr[5] = c->max_csr; tr->hdr[6] = cc; tr->hdr[8] = rows; tr->hdr[9] = est;
+      tr->seeds = fetch(c->seeds.p, ns, s);
+      tr->cands = fetch(c->cands.p, nct, s);
+      tr->cid_after = fetch(c->cid.p, n, s);
+      if (exact) tr->row_len = fetch(c->rowlens.p, rows, s);
+    }
+
+    // ---- assignment + order (cluster ascending, index descending)
+    const int64_t limit = std::min<int64_t>(cc, kMaxBatchEdges);
+    MF_CUDA(cudaMemsetAsync(cnt + 9, 0, sizeof(int64_t), s));
+    k_assign<<<grid_for(q - p), kTB, 0, s>>>(c->bu.p, c->bv.p, p, q - p, c->cid.p, limit, c->keys.p, c->vals.p, ucnt + 9);
+    MF_CUDA(cudaMemcpyAsync(h + 9, cnt + 9, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t nproc = h[9];
+    radix_sort_pairs(c->keys.p, c->vals.p, nproc, kRowBits + bits_for(std::max<int64_t>(limit, 1)), c->ws, s);
+
+    // ---- repair
+    if (nproc > 0) {
+      RepairArgs ra{g, c->bu.p, c->bv.p, c->bins.p, p, c->vals.p, nproc, ns, c->v2i.p, c->mis.p};
+      k_repair_sequential<<<1, 1024, 0, s>>>(ra);
+      MF_CUDA(cudaGetLastError());
+    }
+    if (tr) {
+      tr->hdr[7] = nproc;
+      std::vector<uint32_t> ord = fetch(c->vals.p, nproc, s);
+      tr->order.resize(ord.size());
+      for (size_t i = 0; i < ord.size(); ++i) tr->order[i] = (int32_t)(p + ord[i]);
+      tr->mis_after = fetch(c->mis.p, n, s);
+    }
+
+    // ---- clear (mapped vertices only)
+    k_clear<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->v2i.p);
+    MF_CUDA(cudaGetLastError());
+
+    c->stats.sub_batches += 1;
+    c->stats.seeds += ns;
+    c->stats.candidates += nct;
+    c->stats.clusters += cc;
+    c->stats.processed_edges += nproc;
+    p = q;
+  }
+  c->stats.max_csr = c->max_csr;
+}
+
+}  // namespace mf

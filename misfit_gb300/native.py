@@ -1,0 +1,304 @@
+"""ctypes binding of libmisfit_gb (include/misfit_gb.h).
+
+This is the reference-side binding a Python caller would add: one class per
+graph context, numpy arrays in and out.  It loads the in-tree library built
+by ``misfit_gb300/build.py`` and raises immediately when it is missing --
+there is no fallback implementation.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libmisfit_gb.so")
+
+# the symbols include/misfit_gb.h declares
+EXPORTS = [
+    "mf_version", "mf_status_string", "mf_last_error", "mf_open_egr", "mf_open_csr", "mf_close",
+    "mf_num_nodes", "mf_num_base_entries", "mf_set_mis", "mf_get_mis", "mf_mis_size", "mf_greedy_mis",
+    "mf_flag_updates", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_sync",
+    "mf_last_batch_stats", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
+    "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_compact", "mf_read_mis_file",
+    "mf_write_mis_file", "mf_read_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
+    "mf_trace_count", "mf_trace_get",
+]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("updates", C.c_int64), ("sub_batches", C.c_int64), ("seeds", C.c_int64),
+        ("candidates", C.c_int64), ("clusters", C.c_int64), ("processed_edges", C.c_int64),
+        ("exact_sizes", C.c_int64), ("max_csr", C.c_int64), ("repair_rounds", C.c_int64),
+        ("device_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class MisfitError(RuntimeError):
+    def __init__(self, status, what):
+        super().__init__("%s (status %d): %s" % (what, status, _lib().mf_last_error().decode()))
+        self.status = status
+
+
+_LIB = None
+
+_P = C.c_void_p
+_I32P = C.POINTER(C.c_int32)
+_I64P = C.POINTER(C.c_int64)
+_U8P = C.POINTER(C.c_uint8)
+
+
+def _lib():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libmisfit_gb.so is not built (%s); run misfit_gb300/build.py" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    sig = {
+        "mf_version": (C.c_int, []),
+        "mf_status_string": (C.c_char_p, [C.c_int]),
+        "mf_last_error": (C.c_char_p, []),
+        "mf_open_egr": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
+        "mf_open_csr": (C.c_int, [C.c_int32, _I64P, _I32P, C.c_int, C.POINTER(_P)]),
+        "mf_close": (C.c_int, [_P]),
+        "mf_num_nodes": (C.c_int, [_P, _I32P]),
+        "mf_num_base_entries": (C.c_int, [_P, _I64P]),
+        "mf_set_mis": (C.c_int, [_P, _U8P, C.c_int64]),
+        "mf_get_mis": (C.c_int, [_P, _U8P, C.c_int64]),
+        "mf_mis_size": (C.c_int, [_P, _I64P]),
+        "mf_greedy_mis": (C.c_int, [_P, _U8P, C.c_int64]),
+        "mf_flag_updates": (C.c_int, [_P, _I32P, _I32P, C.c_int64, _U8P]),
+        "mf_apply_batch": (C.c_int, [_P, _I32P, _I32P, _U8P, C.c_int64]),
+        "mf_apply_batch_device": (C.c_int, [_P, _P, _P, _P, C.c_int64]),
+        "mf_apply_batch_async": (C.c_int, [_P, _I32P, _I32P, _U8P, C.c_int64]),
+        "mf_sync": (C.c_int, [_P]),
+        "mf_last_batch_stats": (C.c_int, [_P, C.POINTER(BatchStats)]),
+        "mf_get_row": (C.c_int, [_P, C.c_int32, _I32P, C.c_int64, _I64P]),
+        "mf_get_degrees": (C.c_int, [_P, _I32P, C.c_int64]),
+        "mf_is_adjacent": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int)]),
+        "mf_get_max_csr": (C.c_int, [_P, _I64P]),
+        "mf_set_max_csr": (C.c_int, [_P, C.c_int64]),
+        "mf_get_cluster_ids": (C.c_int, [_P, _I32P, C.c_int64]),
+        "mf_check_mis": (C.c_int, [_P, _I64P, _I64P]),
+        "mf_compact": (C.c_int, [_P, C.c_char_p, C.c_int]),
+        "mf_read_mis_file": (C.c_int, [C.c_char_p, C.c_int32, _U8P, _I64P]),
+        "mf_write_mis_file": (C.c_int, [C.c_char_p, _U8P, C.c_int32]),
+        "mf_read_batch_file": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(_I32P), C.POINTER(_I32P), _I64P]),
+        "mf_list_batch_files": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), _I64P]),
+        "mf_free": (None, [C.c_void_p]),
+        "mf_trace_enable": (C.c_int, [_P, C.c_int]),
+        "mf_trace_count": (C.c_int, [_P, _I64P]),
+        "mf_trace_get": (C.c_int, [_P, C.c_int64, C.c_int, C.c_void_p, C.c_int64, _I64P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def load_library():
+    """Load libmisfit_gb.so (raises ImportError when it is not built)."""
+    return _lib()
+
+
+def _check(status, what):
+    if status != 0:
+        raise MisfitError(status, what)
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _u8(a):
+    return np.ascontiguousarray(a, dtype=np.uint8)
+
+
+_TRACE_FIELDS = {0: np.int64, 1: np.int32, 2: np.int32, 3: np.int32, 4: np.int32, 5: np.uint8, 6: np.int64}
+
+
+class Graph:
+    """One device-resident graph context (mf_ctx)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+        n = C.c_int32()
+        _check(_lib().mf_num_nodes(self._h, C.byref(n)), "mf_num_nodes")
+        self.n = n.value
+
+    @classmethod
+    def open_egr(cls, path, gpu=0):
+        h = C.c_void_p()
+        _check(_lib().mf_open_egr(os.fsencode(path), gpu, C.byref(h)), "mf_open_egr")
+        return cls(h.value)
+
+    @classmethod
+    def from_csr(cls, nindex, nlist, gpu=0):
+        nindex = np.ascontiguousarray(nindex, dtype=np.int64)
+        nlist = np.ascontiguousarray(nlist, dtype=np.int32)
+        h = C.c_void_p()
+        n = nindex.size - 1
+        _check(_lib().mf_open_csr(n, _ptr(nindex, C.c_int64), _ptr(nlist, C.c_int32), gpu, C.byref(h)),
+               "mf_open_csr")
+        return cls(h.value)
+
+    def close(self):
+        if self._h:
+            _check(_lib().mf_close(self._h), "mf_close")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_mis(self, mis):
+        mis = _u8(mis)
+        _check(_lib().mf_set_mis(self._h, _ptr(mis, C.c_uint8), mis.size), "mf_set_mis")
+
+    def get_mis(self):
+        out = np.zeros(self.n, dtype=np.uint8)
+        _check(_lib().mf_get_mis(self._h, _ptr(out, C.c_uint8), self.n), "mf_get_mis")
+        return out
+
+    def greedy_mis(self):
+        out = np.zeros(self.n, dtype=np.uint8)
+        _check(_lib().mf_greedy_mis(self._h, _ptr(out, C.c_uint8), self.n), "mf_greedy_mis")
+        return out
+
+    def flag_updates(self, u, v):
+        u, v = _i32(u), _i32(v)
+        out = np.zeros(u.size, dtype=np.uint8)
+        _check(_lib().mf_flag_updates(self._h, _ptr(u, C.c_int32), _ptr(v, C.c_int32), u.size,
+                                      _ptr(out, C.c_uint8)), "mf_flag_updates")
+        return out
+
+    def apply_batch(self, u, v, ins):
+        u, v, ins = _i32(u), _i32(v), _u8(ins)
+        _check(_lib().mf_apply_batch(self._h, _ptr(u, C.c_int32), _ptr(v, C.c_int32), _ptr(ins, C.c_uint8),
+                                     u.size), "mf_apply_batch")
+
+    def apply_batch_device(self, d_u, d_v, d_ins, m):
+        """Device pointers (ints), e.g. torch ``tensor.data_ptr()``."""
+        _check(_lib().mf_apply_batch_device(self._h, C.c_void_p(d_u), C.c_void_p(d_v), C.c_void_p(d_ins), m),
+               "mf_apply_batch_device")
+
+    def stats(self):
+        st = BatchStats()
+        _check(_lib().mf_last_batch_stats(self._h, C.byref(st)), "mf_last_batch_stats")
+        return st.as_dict()
+
+    def row(self, x):
+        ln = C.c_int64()
+        _check(_lib().mf_get_row(self._h, x, None, 0, C.byref(ln)), "mf_get_row")
+        out = np.zeros(max(ln.value, 1), dtype=np.int32)
+        _check(_lib().mf_get_row(self._h, x, _ptr(out, C.c_int32), ln.value, C.byref(ln)), "mf_get_row")
+        return out[: ln.value]
+
+    def degrees(self):
+        out = np.zeros(self.n, dtype=np.int32)
+        _check(_lib().mf_get_degrees(self._h, _ptr(out, C.c_int32), self.n), "mf_get_degrees")
+        return out
+
+    def cluster_ids(self):
+        out = np.zeros(self.n, dtype=np.int32)
+        _check(_lib().mf_get_cluster_ids(self._h, _ptr(out, C.c_int32), self.n), "mf_get_cluster_ids")
+        return out
+
+    def is_adjacent(self, u, v):
+        r = C.c_int()
+        _check(_lib().mf_is_adjacent(self._h, u, v, C.byref(r)), "mf_is_adjacent")
+        return bool(r.value)
+
+    @property
+    def max_csr(self):
+        v = C.c_int64()
+        _check(_lib().mf_get_max_csr(self._h, C.byref(v)), "mf_get_max_csr")
+        return v.value
+
+    @max_csr.setter
+    def max_csr(self, value):
+        _check(_lib().mf_set_max_csr(self._h, int(value)), "mf_set_max_csr")
+
+    def check_mis(self):
+        a, b = C.c_int64(), C.c_int64()
+        _check(_lib().mf_check_mis(self._h, C.byref(a), C.byref(b)), "mf_check_mis")
+        return a.value, b.value
+
+    def compact(self, path, rebase=False):
+        _check(_lib().mf_compact(self._h, os.fsencode(path), 1 if rebase else 0), "mf_compact")
+
+    def trace(self, on=True):
+        _check(_lib().mf_trace_enable(self._h, 1 if on else 0), "mf_trace_enable")
+
+    def trace_records(self):
+        cnt = C.c_int64()
+        _check(_lib().mf_trace_count(self._h, C.byref(cnt)), "mf_trace_count")
+        recs = []
+        for i in range(cnt.value):
+            rec = {}
+            for field, dt in _TRACE_FIELDS.items():
+                ln = C.c_int64()
+                _check(_lib().mf_trace_get(self._h, i, field, None, 0, C.byref(ln)), "mf_trace_get")
+                arr = np.zeros(max(ln.value, 1), dtype=dt)
+                _check(_lib().mf_trace_get(self._h, i, field, arr.ctypes.data_as(C.c_void_p), ln.value,
+                                           C.byref(ln)), "mf_trace_get")
+                rec[field] = arr[: ln.value]
+            recs.append(rec)
+        return recs
+
+
+def read_mis_file(path, n):
+    out = np.zeros(n, dtype=np.uint8)
+    lines = C.c_int64()
+    _check(_lib().mf_read_mis_file(os.fsencode(path), n, _ptr(out, C.c_uint8), C.byref(lines)),
+           "mf_read_mis_file")
+    return out, lines.value
+
+
+def write_mis_file(path, mis):
+    mis = _u8(mis)
+    _check(_lib().mf_write_mis_file(os.fsencode(path), _ptr(mis, C.c_uint8), mis.size), "mf_write_mis_file")
+
+
+def read_batch_file(path, n):
+    u = _I32P()
+    v = _I32P()
+    m = C.c_int64()
+    _check(_lib().mf_read_batch_file(os.fsencode(path), n, C.byref(u), C.byref(v), C.byref(m)),
+           "mf_read_batch_file")
+    try:
+        a = np.ctypeslib.as_array(u, shape=(max(m.value, 1),))[: m.value].copy()
+        b = np.ctypeslib.as_array(v, shape=(max(m.value, 1),))[: m.value].copy()
+    finally:
+        _lib().mf_free(u)
+        _lib().mf_free(v)
+    return a, b
+
+
+def list_batch_files(folder):
+    names = C.c_void_p()
+    cnt = C.c_int64()
+    _check(_lib().mf_list_batch_files(os.fsencode(folder), C.byref(names), C.byref(cnt)), "mf_list_batch_files")
+    try:
+        s = C.string_at(names).decode() if names.value else ""
+    finally:
+        _lib().mf_free(names)
+    return [x for x in s.split("\n") if x]

@@ -1,0 +1,325 @@
+"""Synthetic inputs in MISFIT's own formats.
+
+* ``.egr`` binary CSR (int32 or int64-sentinel ``nindex``), read and written
+  exactly as the reference describes it (README "File formats";
+  core/FlashGraph.h:108-169 reads it, tools/efficient_converter.py writes the
+  int64 form only).
+* Graph families of the benchmark configurations: Erdos-Renyi G(n, m),
+  R-MAT, and 2-D random geometric graphs.  All are undirected, stored with
+  both directions, without self-loops or duplicates, rows sorted ascending.
+* Update streams of toggles: deletes of existing edges and inserts of
+  non-adjacent pairs, drawn against the nominal graph as it evolves.
+* The initial-MIS and batch-folder text formats (one 1-indexed id per line;
+  ``k.mtx`` files of ``u v`` lines, 1-indexed).
+
+Everything is numpy and seeded, so the same arguments give the same bytes on
+every machine.
+"""
+import os
+import struct
+
+import numpy as np
+
+__all__ = [
+    "read_egr", "write_egr", "csr_from_pairs", "er_graph", "rmat_graph", "rgg_graph",
+    "ToggleStream", "write_batch_file", "write_batch_folder", "read_batch_file",
+    "write_mis_file", "read_mis_file", "undirected_pairs",
+]
+
+
+def read_egr(path):
+    """Return (n, nindex int64[n+1], nlist int32[E], wide)."""
+    with open(path, "rb") as f:
+        n, e32 = struct.unpack("<ii", f.read(8))
+        if e32 == -1:
+            (e,) = struct.unpack("<Q", f.read(8))
+            nindex = np.fromfile(f, dtype="<i8", count=n + 1)
+            wide = True
+        else:
+            e = e32
+            nindex = np.fromfile(f, dtype="<i4", count=n + 1).astype(np.int64)
+            wide = False
+        nlist = np.fromfile(f, dtype="<i4", count=e)
+    if nindex.size != n + 1 or nlist.size != e:
+        raise ValueError("truncated .egr file: %s" % path)
+    return n, nindex, nlist, wide
+
+
+def write_egr(path, n, nindex, nlist, wide=None):
+    """Write a .egr file.  ``wide`` None picks int32 when the entry count fits."""
+    nindex = np.asarray(nindex, dtype=np.int64)
+    nlist = np.asarray(nlist, dtype=np.int32)
+    e = int(nlist.size)
+    if wide is None:
+        wide = e > 0x7FFFFFFF
+    tmp = path + ".tmp"
+    with open(tmp, "wb") as f:
+        if wide:
+            f.write(struct.pack("<iiQ", n, -1, e))
+            f.write(nindex.astype("<i8").tobytes())
+        else:
+            if e > 0x7FFFFFFF:
+                raise ValueError("int32 layout cannot hold %d entries" % e)
+            f.write(struct.pack("<ii", n, e))
+            f.write(nindex.astype("<i4").tobytes())
+        nlist.astype("<i4").tofile(f)
+    os.replace(tmp, path)
+
+
+def csr_from_pairs(n, u, v):
+    """Symmetric CSR with sorted rows from undirected pairs (self-loops and
+    duplicates removed)."""
+    u = np.asarray(u, dtype=np.int64)
+    v = np.asarray(v, dtype=np.int64)
+    keep = u != v
+    u, v = u[keep], v[keep]
+    key = np.concatenate([u * n + v, v * n + u])
+    key = np.unique(key)
+    src = key // n
+    dst = (key % n).astype(np.int32)
+    deg = np.bincount(src, minlength=n).astype(np.int64)
+    nindex = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(deg, out=nindex[1:])
+    return nindex, dst
+
+
+def undirected_pairs(n, nindex, nlist):
+    """Unique undirected pairs (lo, hi) of a symmetric CSR, sorted by key."""
+    deg = np.diff(nindex)
+    src = np.repeat(np.arange(n, dtype=np.int64), deg)
+    dst = nlist.astype(np.int64)
+    sel = src < dst
+    return src[sel], dst[sel]
+
+
+def er_graph(n, avg_degree, seed):
+    """G(n, m) with m = n*avg_degree/2 distinct undirected edges."""
+    rng = np.random.default_rng(seed)
+    m = int(round(n * avg_degree / 2))
+    keys = np.empty(0, dtype=np.int64)
+    while keys.size < m:
+        need = m - keys.size
+        a = rng.integers(0, n, size=2 * need + 16)
+        b = rng.integers(0, n, size=2 * need + 16)
+        ok = a != b
+        lo = np.minimum(a[ok], b[ok])
+        hi = np.maximum(a[ok], b[ok])
+        new = lo * n + hi
+        keys = np.unique(np.concatenate([keys, new]))
+        if keys.size > m:
+            # keep a seeded random subset of exactly m keys
+            keys = np.sort(rng.choice(keys, size=m, replace=False))
+    return csr_from_pairs(n, keys // n, keys % n)
+
+
+def rmat_graph(scale, edge_factor, seed, abcd=(0.57, 0.19, 0.19, 0.05), chunk=1 << 24):
+    """R-MAT with 2**scale vertices and edge_factor * 2**scale samples,
+    symmetrised and de-duplicated."""
+    a, b, c, _ = abcd
+    n = 1 << scale
+    total = n * edge_factor
+    rng = np.random.default_rng(seed)
+    keys = []
+    done = 0
+    while done < total:
+        cnt = min(chunk, total - done)
+        u = np.zeros(cnt, dtype=np.int64)
+        v = np.zeros(cnt, dtype=np.int64)
+        for lvl in range(scale):
+            r = rng.random(cnt, dtype=np.float32)
+            ubit = r >= (a + b)
+            vbit = ((r >= a) & (r < a + b)) | (r >= (a + b + c))
+            u |= ubit.astype(np.int64) << lvl
+            v |= vbit.astype(np.int64) << lvl
+        keep = u != v
+        lo = np.minimum(u[keep], v[keep])
+        hi = np.maximum(u[keep], v[keep])
+        keys.append(np.unique(lo * n + hi))
+        done += cnt
+    key = np.unique(np.concatenate(keys))
+    return n, csr_from_pairs(n, key // n, key % n)
+
+
+def rgg_graph(n, mean_degree, seed):
+    """2-D random geometric graph in the unit square with the radius set for
+    the requested mean degree (with a first-order boundary correction)."""
+    rng = np.random.default_rng(seed)
+    pts = rng.random((n, 2))
+    # expected degree with boundary loss ~ n*pi*r^2*(1 - 8r/(3pi))
+    r = np.sqrt(mean_degree / (n * np.pi))
+    for _ in range(3):
+        r = np.sqrt(mean_degree / (n * np.pi * max(1e-9, 1 - 8 * r / (3 * np.pi))))
+    cells = max(1, int(1.0 / r))
+    cx = np.minimum((pts[:, 0] * cells).astype(np.int64), cells - 1)
+    cy = np.minimum((pts[:, 1] * cells).astype(np.int64), cells - 1)
+    cell = cx * cells + cy
+    order = np.argsort(cell, kind="stable")
+    cell_sorted = cell[order]
+    starts = np.searchsorted(cell_sorted, np.arange(cells * cells + 1))
+    us, vs = [], []
+    r2 = r * r
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            ncx = cx + dx
+            ncy = cy + dy
+            ok = (ncx >= 0) & (ncx < cells) & (ncy >= 0) & (ncy < cells)
+            idx = np.nonzero(ok)[0]
+            nc = ncx[idx] * cells + ncy[idx]
+            lo = starts[nc]
+            hi = starts[nc + 1]
+            cnt = hi - lo
+            rep = np.repeat(idx, cnt)
+            off = np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+            cand = order[np.repeat(lo, cnt) + off]
+            d = pts[rep] - pts[cand]
+            close = (d * d).sum(axis=1) <= r2
+            sel = close & (rep < cand)
+            us.append(rep[sel])
+            vs.append(cand[sel])
+    return csr_from_pairs(n, np.concatenate(us), np.concatenate(vs))
+
+
+class ToggleStream:
+    """Batches of toggles drawn against the nominal graph as it evolves.
+
+    Each batch holds ``batch_size`` lines: ``round(batch_size*delete_frac)``
+    deletes of existing edges and the rest inserts of non-adjacent pairs,
+    shuffled.  ``endpoints`` picks how endpoints are drawn: ``uniform``
+    (deletes uniform over edges, inserts uniform over pairs), ``preferential``
+    (probability proportional to current degree) or ``low_degree``
+    (proportional to 1/degree).  After each batch the nominal graph applies
+    the toggles, so later batches may delete edges inserted earlier.
+    """
+
+    def __init__(self, n, nindex, nlist, seed):
+        self.n = int(n)
+        lo, hi = undirected_pairs(self.n, nindex, nlist)
+        self.keys = np.sort(lo * self.n + hi)
+        self.rng = np.random.default_rng(seed)
+        self.deg = np.diff(np.asarray(nindex, dtype=np.int64)).astype(np.float64)
+
+    def _has(self, keys):
+        if self.keys.size == 0:
+            return np.zeros(keys.shape, dtype=bool)
+        pos = np.minimum(np.searchsorted(self.keys, keys), self.keys.size - 1)
+        return self.keys[pos] == keys
+
+    def _vertex_sampler(self, mode, size):
+        if mode == "uniform":
+            return self.rng.integers(0, self.n, size=size)
+        if mode == "preferential":
+            w = self.deg + 1e-12
+        elif mode == "low_degree":
+            w = 1.0 / np.maximum(self.deg, 1.0)
+        else:
+            raise ValueError(mode)
+        cdf = np.cumsum(w)
+        cdf /= cdf[-1]
+        return np.minimum(np.searchsorted(cdf, self.rng.random(size)), self.n - 1)
+
+    def next_batch(self, batch_size, delete_frac=0.5, endpoints="uniform"):
+        n = self.n
+        nd = int(round(batch_size * delete_frac))
+        nd = min(nd, int(self.keys.size))
+        ni = batch_size - nd
+        # deletes: existing edges
+        if endpoints == "uniform" or nd == 0:
+            pick = self.rng.choice(self.keys.size, size=nd, replace=False) if nd else np.empty(0, np.int64)
+            dkeys = self.keys[pick]
+        else:
+            # weight each edge by the endpoint weights of its lower endpoint
+            dkeys = np.empty(0, dtype=np.int64)
+            while dkeys.size < nd:
+                x = self._vertex_sampler(endpoints, 4 * (nd - dkeys.size) + 16)
+                start = np.searchsorted(self.keys, x * n)
+                stop = np.searchsorted(self.keys, x * n + n)
+                has = stop > start
+                x, start, stop = x[has], start[has], stop[has]
+                j = start + (self.rng.random(x.size) * (stop - start)).astype(np.int64)
+                cand = self.keys[j]
+                dkeys = np.unique(np.concatenate([dkeys, cand]))
+            dkeys = self.rng.permutation(dkeys)[:nd]
+        # inserts: non-adjacent distinct pairs
+        ikeys = np.empty(0, dtype=np.int64)
+        while ikeys.size < ni:
+            need = ni - ikeys.size
+            a = self._vertex_sampler(endpoints, 2 * need + 16)
+            b = self._vertex_sampler(endpoints, 2 * need + 16)
+            ok = a != b
+            lo = np.minimum(a[ok], b[ok])
+            hi = np.maximum(a[ok], b[ok])
+            k = lo * n + hi
+            k = k[~self._has(k)]
+            ikeys = np.unique(np.concatenate([ikeys, k]))
+            if ikeys.size > ni:
+                ikeys = self.rng.permutation(ikeys)[:ni]
+        keys = np.concatenate([dkeys, ikeys])
+        perm = self.rng.permutation(keys.size)
+        keys = keys[perm]
+        lo = keys // n
+        hi = keys % n
+        flip = self.rng.random(keys.size) < 0.5
+        u = np.where(flip, hi, lo).astype(np.int32)
+        v = np.where(flip, lo, hi).astype(np.int32)
+        # nominal graph update
+        self.keys = np.sort(np.concatenate([np.setdiff1d(self.keys, dkeys, assume_unique=True), ikeys]))
+        dl, dh = dkeys // n, dkeys % n
+        il, ih = ikeys // n, ikeys % n
+        np.subtract.at(self.deg, dl, 1)
+        np.subtract.at(self.deg, dh, 1)
+        np.add.at(self.deg, il, 1)
+        np.add.at(self.deg, ih, 1)
+        return u, v
+
+
+def write_batch_file(path, u, v):
+    """``u v`` lines, 1-indexed."""
+    arr = np.stack([np.asarray(u, np.int64) + 1, np.asarray(v, np.int64) + 1], axis=1)
+    with open(path, "w") as f:
+        if arr.size:
+            f.write("\n".join("%d %d" % (a, b) for a, b in arr))
+            f.write("\n")
+
+
+def write_batch_folder(folder, batches):
+    os.makedirs(folder, exist_ok=True)
+    for i, (u, v) in enumerate(batches):
+        write_batch_file(os.path.join(folder, "%d.mtx" % (i + 1)), u, v)
+
+
+def read_batch_file(path):
+    """0-indexed (u, v) of every line that starts with two integers."""
+    us, vs = [], []
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) < 2:
+                continue
+            try:
+                a, b = int(parts[0]), int(parts[1])
+            except ValueError:
+                continue
+            us.append(a - 1)
+            vs.append(b - 1)
+    return np.array(us, dtype=np.int64), np.array(vs, dtype=np.int64)
+
+
+def write_mis_file(path, mis):
+    idx = np.nonzero(np.asarray(mis))[0] + 1
+    with open(path, "w") as f:
+        if idx.size:
+            f.write("\n".join(str(int(i)) for i in idx))
+            f.write("\n")
+
+
+def read_mis_file(path, n):
+    out = np.zeros(n, dtype=np.uint8)
+    with open(path) as f:
+        for line in f:
+            s = line.strip()
+            if not s:
+                continue
+            i = int(s) - 1
+            if 0 <= i < n:
+                out[i] = 1
+    return out

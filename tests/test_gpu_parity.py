@@ -1,0 +1,200 @@
+"""GPU path (libmisfit_gb through its C-ABI) against the oracle and the
+golden vectors.  Integer work: every comparison is bit-exact."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+from misfit_gb300 import native
+from misfit_gb300 import workloads as W
+from tests import _golden as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _assert_same_trace(gpu_recs, orc_recs, n):
+    assert len(gpu_recs) == len(orc_recs)
+    for k, (a, b) in enumerate(zip(gpu_recs, orc_recs)):
+        ha, hb = a[0], b[0]
+        # p, q, seeds, candidates, max_after, clusters, processed, rows, estimate
+        for f in (0, 1, 2, 3, 5, 6, 7, 8, 9):
+            assert ha[f] == hb[f], ("header", k, f, ha.tolist(), hb.tolist())
+        if ha[4] >= 0:
+            assert ha[4] == hb[4], ("packed", k)
+            assert np.array_equal(a[6], b[6]), ("row lengths", k)
+        for f, what in ((1, "seeds"), (2, "candidates"), (3, "cluster ids"), (4, "order"), (5, "membership")):
+            assert np.array_equal(a[f], b[f]), (what, k)
+
+
+@pytest.mark.parametrize("name", G.NAMES)
+def test_golden_streams(name, gpu_lib, tmp_path):
+    g = G.load(name)
+    gr = native.Graph.from_csr(g["nindex"], g["nlist"])
+    assert gr.max_csr == int(g["initial_max_csr"])
+    if "max_csr" in g:
+        gr.max_csr = int(g["max_csr"])
+    gr.set_mis(g["mis0"])
+    assert np.array_equal(gr.greedy_mis(), g["mis0"])
+    bs = G.batches(g)
+    for u, v, ins in bs:
+        assert np.array_equal(gr.flag_updates(u, v), ins)
+    for i, (u, v, ins) in enumerate(bs):
+        gr.trace(True)
+        gr.apply_batch(u, v, ins)
+        want = G.rows(g, i)
+        for x in range(gr.n):
+            assert np.array_equal(gr.row(x), want[x]), (i, x)
+        assert np.array_equal(gr.degrees(), g["b%d_deg" % i])
+        assert np.array_equal(gr.get_mis(), g["b%d_mis_oracle" % i]), i
+        hdr = np.stack([r[0] for r in gr.trace_records()])
+        ref_hdr = g["b%d_trace_hdr" % i]
+        assert hdr.shape == ref_hdr.shape
+        cols = [0, 1, 2, 3, 5, 6, 7, 8, 9]
+        assert np.array_equal(hdr[:, cols], ref_hdr[:, cols]), i
+        known = hdr[:, 4] >= 0
+        assert np.array_equal(hdr[known, 4], ref_hdr[known, 4])
+    out = str(tmp_path / "c.egr")
+    gr.compact(out)
+    data = open(out, "rb").read()
+    assert len(data) == int(g["compact_len"])
+    assert hashlib.sha256(data).digest() == bytes(g["compact_sha256"])
+    gr.close()
+
+
+def _stream(kind, seed, batches, size, endpoints="uniform"):
+    if kind == "er":
+        n = 3000
+        ni, nl = W.er_graph(n, 8, seed)
+    else:
+        n, (ni, nl) = W.rmat_graph(11, 8, seed)
+    ts = W.ToggleStream(n, ni, nl, seed + 1)
+    return n, ni, nl, [ts.next_batch(size, endpoints=endpoints) for _ in range(batches)]
+
+
+@pytest.mark.parametrize("kind,seed,max_csr", [("er", 11, None), ("rmat", 12, None), ("rmat", 13, 3000),
+                                               ("rmat", 14, 40000)])
+def test_stage_parity_live(kind, seed, max_csr, gpu_lib):
+    n, ni, nl, bs = _stream(kind, seed, 4, 500)
+    orc = O.Oracle.from_csr(ni, nl)
+    gr = native.Graph.from_csr(ni, nl)
+    if max_csr:
+        orc.max_csr = max_csr
+        gr.max_csr = max_csr
+    mis = O.greedy_mis(ni, nl)
+    orc.set_mis(mis)
+    gr.set_mis(mis)
+    flags = [orc.flag_updates(u, v) for u, v in bs]
+    for (u, v), ins in zip(bs, flags):
+        assert np.array_equal(gr.flag_updates(u, v), ins)
+    for (u, v), ins in zip(bs, flags):
+        orc.trace(True)
+        gr.trace(True)
+        orc.apply_batch(u, v, ins)
+        gr.apply_batch(u, v, ins)
+        _assert_same_trace(gr.trace_records(), orc.trace_records(), n)
+        assert np.array_equal(gr.get_mis(), orc.get_mis())
+        assert np.array_equal(gr.cluster_ids(), orc.cluster_ids())
+        assert np.array_equal(gr.degrees(), orc.degrees())
+        assert gr.max_csr == orc.max_csr
+        assert gr.check_mis() == orc.check_mis()
+
+
+def test_config1_er10k_ten_batches(gpu_lib, tmp_path):
+    """ER G(10000, avg 8), int32 .egr, seed 42; 10 batches of 2000 toggles
+    (1000 deletes of existing edges, 1000 inserts of non-adjacent pairs);
+    MIS after every batch identical to the oracle."""
+    n = 10000
+    ni, nl = W.er_graph(n, 8, 42)
+    p = str(tmp_path / "er10k.egr")
+    W.write_egr(p, n, ni, nl)
+    ts = W.ToggleStream(n, ni, nl, 42)
+    bs = [ts.next_batch(2000) for _ in range(10)]
+    gr = native.Graph.open_egr(p)
+    orc = O.Oracle.open_egr(p)
+    mis = gr.greedy_mis()
+    assert np.array_equal(mis, O.greedy_mis(ni, nl))
+    gr.set_mis(mis)
+    orc.set_mis(mis)
+    flags = [gr.flag_updates(u, v) for u, v in bs]
+    for (u, v), ins in zip(bs, flags):
+        assert np.array_equal(ins, orc.flag_updates(u, v))
+    for (u, v), ins in zip(bs, flags):
+        gr.apply_batch(u, v, ins)
+        orc.apply_batch(u, v, ins)
+        assert np.array_equal(gr.get_mis(), orc.get_mis())
+    assert gr.check_mis() == orc.check_mis()
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_open_egr_layouts(wide, gpu_lib, tmp_path):
+    g = G.load("er1500")
+    p = str(tmp_path / "g.egr")
+    W.write_egr(p, int(g["n"]), g["nindex"], g["nlist"], wide=wide)
+    gr = native.Graph.open_egr(p)
+    gr.set_mis(g["mis0"])
+    for i, (u, v, ins) in enumerate(G.batches(g)):
+        gr.apply_batch(u, v, ins)
+        assert np.array_equal(gr.get_mis(), g["b%d_mis_oracle" % i])
+
+
+def test_free_flags_all_overlay_transitions(gpu_lib):
+    """Flags chosen at random instead of from the base graph: inserts of base
+    edges, deletes of absent pairs, un-tombstones and forgets all occur,
+    repeatedly on the same pairs within one batch."""
+    n = 80
+    ni, nl = W.er_graph(n, 5, 3)
+    orc = O.Oracle.from_csr(ni, nl)
+    gr = native.Graph.from_csr(ni, nl)
+    mis = O.greedy_mis(ni, nl)
+    orc.set_mis(mis)
+    gr.set_mis(mis)
+    rng = np.random.default_rng(5)
+    for _ in range(8):
+        m = 300
+        u = rng.integers(0, n, m).astype(np.int32)
+        v = rng.integers(0, n, m).astype(np.int32)
+        keep = u != v
+        u, v = u[keep], v[keep]
+        ins = rng.integers(0, 2, u.size).astype(np.uint8)
+        orc.apply_batch(u, v, ins)
+        gr.apply_batch(u, v, ins)
+        for x in range(n):
+            assert np.array_equal(gr.row(x), orc.row(x)), x
+        assert np.array_equal(gr.degrees(), orc.degrees())
+        assert np.array_equal(gr.get_mis(), orc.get_mis())
+
+
+def test_empty_and_invalid_batches(gpu_lib):
+    g = G.load("er1500")
+    gr = native.Graph.from_csr(g["nindex"], g["nlist"])
+    gr.set_mis(g["mis0"])
+    gr.apply_batch(np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0, np.uint8))
+    assert np.array_equal(gr.get_mis(), g["mis0"])
+    assert gr.stats()["sub_batches"] == 0
+    for u, v in (([0], [0]), ([0], [1500]), ([-1], [3])):
+        with pytest.raises(native.MisfitError) as e:
+            gr.apply_batch(np.array(u, np.int32), np.array(v, np.int32), np.zeros(1, np.uint8))
+        assert e.value.status == -1
+    # the context stays usable after a rejected call
+    u, v, ins = G.batches(g)[0]
+    gr.apply_batch(u, v, ins)
+    assert np.array_equal(gr.get_mis(), g["b0_mis_oracle"])
+
+
+def test_bad_egr_files(gpu_lib, tmp_path):
+    p = tmp_path / "t.egr"
+    p.write_bytes(b"\x05\x00\x00\x00")
+    with pytest.raises(native.MisfitError) as e:
+        native.Graph.open_egr(str(p))
+    assert e.value.status == -3
+    g = G.load("er1500")
+    W.write_egr(str(p), int(g["n"]), g["nindex"], g["nlist"])
+    data = p.read_bytes()
+    p.write_bytes(data[:-40])
+    with pytest.raises(native.MisfitError) as e:
+        native.Graph.open_egr(str(p))
+    assert e.value.status == -3
+    with pytest.raises(native.MisfitError) as e:
+        native.Graph.open_egr(str(tmp_path / "missing.egr"))
+    assert e.value.status == -2
