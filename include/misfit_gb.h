@@ -171,6 +171,21 @@ int mf_read_batch_file(const char* path, int32_t n, int32_t** u, int32_t** v, in
 int mf_list_batch_files(const char* folder, char** names, int64_t* count);
 void mf_free(void* p);
 
+/* ---- profiling ----------------------------------------------------------- */
+
+/* Number of stages the profiler distinguishes. */
+#define MF_NUM_STAGES 10
+/* Name of stage i (0 <= i < MF_NUM_STAGES), NULL otherwise. */
+const char* mf_stage_name(int stage);
+/* When on, every later batch records CUDA events around each stage on the
+ * context's stream; times accumulate until mf_profile_reset. */
+int mf_profile_enable(mf_ctx* ctx, int on);
+int mf_profile_reset(mf_ctx* ctx);
+/* Accumulated device milliseconds and occurrences per stage (cap entries). */
+int mf_profile_read(mf_ctx* ctx, double* ms, int64_t* calls, int cap);
+/* Kernels launched by this library in this process so far. */
+int64_t mf_kernel_launches(void);
+
 /* ---- trace (parity tests) ---------------------------------------------- */
 
 /* When enabled, mf_apply_batch keeps, per sub-batch, the stage outputs the

@@ -23,6 +23,10 @@ namespace {
 thread_local std::string g_error;
 }
 
+std::atomic<long long> g_launches{0};
+const char* const kStageNames[kStCount] = {"overlay", "split", "seeds", "hop1", "sizes",
+                                           "cluster_read", "cluster_write", "assign", "repair", "clear"};
+
 void set_error(const std::string& msg) { g_error = msg; }
 const char* get_error() { return g_error.c_str(); }
 
@@ -74,9 +78,21 @@ void release_all(mf_ctx* c) {
   c->vals.release();
   c->app_keys.release();
   c->app_vals.release();
+  for (auto* b : {&c->rp_w0, &c->rp_w1, &c->rp_n0, &c->rp_n1}) b->release();
+  c->rp_keys.release();
+  c->rp_keys2.release();
+  c->rp_vals.release();
+  c->rp_vals2.release();
+  c->rp_u8.release();
+  c->rp_pos.release();
+  for (auto* b : {&c->big_pos, &c->big_off, &c->big_nr, &c->big_chunks, &c->big_pre}) b->release();
+  c->big_r.release();
+  c->big_best.release();
   c->ws.release();
   if (c->h_counters) cudaFreeHost(c->h_counters);
   c->h_counters = nullptr;
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  c->ev_pool.clear();
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -114,7 +130,10 @@ void run_batch(mf_ctx* c, int64_t m) {
   c->traces.clear();
   MF_CUDA(cudaEventRecord(c->ev0, s));
   if (m > 0) {
-    mf::apply_overlay(c, m);
+    {
+      mf::StageScope sc(c, mf::kStOverlay);
+      mf::apply_overlay(c, m);
+    }
     mf::process_batch(c, m);
   }
   MF_CUDA(cudaEventRecord(c->ev1, s));
@@ -123,6 +142,15 @@ void run_batch(mf_ctx* c, int64_t m) {
   MF_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->stats.device_ms = ms;
   c->stats.max_csr = c->max_csr;
+  for (const auto& mk : c->ev_marks) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, c->ev_pool[mk.second], c->ev_pool[mk.second + 1]) == cudaSuccess) {
+      c->stage_ms[mk.first] += t;
+      c->stage_calls[mk.first] += 1;
+    }
+  }
+  c->ev_marks.clear();
+  c->ev_used = 0;
 }
 
 __global__ void k_validate(const int32_t* u, const int32_t* v, int64_t m, int32_t n, unsigned long long* bad) {
@@ -143,8 +171,8 @@ void stage_inputs(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* 
   MF_CUDA(cudaMemcpyAsync(c->bv.p, v, sizeof(int32_t) * (size_t)m, kind, s));
   if (ins) MF_CUDA(cudaMemcpyAsync(c->bins.p, ins, (size_t)m, kind, s));
   MF_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int64_t), s));
-  k_validate<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(c->bu.p, c->bv.p, m, c->n,
-                                                          reinterpret_cast<unsigned long long*>(c->counters.p));
+  MF_K(k_validate<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(c->bu.p, c->bv.p, m, c->n,
+                                                          reinterpret_cast<unsigned long long*>(c->counters.p)));
   MF_CUDA(cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   MF_CUDA(cudaStreamSynchronize(s));
   if (c->h_counters[0] != 0) MF_FAIL(MF_EINVAL, "update endpoints must be distinct vertex ids in [0, n)");
@@ -361,8 +389,11 @@ int mf_set_mis(mf_ctx* c, const uint8_t* mis, int64_t n) {
     need(c && mis && n == c->n, MF_EINVAL, "membership vector must have n entries");
     bind(c);
     if (n > 0) {
-      MF_CUDA(cudaMemcpyAsync(c->mis.p, mis, (size_t)n, cudaMemcpyHostToDevice, c->stream));
+      std::vector<uint8_t> norm((size_t)n);
+      for (int64_t i = 0; i < n; ++i) norm[(size_t)i] = mis[i] ? 1 : 0;
+      MF_CUDA(cudaMemcpyAsync(c->mis.p, norm.data(), (size_t)n, cudaMemcpyHostToDevice, c->stream));
       MF_CUDA(cudaMemsetAsync(c->cid.p, 0xFF, sizeof(int32_t) * (size_t)n, c->stream));
+      MF_CUDA(cudaStreamSynchronize(c->stream));
     }
     MF_CUDA(cudaStreamSynchronize(c->stream));
   });
@@ -676,6 +707,39 @@ int mf_list_batch_files(const char* folder, char** names, int64_t* count) {
 }
 
 void mf_free(void* p) { std::free(p); }
+
+const char* mf_stage_name(int stage) {
+  return (stage >= 0 && stage < mf::kStCount) ? mf::kStageNames[stage] : nullptr;
+}
+
+int mf_profile_enable(mf_ctx* c, int on) {
+  return guarded([&] {
+    need(c != nullptr, MF_EINVAL, "null context");
+    c->profile = on != 0;
+  });
+}
+
+int mf_profile_reset(mf_ctx* c) {
+  return guarded([&] {
+    need(c != nullptr, MF_EINVAL, "null context");
+    for (int i = 0; i < mf::kStCount; ++i) {
+      c->stage_ms[i] = 0;
+      c->stage_calls[i] = 0;
+    }
+  });
+}
+
+int mf_profile_read(mf_ctx* c, double* ms, int64_t* calls, int cap) {
+  return guarded([&] {
+    need(c && ms && calls && cap >= 0, MF_EINVAL, "bad arguments");
+    for (int i = 0; i < mf::kStCount && i < cap; ++i) {
+      ms[i] = c->stage_ms[i];
+      calls[i] = c->stage_calls[i];
+    }
+  });
+}
+
+int64_t mf_kernel_launches(void) { return (int64_t)mf::g_launches.load(); }
 
 int mf_trace_enable(mf_ctx* c, int on) {
   return guarded([&] {

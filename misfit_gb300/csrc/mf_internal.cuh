@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -54,6 +55,32 @@ struct Failure {
     ::mf::set_error(msg);               \
     throw ::mf::Failure{status};        \
   } while (0)
+
+// Every kernel launch of the library goes through MF_K so that the number of
+// launches can be reported (mf_kernel_launches).
+extern std::atomic<long long> g_launches;
+inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+#define MF_K(...)            \
+  do {                       \
+    __VA_ARGS__;             \
+    ::mf::note_launch();     \
+  } while (0)
+
+// Stages timed by the optional profiler (mf_profile_enable).
+enum Stage : int {
+  kStOverlay = 0,   // batch apply to the overlay
+  kStSplit,         // previous-occurrence sort + split rule
+  kStSeeds,         // seed compaction
+  kStHop1,          // hop-1 marking + candidates
+  kStSizes,         // packed-size bound, exact 2-hop sizes, growth
+  kStFirst,         // clustering read pass (first existing ids, row decisions)
+  kStPush,          // clustering write pass (2-hop max pushes, finalize)
+  kStAssign,        // assignment + ordering sort
+  kStRepair,        // MIS repair
+  kStClear,         // clear of mapped vertices
+  kStCount
+};
+extern const char* const kStageNames[kStCount];
 
 // ---- device buffers ------------------------------------------------------
 
@@ -250,6 +277,16 @@ struct mf_ctx {
   mf::DBuf<int32_t> rowcid;
   mf::DBuf<uint8_t> creates;
   mf::DBuf<int64_t> rowlens;
+  // speculative repair
+  mf::DBuf<int32_t> rp_w0, rp_w1, rp_n0, rp_n1;
+  mf::DBuf<uint64_t> rp_keys, rp_keys2;
+  mf::DBuf<uint32_t> rp_vals, rp_vals2;
+  mf::DBuf<uint8_t> rp_u8;
+  mf::DBuf<int64_t> rp_pos;
+  mf::DBuf<int64_t> big_pos, big_off, big_nr, big_chunks, big_pre;
+  mf::DBuf<int32_t> big_r;
+  mf::DBuf<unsigned long long> big_best;
+  int big_grid = 0;
   mf::DBuf<uint32_t> bitmaps;   // per-CTA vertex bitmaps for exact 2-hop sizes
   int64_t bitmap_words = 0;
   int bitmap_ctas = 0;
@@ -262,6 +299,14 @@ struct mf_ctx {
   bool trace = false;
   std::vector<SubBatchTrace> traces;
 
+  // optional per-stage CUDA-event profiling
+  bool profile = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, size_t>> ev_marks;
+  double stage_ms[mf::kStCount] = {};
+  int64_t stage_calls[mf::kStCount] = {};
+
   // pinned staging for host-input batches
   uint8_t* h_stage = nullptr;
   int64_t h_stage_cap = 0;
@@ -273,6 +318,32 @@ struct mf_ctx {
 };
 
 namespace mf {
+// Records a start/end event pair around a stage when profiling is on.
+struct StageScope {
+  mf_ctx* c;
+  int stage;
+  size_t first = 0;
+  bool on;
+  StageScope(mf_ctx* ctx, int st) : c(ctx), stage(st), on(ctx->profile) {
+    if (!on) return;
+    if (c->ev_used + 2 > c->ev_pool.size()) {
+      for (int k = 0; k < 64; ++k) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) { on = false; return; }
+        c->ev_pool.push_back(e);
+      }
+    }
+    first = c->ev_used;
+    c->ev_used += 2;
+    cudaEventRecord(c->ev_pool[first], c->stream);
+  }
+  ~StageScope() {
+    if (!on) return;
+    cudaEventRecord(c->ev_pool[first + 1], c->stream);
+    c->ev_marks.emplace_back(stage, first);
+  }
+};
+
 // mf_overlay.cu
 void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nlist, int64_t nnz);
 void apply_overlay(mf_ctx* c, int64_t m);          // uses c->bu/bv/bins

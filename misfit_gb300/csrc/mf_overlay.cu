@@ -365,19 +365,19 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   c->epoch = 0;
   c->counters.reserve(64);
   if (n > 0) {
-    k_base_degree<<<grid_for(n), kTB, 0, s>>>(c->nindex.p, n, c->deg.p);
+    MF_K(k_base_degree<<<grid_for(n), kTB, 0, s>>>(c->nindex.p, n, c->deg.p));
   }
   // validate and detect sorted rows
   MF_CUDA(cudaMemsetAsync(c->counters.p, 0xFF, sizeof(int64_t) * 4, s));
   int* okp = reinterpret_cast<int*>(c->counters.p);
-  k_check_index<<<grid_for((int64_t)n + 1), kTB, 0, s>>>(c->nindex.p, n, nnz, okp);
-  if (nnz > 0) k_check_ids<<<grid_for(std::min<int64_t>(nnz, (int64_t)1 << 22)), kTB, 0, s>>>(c->nlist.p, nnz, n, okp + 1);
+  MF_K(k_check_index<<<grid_for((int64_t)n + 1), kTB, 0, s>>>(c->nindex.p, n, nnz, okp));
+  if (nnz > 0) MF_K(k_check_ids<<<grid_for(std::min<int64_t>(nnz, (int64_t)1 << 22)), kTB, 0, s>>>(c->nlist.p, nnz, n, okp + 1));
   MF_CUDA(cudaStreamSynchronize(s));
   int ok[2] = {0, 0};
   MF_CUDA(cudaMemcpy(ok, okp, sizeof(ok), cudaMemcpyDeviceToHost));
   if (!ok[0]) MF_FAIL(MF_EFORMAT, "nindex is not a valid offset array (non-monotone or outside [0, entries])");
   if (!ok[1]) MF_FAIL(MF_EFORMAT, "nlist holds a vertex id outside [0, nodes)");
-  if (n > 0) k_check_sorted<<<grid_for(n), kTB, 0, s>>>(c->nindex.p, c->nlist.p, n, okp + 2);
+  if (n > 0) MF_K(k_check_sorted<<<grid_for(n), kTB, 0, s>>>(c->nindex.p, c->nlist.p, n, okp + 2));
   MF_CUDA(cudaMemcpyAsync(ok, okp + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
   MF_CUDA(cudaStreamSynchronize(s));
   c->rows_sorted = ok[0] != 0;
@@ -386,7 +386,7 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
 
 void flag_updates(mf_ctx* c, int64_t m) {
   if (m <= 0) return;
-  k_flags<<<grid_for(m), kTB, 0, c->stream>>>(c->view(), c->rows_sorted, c->bu.p, c->bv.p, m, c->bins.p);
+  MF_K(k_flags<<<grid_for(m), kTB, 0, c->stream>>>(c->view(), c->rows_sorted, c->bu.p, c->bv.p, m, c->bins.p));
   MF_CUDA(cudaGetLastError());
 }
 
@@ -396,7 +396,7 @@ void apply_overlay(mf_ctx* c, int64_t m) {
   const int nbits = bits_for(std::max<int32_t>(c->n - 1, 1));
   c->keys.reserve(2 * m);
   c->vals.reserve(2 * m);
-  k_pair_keys<<<grid_for(m), kTB, 0, s>>>(c->bu.p, c->bv.p, m, nbits, c->keys.p, c->vals.p);
+  MF_K(k_pair_keys<<<grid_for(m), kTB, 0, s>>>(c->bu.p, c->bv.p, m, nbits, c->keys.p, c->vals.p));
   radix_sort_pairs(c->keys.p, c->vals.p, m, 2 * nbits, c->ws, s);
 
   const int64_t cap_new = c->a_total + 2 * m;
@@ -410,17 +410,17 @@ void apply_overlay(mf_ctx* c, int64_t m) {
   c->i64a.reserve(std::max<int64_t>(c->a_total, 1) + 1);
   if (c->a_total > 0) MF_CUDA(cudaMemsetAsync(c->akill.p, 0, (size_t)c->a_total, s));
   MF_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int64_t) * 2, s));
-  k_init_acnt<<<grid_for(c->n), kTB, 0, s>>>(c->aoff.p, c->n, c->acnt_new.p);
-  k_apply_pairs<<<grid_for(m), kTB, 0, s>>>(c->view(), c->live.p, c->dead.p, c->rcnt.p, c->rows_sorted,
+  MF_K(k_init_acnt<<<grid_for(c->n), kTB, 0, s>>>(c->aoff.p, c->n, c->acnt_new.p));
+  MF_K(k_apply_pairs<<<grid_for(m), kTB, 0, s>>>(c->view(), c->live.p, c->dead.p, c->rcnt.p, c->rows_sorted,
                                             c->keys.p, c->vals.p, m, nbits, c->bu.p, c->bv.p, c->bins.p,
                                             c->acnt_new.p, c->akill.p, c->app_keys.p, c->app_vals.p,
-                                            c->counters.p);
+                                            c->counters.p));
   MF_CUDA(cudaGetLastError());
   MF_CUDA(cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
   MF_CUDA(cudaStreamSynchronize(s));
   const int64_t appended = c->h_counters[0], killed = c->h_counters[1];
   if (appended == 0 && killed == 0) {
-    k_degrees<<<grid_for(c->n), kTB, 0, s>>>(c->nindex.p, c->rcnt.p, c->aoff.p, c->n, c->deg.p);
+    MF_K(k_degrees<<<grid_for(c->n), kTB, 0, s>>>(c->nindex.p, c->rcnt.p, c->aoff.p, c->n, c->deg.p));
     MF_CUDA(cudaGetLastError());
     return;
   }
@@ -428,20 +428,20 @@ void apply_overlay(mf_ctx* c, int64_t m) {
   scan_exclusive_i32(c->acnt_new.p, c->aoff_alt.p, c->n, c->ws, s);
   if (c->a_total > 0) {
     scan_exclusive_u8(c->akill.p, c->i64a.p, c->a_total, c->ws, s);
-    k_move_survivors<<<grid_for(c->a_total), kTB, 0, s>>>(c->aoff.p, c->aadj.p, c->aown.p, c->akill.p, c->i64a.p,
-                                                          c->a_total, c->aoff_alt.p, c->aadj_alt.p, c->aown_alt.p);
+    MF_K(k_move_survivors<<<grid_for(c->a_total), kTB, 0, s>>>(c->aoff.p, c->aadj.p, c->aown.p, c->akill.p, c->i64a.p,
+                                                          c->a_total, c->aoff_alt.p, c->aadj_alt.p, c->aown_alt.p));
   }
   if (appended > 0) {
     radix_sort_pairs(c->app_keys.p, c->app_vals.p, appended, 32 + nbits, c->ws, s);
-    k_place_appends<<<grid_for(appended), kTB, 0, s>>>(c->app_keys.p, c->app_vals.p, appended, c->aoff_alt.p,
-                                                       c->aadj_alt.p, c->aown_alt.p);
+    MF_K(k_place_appends<<<grid_for(appended), kTB, 0, s>>>(c->app_keys.p, c->app_vals.p, appended, c->aoff_alt.p,
+                                                       c->aadj_alt.p, c->aown_alt.p));
   }
   MF_CUDA(cudaGetLastError());
   std::swap(c->aoff, c->aoff_alt);
   std::swap(c->aadj, c->aadj_alt);
   std::swap(c->aown, c->aown_alt);
   c->a_total = c->a_total + appended - killed;
-  k_degrees<<<grid_for(c->n), kTB, 0, s>>>(c->nindex.p, c->rcnt.p, c->aoff.p, c->n, c->deg.p);
+  MF_K(k_degrees<<<grid_for(c->n), kTB, 0, s>>>(c->nindex.p, c->rcnt.p, c->aoff.p, c->n, c->deg.p));
   MF_CUDA(cudaGetLastError());
 }
 
@@ -449,7 +449,7 @@ void compact_graph(mf_ctx* c, std::vector<int64_t>& nindex_out, std::vector<int3
   cudaStream_t s = c->stream;
   const int32_t n = c->n;
   MF_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int64_t) * 2, s));
-  if (n > 0) k_compact_check<<<grid_for(n), kTB, 0, s>>>(c->view(), c->deg.p, c->counters.p);
+  if (n > 0) MF_K(k_compact_check<<<grid_for(n), kTB, 0, s>>>(c->view(), c->deg.p, c->counters.p));
   MF_CUDA(cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
   MF_CUDA(cudaStreamSynchronize(s));
   if (c->h_counters[0] > 0) MF_FAIL(MF_ESTATE, "compaction computed a negative degree: delta is inconsistent with the base graph");
@@ -461,7 +461,7 @@ void compact_graph(mf_ctx* c, std::vector<int64_t>& nindex_out, std::vector<int3
   MF_CUDA(cudaStreamSynchronize(s));
   DBuf<int32_t> out;
   out.reserve(std::max<int64_t>(total, 1));
-  if (n > 0) k_compact_gather<<<grid_for((int64_t)n * 32), kTB, 0, s>>>(c->view(), c->i64b.p, out.p);
+  if (n > 0) MF_K(k_compact_gather<<<grid_for((int64_t)n * 32), kTB, 0, s>>>(c->view(), c->i64b.p, out.p));
   MF_CUDA(cudaGetLastError());
   nindex_out.resize((size_t)n + 1);
   nlist_out.resize((size_t)total);
@@ -480,13 +480,13 @@ void greedy_mis(mf_ctx* c, uint8_t* d_out) {
   MF_CUDA(cudaMemsetAsync(st.p, 0, (size_t)n, s));
   for (int round = 0;; ++round) {
     MF_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int64_t), s));
-    k_greedy_round<<<grid_for(n), kTB, 0, s>>>(c->view(), c->rows_sorted, st.p, c->counters.p);
+    MF_K(k_greedy_round<<<grid_for(n), kTB, 0, s>>>(c->view(), c->rows_sorted, st.p, c->counters.p));
     MF_CUDA(cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     if (c->h_counters[0] == 0) break;
     if (round > n + 2) MF_FAIL(MF_ESTATE, "greedy MIS did not settle");
   }
-  k_greedy_out<<<grid_for(n), kTB, 0, s>>>(st.p, n, d_out);
+  MF_K(k_greedy_out<<<grid_for(n), kTB, 0, s>>>(st.p, n, d_out));
   MF_CUDA(cudaStreamSynchronize(s));
   st.release();
 }
@@ -494,7 +494,7 @@ void greedy_mis(mf_ctx* c, uint8_t* d_out) {
 void check_mis(mf_ctx* c, int64_t* viol, int64_t* uncovered) {
   cudaStream_t s = c->stream;
   MF_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int64_t) * 2, s));
-  if (c->n > 0) k_check_mis<<<grid_for(c->n), kTB, 0, s>>>(c->view(), c->mis.p, c->counters.p);
+  if (c->n > 0) MF_K(k_check_mis<<<grid_for(c->n), kTB, 0, s>>>(c->view(), c->mis.p, c->counters.p));
   MF_CUDA(cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
   MF_CUDA(cudaStreamSynchronize(s));
   *viol = c->h_counters[0];

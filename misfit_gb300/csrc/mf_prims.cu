@@ -141,9 +141,9 @@ void scan_exclusive(L load, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s
   }
   const int64_t nb = (n + kTile - 1) / kTile;
   ws.block_sums.reserve(nb + 1);
-  k_tile_reduce<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p);
-  k_scan_sums<<<1, kThreads, 0, s>>>(ws.block_sums.p, nb);
-  k_tile_scan<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p, out);
+  MF_K(k_tile_reduce<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p));
+  MF_K(k_scan_sums<<<1, kThreads, 0, s>>>(ws.block_sums.p, nb));
+  MF_K(k_tile_scan<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p, out));
   MF_CUDA(cudaGetLastError());
 }
 
@@ -243,9 +243,9 @@ void radix_sort_pairs(uint64_t* keys, uint32_t* vals, int64_t n, int bits, Scrat
   const int passes = (bits + 7) / 8;
   for (int pass = 0; pass < passes; ++pass) {
     const int shift = pass * 8;
-    k_radix_hist<<<nblocks, kThreads, 0, s>>>(ka, n, shift, ws.hist.p, nblocks);
+    MF_K(k_radix_hist<<<nblocks, kThreads, 0, s>>>(ka, n, shift, ws.hist.p, nblocks));
     scan_exclusive_i32(ws.hist.p, ws.hist_scan.p, (int64_t)256 * nblocks, ws, s);
-    k_radix_scatter<<<nblocks, kThreads, 0, s>>>(ka, va, n, shift, ws.hist_scan.p, nblocks, kb, vb);
+    MF_K(k_radix_scatter<<<nblocks, kThreads, 0, s>>>(ka, va, n, shift, ws.hist_scan.p, nblocks, kb, vb));
     MF_CUDA(cudaGetLastError());
     uint64_t* tk = ka; ka = kb; kb = tk;
     uint32_t* tv = va; va = vb; vb = tv;

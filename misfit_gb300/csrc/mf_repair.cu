@@ -19,7 +19,9 @@
 //   highest row writes last); assignment by ascending sub-batch index (lists
 //   walked descending); clusters processed in ascending id.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <optional>
 
 #include "mf_internal.cuh"
 
@@ -557,6 +559,388 @@ __global__ void __launch_bounds__(1024) k_repair_sequential(RepairArgs a) {
   }
 }
 
+// ---- speculative repair ---------------------------------------------------------------------
+// The repair order is a total order of edges; the result must equal walking
+// it one edge at a time.  Each round evaluates every pending edge (one warp
+// per edge) against a view: the committed membership plus the writes that the
+// previous round's evaluations made at earlier positions.  The first position
+// whose writes changed since the previous round is final together with
+// everything before it (each of those saw exactly the writes of its
+// predecessors), so that prefix is committed and the next round starts after
+// it.  Independent edges settle in the same round; a chain of k dependent
+// edges needs k rounds.  After kMaxRounds rounds the remainder is walked by
+// the sequential kernel.
+
+constexpr int kMaxRounds = 48;
+constexpr int64_t kBigThreshold = 4096;   // hop-2 volume above which the grid-wide search runs
+
+struct View {
+  const uint8_t* m;     // bit 0: committed membership; bit 1: pending writes exist
+  const uint64_t* keys; // pending writes sorted by (vertex << 32 | position)
+  const uint32_t* vals;
+  int64_t nkeys;
+};
+
+__device__ __forceinline__ int view_get(const View& V, int32_t x, uint32_t t) {
+  const uint8_t b = V.m[x];
+  if (!(b & 2)) return b & 1;
+  const uint64_t q = ((uint64_t)(uint32_t)x << 32) | t;
+  int64_t lo = 0, hi = V.nkeys;  // first key >= q
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (V.keys[mid] < q) lo = mid + 1; else hi = mid;
+  }
+  if (lo > 0 && (uint32_t)(V.keys[lo - 1] >> 32) == (uint32_t)x) return (int)V.vals[lo - 1];
+  return b & 1;
+}
+
+struct SpecArgs {
+  GraphView g;
+  const int32_t* u;
+  const int32_t* v;
+  const uint8_t* ins;
+  int64_t p;
+  const uint32_t* order;
+  int64_t p0, cnt, ns;
+  const int32_t* v2i;
+  View view;
+  int32_t* out0;   // vertex written first (removal for an insert, join for a delete) or -1
+  int32_t* out1;   // vertex that joins after an insert's removal, or -1
+  // deferral of long hop-2 searches to the grid-wide kernel
+  int64_t big_threshold;
+  unsigned long long* big_count;
+  int64_t* big_pos;       // repair position of each deferred edge
+  int32_t* big_r;         // its removed vertex r
+  int64_t* big_off;       // offset of its prefix array in `pre`
+  int64_t* big_nr;        // entries of row(r)
+  int64_t* pre;           // prefix sums of len(h) over row(r), nr + 1 entries per deferred edge
+  unsigned long long* pre_used;
+  int64_t pre_cap;
+};
+
+constexpr int32_t kDeferred = -2;
+
+// Membership seen by the edge at position t (its own removal of `self0` applied).
+struct Member {
+  const View* V;
+  uint32_t t;
+  int32_t self0;
+  __device__ __forceinline__ int operator()(int32_t x) const { return x == self0 ? 0 : view_get(*V, x, t); }
+};
+
+__device__ __forceinline__ bool spec_seed(const SpecArgs& a, int32_t x) {
+  const int32_t i = a.v2i[x];
+  return i >= 0 && (int64_t)i < a.ns;
+}
+
+__device__ bool t_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t except) {
+  auto hit = [&](int32_t z) { return z != except && mem(z) != 0; };
+  if (!spec_seed(a, x)) return thread_row_until(a.g, x, hit);
+  if (hit(x)) return true;
+  if (thread_row_until(a.g, x, hit)) return true;
+  return thread_row_until(a.g, x, [&](int32_t h) { return thread_row_until(a.g, h, hit); });
+}
+
+__device__ bool t_eligible(const SpecArgs& a, const Member& mem, int32_t w) {
+  if (mem(w)) return false;
+  if (a.v2i[w] < 0) return false;
+  return !t_any(a, mem, w, -1);
+}
+
+// Warp: does row-of(x) hold a member other than `except`?
+__device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t except) {
+  const GraphView& g = a.g;
+  const int lane = threadIdx.x & 31;
+  auto hit = [&](int32_t z) { return z != except && mem(z) != 0; };
+  const bool seed = spec_seed(a, x);
+  if (seed && hit(x)) return true;
+  int32_t dummy;
+  if (warp_row_first(g, x, hit, &dummy)) return true;
+  if (!seed) return false;
+  const int64_t nb = g.nindex[x + 1] - g.nindex[x];
+  const int64_t nr = nb + (g.aoff[x + 1] - g.aoff[x]);
+  for (int64_t k0 = 0; k0 < nr; k0 += 32) {
+    const int64_t k = k0 + lane;
+    const int32_t h = k < nr ? row_elem(g, x, k, nb) : -1;
+    bool found = false, longrow = false;
+    if (h >= 0) {
+      if (row_len(g, h) <= 64) found = thread_row_until(g, h, hit);
+      else longrow = true;
+    }
+    if (__any_sync(0xffffffffu, found)) return true;
+    unsigned lm = __ballot_sync(0xffffffffu, longrow);
+    while (lm) {
+      const int src = __ffs(lm) - 1;
+      lm &= lm - 1;
+      const int32_t hh = __shfl_sync(0xffffffffu, h, src);
+      if (warp_row_first(g, hh, hit, &dummy)) return true;
+    }
+  }
+  return false;
+}
+
+// Warp: first eligible w of row-of(r) in order (src/misfit/misfit.cu:300-314), or -1.
+__device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_t r) {
+  const GraphView& g = a.g;
+  const int lane = threadIdx.x & 31;
+  const bool seed = spec_seed(a, r);
+  if (seed) {
+    const int e = (lane == 0 && t_eligible(a, mem, r)) ? 1 : 0;
+    if (__shfl_sync(0xffffffffu, e, 0)) return r;
+  }
+  auto pred = [&](int32_t z) { return t_eligible(a, mem, z); };
+  int32_t w = -1;
+  if (warp_row_first(g, r, pred, &w)) return w;
+  if (!seed) return -1;
+  const int64_t nb = g.nindex[r + 1] - g.nindex[r];
+  const int64_t nr = nb + (g.aoff[r + 1] - g.aoff[r]);
+  // Volume of the hop-2 part; long ones go to the grid-wide search.
+  int64_t vol = 0;
+  for (int64_t k = lane; k < nr; k += 32) {
+    const int32_t h = row_elem(g, r, k, nb);
+    if (h >= 0) vol += row_len(g, h);
+  }
+  for (int o = 16; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
+  if (vol > a.big_threshold) {
+    unsigned long long off = 0;
+    if (lane == 0) off = atomicAdd(a.pre_used, (unsigned long long)(nr + 1));
+    off = __shfl_sync(0xffffffffu, off, 0);
+    if ((int64_t)(off + nr + 1) <= a.pre_cap) {
+      int64_t carry = 0;
+      for (int64_t k0 = 0; k0 < nr; k0 += 32) {
+        const int64_t k = k0 + lane;
+        int64_t len = 0;
+        if (k < nr) {
+          const int32_t h = row_elem(g, r, k, nb);
+          if (h >= 0) len = row_len(g, h);
+        }
+        int64_t inc = len;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += t;
+        }
+        if (k < nr) a.pre[off + k] = carry + inc - len;
+        carry += __shfl_sync(0xffffffffu, inc, 31);
+      }
+      if (lane == 0) {
+        a.pre[off + nr] = carry;
+        const unsigned long long b = atomicAdd(a.big_count, 1ull);
+        a.big_pos[b] = (int64_t)mem.t;
+        a.big_r[b] = r;
+        a.big_off[b] = (int64_t)off;
+        a.big_nr[b] = nr;
+      }
+      return kDeferred;
+    }
+  }
+  for (int64_t k = 0; k < nr; ++k) {
+    const int32_t h = row_elem(g, r, k, nb);
+    if (h < 0) continue;
+    if (warp_row_first(g, h, pred, &w)) return w;
+  }
+  return -1;
+}
+
+__global__ void k_spec_eval(SpecArgs a) {
+  const int64_t wi = warp_id();
+  if (wi >= a.cnt - a.p0) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t pos = a.p0 + wi;
+  const int64_t j = a.p + a.order[pos];
+  const int32_t x = a.u[j], y = a.v[j];
+  const bool ins = a.ins[j] != 0;
+  Member mem{&a.view, (uint32_t)pos, -1};
+  const int mx = mem(x), my = mem(y);
+  int32_t o0 = -1, o1 = -1;
+  if (ins) {
+    if (mx && my) {
+      const int32_t r = x > y ? x : y;
+      o0 = r;
+      mem.self0 = r;
+      if (a.v2i[r] >= 0) o1 = w_first_eligible(a, mem, r);
+    }
+  } else if (mx != my) {
+    const int32_t yy = mx ? y : x, keep = mx ? x : y;
+    if (a.v2i[yy] < 0 || !w_any(a, mem, yy, keep)) o0 = yy;
+  }
+  if (lane == 0) {
+    a.out0[pos] = o0;
+    a.out1[pos] = o1;
+  }
+}
+
+constexpr int64_t kBigChunk = 2048;
+
+// Chunk prefix over the deferred edges (one block): chunk_pre[i] = first chunk
+// of deferred edge i, chunk_pre[nbig] = total; best[i] = none.
+__global__ void k_big_prep(SpecArgs a, int64_t* chunk_pre, unsigned long long* best, unsigned long long* queue) {
+  const int64_t nbig = (int64_t)*a.big_count;
+  __shared__ int64_t s_carry;
+  if (threadIdx.x == 0) { s_carry = 0; *queue = 0; }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ int64_t s_w[32];
+  for (int64_t base = 0; base < nbig; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    int64_t cnt = 0;
+    if (i < nbig) {
+      const int64_t vol = a.pre[a.big_off[i] + a.big_nr[i]];
+      cnt = (vol + kBigChunk - 1) / kBigChunk;
+      best[i] = ~0ull;
+    }
+    int64_t inc = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) s_w[wid] = inc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int64_t acc = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { const int64_t t = s_w[k]; s_w[k] = acc; acc += t; }
+    }
+    __syncthreads();
+    if (i < nbig) chunk_pre[i] = s_carry + s_w[wid] + inc - cnt;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_carry += s_w[wid] + inc;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) chunk_pre[nbig] = s_carry;
+}
+
+// Grid-wide first-eligible search over the flattened hop-2 sequences of the
+// deferred edges; chunks are handed out in increasing position order.
+__global__ void __launch_bounds__(256) k_big_scan(SpecArgs a, const int64_t* chunk_pre, unsigned long long* best,
+                                                  unsigned long long* queue) {
+  const GraphView& g = a.g;
+  const int64_t nbig = (int64_t)*a.big_count;
+  const int64_t total = chunk_pre[nbig];
+  __shared__ unsigned long long s_chunk;
+  __shared__ unsigned long long s_best;
+  while (true) {
+    if (threadIdx.x == 0) s_chunk = atomicAdd(queue, 1ull);
+    __syncthreads();
+    const int64_t chunk = (int64_t)s_chunk;
+    if (chunk >= total) break;
+    int64_t lo = 0, hi = nbig;  // last i with chunk_pre[i] <= chunk
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (chunk_pre[mid] <= chunk) lo = mid; else hi = mid;
+    }
+    const int64_t i = lo;
+    const int64_t p0 = (chunk - chunk_pre[i]) * kBigChunk;
+    const int64_t* pre = a.pre + a.big_off[i];
+    const int64_t nr = a.big_nr[i];
+    const int64_t vol = pre[nr];
+    const int32_t r = a.big_r[i];
+    if (threadIdx.x == 0) s_best = ~0ull;
+    __syncthreads();
+    if ((unsigned long long)p0 < best[i]) {
+      Member mem{&a.view, (uint32_t)a.big_pos[i], r};
+      const int64_t rb = g.nindex[r + 1] - g.nindex[r];
+      for (int64_t q = p0 + threadIdx.x; q < p0 + kBigChunk && q < vol; q += blockDim.x) {
+        int64_t klo = 0, khi = nr;  // last k with pre[k] <= q
+        while (khi - klo > 1) {
+          const int64_t mid = (klo + khi) >> 1;
+          if (pre[mid] <= q) klo = mid; else khi = mid;
+        }
+        const int32_t h = row_elem(g, r, klo, rb);
+        if (h < 0) continue;
+        const int32_t z = row_elem(g, h, q - pre[klo], g.nindex[h + 1] - g.nindex[h]);
+        if (z >= 0 && t_eligible(a, mem, z)) atomicMin(&s_best, (unsigned long long)q);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_best != ~0ull) atomicMin(best + i, s_best);
+    __syncthreads();
+  }
+}
+
+__global__ void k_big_finalize(SpecArgs a, const unsigned long long* best) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)*a.big_count) return;
+  const GraphView& g = a.g;
+  int32_t w = -1;
+  if (best[i] != ~0ull) {
+    const int64_t q = (int64_t)best[i];
+    const int64_t* pre = a.pre + a.big_off[i];
+    const int64_t nr = a.big_nr[i];
+    const int32_t r = a.big_r[i];
+    int64_t klo = 0, khi = nr;
+    while (khi - klo > 1) {
+      const int64_t mid = (klo + khi) >> 1;
+      if (pre[mid] <= q) klo = mid; else khi = mid;
+    }
+    const int32_t h = row_elem(g, r, klo, g.nindex[r + 1] - g.nindex[r]);
+    w = row_elem(g, h, q - pre[klo], g.nindex[h + 1] - g.nindex[h]);
+  }
+  a.out1[a.big_pos[i]] = w;
+}
+
+__global__ void k_spec_first_change(const int32_t* n0, const int32_t* n1, const int32_t* r0, const int32_t* r1,
+                                    int64_t p0, int64_t cnt, unsigned long long* out) {
+  const int64_t pos = p0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos < cnt && (n0[pos] != r0[pos] || n1[pos] != r1[pos])) atomicMin(out, (unsigned long long)pos);
+}
+
+__global__ void k_spec_count(const int32_t* n0, const int32_t* n1, int64_t p0, int64_t cnt, uint8_t* c) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p0 + i < cnt) c[i] = (uint8_t)((n0[p0 + i] >= 0) + (n1[p0 + i] >= 0));
+}
+
+__global__ void k_spec_fill(const int32_t* n0, const int32_t* n1, const int64_t* pos_out, int64_t p0, int64_t cnt,
+                            const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t p, const uint32_t* order,
+                            uint64_t* keys, uint32_t* vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p0 + i >= cnt) return;
+  const int64_t pos = p0 + i;
+  int64_t k = pos_out[i];
+  const int32_t a = n0[pos], b = n1[pos];
+  if (a >= 0) {
+    keys[k] = ((uint64_t)(uint32_t)a << 32) | (uint64_t)pos;
+    vals[k] = ins[p + order[pos]] ? 0u : 1u;
+    ++k;
+  }
+  if (b >= 0) {
+    keys[k] = ((uint64_t)(uint32_t)b << 32) | (uint64_t)pos;
+    vals[k] = 1u;
+  }
+}
+
+__global__ void k_spec_clear_flags(const uint64_t* keys, int64_t nk, uint8_t* m) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nk) m[keys[k] >> 32] &= 1;
+}
+
+// Commit every write at a position <= f that is the last such write to its vertex.
+__global__ void k_spec_commit(const uint64_t* keys, const uint32_t* vals, int64_t nk, uint64_t f, uint8_t* m) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  const uint64_t key = keys[k];
+  if ((key & 0xffffffffull) > f) return;
+  if (k + 1 < nk) {
+    const uint64_t nx = keys[k + 1];
+    if ((nx >> 32) == (key >> 32) && (nx & 0xffffffffull) <= f) return;
+  }
+  m[key >> 32] = (uint8_t)vals[k];
+}
+
+__global__ void k_spec_keep_flags(const uint64_t* keys, int64_t nk, uint64_t f, uint8_t* m, uint8_t* keep) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  const bool later = (keys[k] & 0xffffffffull) > f;
+  keep[k] = later ? 1 : 0;
+  if (later) m[keys[k] >> 32] |= 2;
+}
+
+__global__ void k_spec_compact(const uint64_t* keys, const uint32_t* vals, const uint8_t* keep, const int64_t* pos,
+                               int64_t nk, uint64_t* okeys, uint32_t* ovals) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk || !keep[k]) return;
+  okeys[pos[k]] = keys[k];
+  ovals[pos[k]] = vals[k];
+}
+
 __global__ void k_clear(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, int32_t* cid,
                         int32_t* v2i) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -585,6 +969,119 @@ void next_epoch(mf_ctx* c) {
   ++c->epoch;
 }
 
+
+int64_t big_threshold() {
+  static const int64_t v = [] {
+    const char* e = std::getenv("MISFIT_GB_BIG_THRESHOLD");
+    return e ? std::max<int64_t>(0, std::atoll(e)) : kBigThreshold;
+  }();
+  return v;
+}
+
+bool sequential_repair_forced() {
+  static const bool forced = [] {
+    const char* e = std::getenv("MISFIT_GB_REPAIR");
+    return e != nullptr && std::strcmp(e, "sequential") == 0;
+  }();
+  return forced;
+}
+
+// Repair of one sub-batch: c->vals holds the order (sub-batch indices),
+// nproc entries.  Returns the number of speculative rounds.
+int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t ns) {
+  cudaStream_t s = c->stream;
+  int64_t* h = c->h_counters;
+  unsigned long long* ucnt = reinterpret_cast<unsigned long long*>(c->counters.p);
+  const uint32_t* order = c->vals.p;
+  if (sequential_repair_forced()) {
+    RepairArgs ra{g, c->bu.p, c->bv.p, c->bins.p, p, order, nproc, ns, c->v2i.p, c->mis.p};
+    MF_K(k_repair_sequential<<<1, 1024, 0, s>>>(ra));
+    MF_CUDA(cudaGetLastError());
+    return 0;
+  }
+  c->rp_w0.reserve(nproc);
+  c->rp_w1.reserve(nproc);
+  c->rp_n0.reserve(nproc);
+  c->rp_n1.reserve(nproc);
+  c->rp_keys.reserve(2 * nproc);
+  c->rp_vals.reserve(2 * nproc);
+  c->rp_keys2.reserve(2 * nproc);
+  c->rp_vals2.reserve(2 * nproc);
+  c->rp_u8.reserve(2 * nproc);
+  c->rp_pos.reserve(2 * nproc + 1);
+  c->big_pos.reserve(nproc);
+  c->big_r.reserve(nproc);
+  c->big_off.reserve(nproc);
+  c->big_nr.reserve(nproc);
+  c->big_chunks.reserve(nproc + 1);
+  c->big_best.reserve(nproc);
+  c->big_pre.reserve((int64_t)1 << 22);
+  if (c->big_grid == 0) {
+    int sms = 0;
+    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    c->big_grid = 4 * sms;
+  }
+  MF_CUDA(cudaMemsetAsync(c->rp_w0.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
+  MF_CUDA(cudaMemsetAsync(c->rp_w1.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
+  const int nbits = bits_for(std::max<int32_t>(c->n - 1, 1));
+  int64_t p0 = 0, nview = 0, rounds = 0;
+  while (p0 < nproc) {
+    if (rounds >= kMaxRounds) {
+      if (nview > 0) MF_K(k_spec_clear_flags<<<grid_for(nview), kTB, 0, s>>>(c->rp_keys.p, nview, c->mis.p));
+      RepairArgs ra{g, c->bu.p, c->bv.p, c->bins.p, p, order + p0, nproc - p0, ns, c->v2i.p, c->mis.p};
+      MF_K(k_repair_sequential<<<1, 1024, 0, s>>>(ra));
+      MF_CUDA(cudaGetLastError());
+      break;
+    }
+    ++rounds;
+    const int64_t pending = nproc - p0;
+    MF_CUDA(cudaMemsetAsync(c->counters.p + 24, 0, sizeof(int64_t) * 2, s));
+    SpecArgs a{g, c->bu.p, c->bv.p, c->bins.p, p, order, p0, nproc, ns, c->v2i.p,
+               View{c->mis.p, c->rp_keys.p, c->rp_vals.p, nview}, c->rp_n0.p, c->rp_n1.p,
+               big_threshold(), ucnt + 24, c->big_pos.p, c->big_r.p, c->big_off.p, c->big_nr.p,
+               c->big_pre.p, ucnt + 25, c->big_pre.cap};
+    MF_K(k_spec_eval<<<warps_grid(pending), kTB, 0, s>>>(a));
+    MF_K(k_big_prep<<<1, 1024, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
+    MF_K(k_big_scan<<<(unsigned)c->big_grid, 256, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
+    MF_K(k_big_finalize<<<grid_for(pending), kTB, 0, s>>>(a, c->big_best.p));
+    h[20] = (int64_t)nproc;
+    MF_CUDA(cudaMemcpyAsync(c->counters.p + 20, h + 20, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    MF_K(k_spec_first_change<<<grid_for(pending), kTB, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0,
+                                                                 nproc, ucnt + 20));
+    // all writes of this round, sorted by (vertex, position)
+    MF_K(k_spec_count<<<grid_for(pending), kTB, 0, s>>>(c->rp_n0.p, c->rp_n1.p, p0, nproc, c->rp_u8.p));
+    scan_exclusive_u8(c->rp_u8.p, c->rp_pos.p, pending, c->ws, s);
+    MF_CUDA(cudaMemcpyAsync(h + 21, c->rp_pos.p + pending, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaMemcpyAsync(h + 20, c->counters.p + 20, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_K(k_spec_fill<<<grid_for(pending), kTB, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_pos.p, p0, nproc, c->bu.p,
+                                                         c->bv.p, c->bins.p, p, order, c->rp_keys2.p,
+                                                         c->rp_vals2.p));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t f = h[20];          // first changed position, nproc when none
+    const int64_t nk = h[21];
+    radix_sort_pairs(c->rp_keys2.p, c->rp_vals2.p, nk, 32 + nbits, c->ws, s);
+    if (nview > 0) MF_K(k_spec_clear_flags<<<grid_for(nview), kTB, 0, s>>>(c->rp_keys.p, nview, c->mis.p));
+    const uint64_t last = (uint64_t)std::min<int64_t>(f, nproc - 1);
+    if (nk > 0) MF_K(k_spec_commit<<<grid_for(nk), kTB, 0, s>>>(c->rp_keys2.p, c->rp_vals2.p, nk, last, c->mis.p));
+    if (f >= nproc) break;
+    nview = 0;
+    if (nk > 0) {
+      MF_K(k_spec_keep_flags<<<grid_for(nk), kTB, 0, s>>>(c->rp_keys2.p, nk, last, c->mis.p, c->rp_u8.p));
+      scan_exclusive_u8(c->rp_u8.p, c->rp_pos.p, nk, c->ws, s);
+      MF_K(k_spec_compact<<<grid_for(nk), kTB, 0, s>>>(c->rp_keys2.p, c->rp_vals2.p, c->rp_u8.p, c->rp_pos.p, nk,
+                                                         c->rp_keys.p, c->rp_vals.p));
+      MF_CUDA(cudaMemcpyAsync(h + 22, c->rp_pos.p + nk, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaStreamSynchronize(s));
+      nview = h[22];
+    }
+    std::swap(c->rp_w0, c->rp_n0);
+    std::swap(c->rp_w1, c->rp_n1);
+    p0 = f + 1;
+  }
+  MF_CUDA(cudaGetLastError());
+  return rounds;
+}
+
 }  // namespace
 
 void process_batch(mf_ctx* c, int64_t m) {
@@ -601,10 +1098,13 @@ void process_batch(mf_ctx* c, int64_t m) {
   c->keys.reserve(2 * m);
   c->vals.reserve(2 * m);
   c->prev.reserve(2 * m);
-  k_slot_keys<<<grid_for(2 * m), kTB, 0, s>>>(c->bu.p, c->bv.p, m, sbits, c->keys.p, c->vals.p);
+  std::optional<StageScope> sc;
+  sc.emplace(c, kStSplit);
+  MF_K(k_slot_keys<<<grid_for(2 * m), kTB, 0, s>>>(c->bu.p, c->bv.p, m, sbits, c->keys.p, c->vals.p));
   radix_sort_pairs(c->keys.p, c->vals.p, 2 * m, sbits + nbits, c->ws, s);
-  k_prev<<<grid_for(2 * m), kTB, 0, s>>>(c->keys.p, c->vals.p, 2 * m, sbits, c->prev.p);
+  MF_K(k_prev<<<grid_for(2 * m), kTB, 0, s>>>(c->keys.p, c->vals.p, 2 * m, sbits, c->prev.p));
   MF_CUDA(cudaGetLastError());
+  sc.reset();
 
   const int64_t big = 2 * std::min<int64_t>(m, kMaxBatchEdges) + (int64_t)n + 2;
   c->i64a.reserve(big);
@@ -620,11 +1120,12 @@ void process_batch(mf_ctx* c, int64_t m) {
   while (p < m) {
     const int64_t len = std::min<int64_t>(m - p, kMaxBatchEdges);
     // ---- split
-    k_contrib<<<grid_for(len), kTB, 0, s>>>(c->bu.p, c->bv.p, c->prev.p, c->deg.p, p, len, c->i64a.p);
+    sc.emplace(c, kStSplit);
+    MF_K(k_contrib<<<grid_for(len), kTB, 0, s>>>(c->bu.p, c->bv.p, c->prev.p, c->deg.p, p, len, c->i64a.p));
     scan_exclusive_i64(c->i64a.p, c->i64b.p, len, c->ws, s);
     const int64_t lenv = len;
     MF_CUDA(cudaMemcpyAsync(cnt, &lenv, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    k_find_cut<<<grid_for(len), kTB, 0, s>>>(c->i64b.p, len, c->max_csr, ucnt);
+    MF_K(k_find_cut<<<grid_for(len), kTB, 0, s>>>(c->i64b.p, len, c->max_csr, ucnt));
     MF_CUDA(cudaMemcpyAsync(h, cnt, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t q = p + h[0];
@@ -632,23 +1133,25 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_CUDA(cudaMemcpyAsync(&est, c->i64b.p + (q - p), sizeof(int64_t), cudaMemcpyDeviceToHost, s));
 
     // ---- seeds (first appearance)
+    sc.emplace(c, kStSeeds);
     const int64_t nslots = 2 * (q - p);
-    k_seed_flags<<<grid_for(nslots), kTB, 0, s>>>(c->prev.p, p, q, c->u8a.p);
+    MF_K(k_seed_flags<<<grid_for(nslots), kTB, 0, s>>>(c->prev.p, p, q, c->u8a.p));
     scan_exclusive_u8(c->u8a.p, c->i64a.p, nslots, c->ws, s);
-    k_seed_compact<<<grid_for(nslots), kTB, 0, s>>>(c->bu.p, c->bv.p, c->u8a.p, c->i64a.p, p, q, c->seeds.p, c->v2i.p);
+    MF_K(k_seed_compact<<<grid_for(nslots), kTB, 0, s>>>(c->bu.p, c->bv.p, c->u8a.p, c->i64a.p, p, q, c->seeds.p, c->v2i.p));
     MF_CUDA(cudaMemcpyAsync(h + 1, c->i64a.p + nslots, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t ns = h[1];
 
     // ---- hop-1 set, candidates in ascending id
+    sc.emplace(c, kStHop1);
     next_epoch(c);
     const uint32_t ep = c->epoch;
     MF_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int64_t), s));
-    k_mark_hop1<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->hmark.p, c->hlist.p, ucnt + 2);
-    k_cand_flags<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->v2i.p, n, ep, c->u8a.p);
+    MF_K(k_mark_hop1<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->hmark.p, c->hlist.p, ucnt + 2));
+    MF_K(k_cand_flags<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->v2i.p, n, ep, c->u8a.p));
     scan_exclusive_u8(c->u8a.p, c->i64a.p, n, c->ws, s);
     const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
-    k_cand_compact<<<grid_for(n), kTB, 0, s>>>(c->u8a.p, c->i64a.p, n, capc, ns, c->cands.p, c->v2i.p);
+    MF_K(k_cand_compact<<<grid_for(n), kTB, 0, s>>>(c->u8a.p, c->i64a.p, n, capc, ns, c->cands.p, c->v2i.p));
     MF_CUDA(cudaMemcpyAsync(h + 3, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaMemcpyAsync(h + 2, cnt + 2, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
@@ -657,8 +1160,9 @@ void process_batch(mf_ctx* c, int64_t m) {
     const int64_t rows = ns + nct;
 
     // ---- packed sizes and MAX_CSR_ELEMENTS growth
+    sc.emplace(c, kStSizes);
     MF_CUDA(cudaMemsetAsync(cnt + 4, 0, sizeof(int64_t), s));
-    k_size_bound<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, ucnt + 4);
+    MF_K(k_size_bound<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, ucnt + 4));
     MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     int64_t packed = -1;
@@ -676,13 +1180,13 @@ void process_batch(mf_ctx* c, int64_t m) {
         MF_CUDA(cudaMemsetAsync(c->bitmaps.p, 0, sizeof(uint32_t) * (size_t)(ctas * c->bitmap_words), s));
       }
       if (ns > 0)
-        k_two_hop_sizes<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ns), 512, 0, s>>>(
-            g, c->seeds.p, ns, c->bitmaps.p, c->bitmap_words, c->rowlens.p);
-      k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns);
+        MF_K(k_two_hop_sizes<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ns), 512, 0, s>>>(
+            g, c->seeds.p, ns, c->bitmaps.p, c->bitmap_words, c->rowlens.p));
+      MF_K(k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns));
       scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
       h[5] = c->max_csr;
       MF_CUDA(cudaMemcpyAsync(cnt + 5, h + 5, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-      k_growth<<<1, 32, 0, s>>>(c->i64a.p, rows, cnt + 5);
+      MF_K(k_growth<<<1, 32, 0, s>>>(c->i64a.p, rows, cnt + 5));
       MF_CUDA(cudaMemcpyAsync(h + 5, cnt + 5, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
       MF_CUDA(cudaStreamSynchronize(s));
       c->max_csr = h[5];
@@ -692,26 +1196,29 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_CUDA(cudaGetLastError());
 
     // ---- clustering (bulk-synchronous)
-    k_first_cid<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->cid.p, c->f1.p);
-    k_first_cid<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, c->cid.p, c->f1.p);
-    k_row_decide<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->f1.p,
-                                                  c->rowcid.p, c->creates.p);
+    sc.emplace(c, kStFirst);
+    MF_K(k_first_cid<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->cid.p, c->f1.p));
+    MF_K(k_first_cid<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, c->cid.p, c->f1.p));
+    MF_K(k_row_decide<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->f1.p,
+                                                  c->rowcid.p, c->creates.p));
     scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
-    k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p);
+    MF_K(k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p));
     MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    k_push_seed<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->rowcid.p, ep, c->bval.p);
+    sc.emplace(c, kStPush);
+    MF_K(k_push_seed<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
     MF_CUDA(cudaMemsetAsync(cnt + 8, 0, sizeof(int64_t), s));
-    k_push_hop<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8);
-    k_push_hop<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8);
-    k_push_cand<<<warps_grid(nct), kTB, 0, s>>>(g, c->cands.p, nct, ns, c->rowcid.p, ep, c->wval.p, c->touched.p,
-                                                ucnt + 8);
+    MF_K(k_push_hop<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
+    MF_K(k_push_hop<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
+    MF_K(k_push_cand<<<warps_grid(nct), kTB, 0, s>>>(g, c->cands.p, nct, ns, c->rowcid.p, ep, c->wval.p, c->touched.p,
+                                                ucnt + 8));
     MF_CUDA(cudaMemcpyAsync(h + 8, cnt + 8, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t cc = h[7];
     const int64_t ntouched = h[8];
-    k_finalize_cid<<<grid_for(ntouched), kTB, 0, s>>>(c->touched.p, ntouched, c->wval.p, c->rowcid.p, c->cid.p);
+    MF_K(k_finalize_cid<<<grid_for(ntouched), kTB, 0, s>>>(c->touched.p, ntouched, c->wval.p, c->rowcid.p, c->cid.p));
     MF_CUDA(cudaGetLastError());
 
+    sc.reset();
     SubBatchTrace* tr = nullptr;
     if (c->trace) {
       c->traces.emplace_back();
@@ -725,20 +1232,19 @@ void process_batch(mf_ctx* c, int64_t m) {
     }
 
     // ---- assignment + order (cluster ascending, index descending)
+    sc.emplace(c, kStAssign);
     const int64_t limit = std::min<int64_t>(cc, kMaxBatchEdges);
     MF_CUDA(cudaMemsetAsync(cnt + 9, 0, sizeof(int64_t), s));
-    k_assign<<<grid_for(q - p), kTB, 0, s>>>(c->bu.p, c->bv.p, p, q - p, c->cid.p, limit, c->keys.p, c->vals.p, ucnt + 9);
+    MF_K(k_assign<<<grid_for(q - p), kTB, 0, s>>>(c->bu.p, c->bv.p, p, q - p, c->cid.p, limit, c->keys.p, c->vals.p, ucnt + 9));
     MF_CUDA(cudaMemcpyAsync(h + 9, cnt + 9, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t nproc = h[9];
     radix_sort_pairs(c->keys.p, c->vals.p, nproc, kRowBits + bits_for(std::max<int64_t>(limit, 1)), c->ws, s);
 
     // ---- repair
-    if (nproc > 0) {
-      RepairArgs ra{g, c->bu.p, c->bv.p, c->bins.p, p, c->vals.p, nproc, ns, c->v2i.p, c->mis.p};
-      k_repair_sequential<<<1, 1024, 0, s>>>(ra);
-      MF_CUDA(cudaGetLastError());
-    }
+    sc.emplace(c, kStRepair);
+    if (nproc > 0) c->stats.repair_rounds += repair(c, g, p, nproc, ns);
+    sc.reset();
     if (tr) {
       tr->hdr[7] = nproc;
       std::vector<uint32_t> ord = fetch(c->vals.p, nproc, s);
@@ -748,9 +1254,11 @@ void process_batch(mf_ctx* c, int64_t m) {
     }
 
     // ---- clear (mapped vertices only)
-    k_clear<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->v2i.p);
+    sc.emplace(c, kStClear);
+    MF_K(k_clear<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->v2i.p));
     MF_CUDA(cudaGetLastError());
 
+    sc.reset();
     c->stats.sub_batches += 1;
     c->stats.seeds += ns;
     c->stats.candidates += nct;

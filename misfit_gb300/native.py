@@ -21,7 +21,8 @@ EXPORTS = [
     "mf_last_batch_stats", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
     "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_compact", "mf_read_mis_file",
     "mf_write_mis_file", "mf_read_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
-    "mf_trace_count", "mf_trace_get",
+    "mf_trace_count", "mf_trace_get", "mf_stage_name", "mf_profile_enable", "mf_profile_reset",
+    "mf_profile_read", "mf_kernel_launches",
 ]
 
 
@@ -90,6 +91,11 @@ def _lib():
         "mf_read_batch_file": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(_I32P), C.POINTER(_I32P), _I64P]),
         "mf_list_batch_files": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), _I64P]),
         "mf_free": (None, [C.c_void_p]),
+        "mf_stage_name": (C.c_char_p, [C.c_int]),
+        "mf_profile_enable": (C.c_int, [_P, C.c_int]),
+        "mf_profile_reset": (C.c_int, [_P]),
+        "mf_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), _I64P, C.c_int]),
+        "mf_kernel_launches": (C.c_int64, []),
         "mf_trace_enable": (C.c_int, [_P, C.c_int]),
         "mf_trace_count": (C.c_int, [_P, _I64P]),
         "mf_trace_get": (C.c_int, [_P, C.c_int64, C.c_int, C.c_void_p, C.c_int64, _I64P]),
@@ -245,6 +251,26 @@ class Graph:
     def compact(self, path, rebase=False):
         _check(_lib().mf_compact(self._h, os.fsencode(path), 1 if rebase else 0), "mf_compact")
 
+    def profile(self, on=True):
+        _check(_lib().mf_profile_enable(self._h, 1 if on else 0), "mf_profile_enable")
+
+    def profile_reset(self):
+        _check(_lib().mf_profile_reset(self._h), "mf_profile_reset")
+
+    def profile_read(self):
+        """{stage name: (device ms, occurrences)} accumulated since the last reset."""
+        k = 16
+        ms = (C.c_double * k)()
+        calls = (C.c_int64 * k)()
+        _check(_lib().mf_profile_read(self._h, ms, calls, k), "mf_profile_read")
+        out = {}
+        for i in range(k):
+            name = _lib().mf_stage_name(i)
+            if name is None:
+                break
+            out[name.decode()] = (ms[i], calls[i])
+        return out
+
     def trace(self, on=True):
         _check(_lib().mf_trace_enable(self._h, 1 if on else 0), "mf_trace_enable")
 
@@ -263,6 +289,11 @@ class Graph:
                 rec[field] = arr[: ln.value]
             recs.append(rec)
         return recs
+
+
+def kernel_launches():
+    """Kernels launched by libmisfit_gb in this process so far."""
+    return int(_lib().mf_kernel_launches())
 
 
 def read_mis_file(path, n):

@@ -21,7 +21,7 @@ import struct
 import numpy as np
 
 __all__ = [
-    "read_egr", "write_egr", "csr_from_pairs", "er_graph", "rmat_graph", "rgg_graph",
+    "read_egr", "write_egr", "csr_from_pairs", "er_graph", "rmat_graph", "rmat_graph_torch", "rgg_graph",
     "ToggleStream", "write_batch_file", "write_batch_folder", "read_batch_file",
     "write_mis_file", "read_mis_file", "undirected_pairs",
 ]
@@ -183,93 +183,158 @@ class ToggleStream:
     """Batches of toggles drawn against the nominal graph as it evolves.
 
     Each batch holds ``batch_size`` lines: ``round(batch_size*delete_frac)``
-    deletes of existing edges and the rest inserts of non-adjacent pairs,
-    shuffled.  ``endpoints`` picks how endpoints are drawn: ``uniform``
-    (deletes uniform over edges, inserts uniform over pairs), ``preferential``
-    (probability proportional to current degree) or ``low_degree``
-    (proportional to 1/degree).  After each batch the nominal graph applies
-    the toggles, so later batches may delete edges inserted earlier.
+    deletes of existing edges (uniform over the current edges) and the rest
+    inserts of non-adjacent pairs, shuffled, each line in a random direction.
+    ``endpoints`` picks how insert endpoints are drawn: ``uniform``,
+    ``preferential`` (probability proportional to current degree) or
+    ``low_degree`` (proportional to 1/max(degree, 1)); for the two weighted
+    modes a delete keeps a sampled edge with probability proportional to the
+    product of its endpoint weights.  After each batch the nominal graph
+    applies the toggles, so later batches may delete edges inserted earlier.
+
+    The base edge set stays a sorted array with an alive mask; inserted pairs
+    that are not base edges live in a small sorted side array, so one batch
+    costs O(batch * log E) whatever the graph size.
     """
 
     def __init__(self, n, nindex, nlist, seed):
         self.n = int(n)
-        lo, hi = undirected_pairs(self.n, nindex, nlist)
-        self.keys = np.sort(lo * self.n + hi)
+        lo, hi = undirected_pairs(self.n, np.asarray(nindex, np.int64), np.asarray(nlist))
+        self.base = lo * self.n + hi          # ascending: rows sorted, sources ascending
+        if self.base.size > 1 and not np.all(self.base[1:] > self.base[:-1]):
+            self.base = np.unique(self.base)
+        self.alive = np.ones(self.base.size, dtype=bool)
+        self.extra = np.empty(0, dtype=np.int64)
         self.rng = np.random.default_rng(seed)
         self.deg = np.diff(np.asarray(nindex, dtype=np.int64)).astype(np.float64)
 
-    def _has(self, keys):
-        if self.keys.size == 0:
-            return np.zeros(keys.shape, dtype=bool)
-        pos = np.minimum(np.searchsorted(self.keys, keys), self.keys.size - 1)
-        return self.keys[pos] == keys
+    @property
+    def num_edges(self):
+        return int(self.alive.sum()) + int(self.extra.size)
 
-    def _vertex_sampler(self, mode, size):
+    def _find(self, arr, keys):
+        if arr.size == 0:
+            return np.zeros(keys.shape, np.int64), np.zeros(keys.shape, bool)
+        pos = np.minimum(np.searchsorted(arr, keys), arr.size - 1)
+        return pos, arr[pos] == keys
+
+    def _adjacent(self, keys):
+        pos, hit = self._find(self.base, keys)
+        a = hit & self.alive[pos]
+        _, e = self._find(self.extra, keys)
+        return a | e
+
+    def _weights(self, mode):
+        if mode == "preferential":
+            return self.deg + 1e-12
+        if mode == "low_degree":
+            return 1.0 / np.maximum(self.deg, 1.0)
+        raise ValueError(mode)
+
+    def _vertices(self, mode, size):
         if mode == "uniform":
             return self.rng.integers(0, self.n, size=size)
-        if mode == "preferential":
-            w = self.deg + 1e-12
-        elif mode == "low_degree":
-            w = 1.0 / np.maximum(self.deg, 1.0)
-        else:
-            raise ValueError(mode)
-        cdf = np.cumsum(w)
+        cdf = np.cumsum(self._weights(mode))
         cdf /= cdf[-1]
         return np.minimum(np.searchsorted(cdf, self.rng.random(size)), self.n - 1)
 
+    def _sample_edges(self, count, mode):
+        total = self.base.size + self.extra.size
+        got = np.empty(0, dtype=np.int64)
+        if count <= 0 or total == 0:
+            return got
+        w = None if mode == "uniform" else self._weights(mode)
+        wmax = None if w is None else float(w.max()) ** 2
+        while got.size < count:
+            r = self.rng.integers(0, total, size=4 * (count - got.size) + 64)
+            inb = r < self.base.size
+            rb = r[inb]
+            k = np.concatenate([self.base[rb[self.alive[rb]]], self.extra[r[~inb] - self.base.size]])
+            if w is not None:
+                a, b = k // self.n, k % self.n
+                k = k[self.rng.random(k.size) * wmax < w[a] * w[b]]
+            got = np.unique(np.concatenate([got, k]))
+            if got.size > count:
+                got = self.rng.permutation(got)[:count]
+        return got
+
     def next_batch(self, batch_size, delete_frac=0.5, endpoints="uniform"):
         n = self.n
-        nd = int(round(batch_size * delete_frac))
-        nd = min(nd, int(self.keys.size))
+        nd = min(int(round(batch_size * delete_frac)), self.num_edges)
         ni = batch_size - nd
-        # deletes: existing edges
-        if endpoints == "uniform" or nd == 0:
-            pick = self.rng.choice(self.keys.size, size=nd, replace=False) if nd else np.empty(0, np.int64)
-            dkeys = self.keys[pick]
-        else:
-            # weight each edge by the endpoint weights of its lower endpoint
-            dkeys = np.empty(0, dtype=np.int64)
-            while dkeys.size < nd:
-                x = self._vertex_sampler(endpoints, 4 * (nd - dkeys.size) + 16)
-                start = np.searchsorted(self.keys, x * n)
-                stop = np.searchsorted(self.keys, x * n + n)
-                has = stop > start
-                x, start, stop = x[has], start[has], stop[has]
-                j = start + (self.rng.random(x.size) * (stop - start)).astype(np.int64)
-                cand = self.keys[j]
-                dkeys = np.unique(np.concatenate([dkeys, cand]))
-            dkeys = self.rng.permutation(dkeys)[:nd]
-        # inserts: non-adjacent distinct pairs
+        dkeys = self._sample_edges(nd, endpoints)
         ikeys = np.empty(0, dtype=np.int64)
         while ikeys.size < ni:
             need = ni - ikeys.size
-            a = self._vertex_sampler(endpoints, 2 * need + 16)
-            b = self._vertex_sampler(endpoints, 2 * need + 16)
+            a = self._vertices(endpoints, 2 * need + 16)
+            b = self._vertices(endpoints, 2 * need + 16)
             ok = a != b
             lo = np.minimum(a[ok], b[ok])
             hi = np.maximum(a[ok], b[ok])
             k = lo * n + hi
-            k = k[~self._has(k)]
+            k = k[~self._adjacent(k)]
             ikeys = np.unique(np.concatenate([ikeys, k]))
             if ikeys.size > ni:
                 ikeys = self.rng.permutation(ikeys)[:ni]
         keys = np.concatenate([dkeys, ikeys])
-        perm = self.rng.permutation(keys.size)
-        keys = keys[perm]
+        keys = keys[self.rng.permutation(keys.size)]
         lo = keys // n
         hi = keys % n
         flip = self.rng.random(keys.size) < 0.5
         u = np.where(flip, hi, lo).astype(np.int32)
         v = np.where(flip, lo, hi).astype(np.int32)
         # nominal graph update
-        self.keys = np.sort(np.concatenate([np.setdiff1d(self.keys, dkeys, assume_unique=True), ikeys]))
-        dl, dh = dkeys // n, dkeys % n
-        il, ih = ikeys // n, ikeys % n
-        np.subtract.at(self.deg, dl, 1)
-        np.subtract.at(self.deg, dh, 1)
-        np.add.at(self.deg, il, 1)
-        np.add.at(self.deg, ih, 1)
+        pos, inb = self._find(self.base, dkeys)
+        self.alive[pos[inb]] = False
+        if (~inb).any():
+            self.extra = np.setdiff1d(self.extra, dkeys[~inb], assume_unique=True)
+        pos, inb = self._find(self.base, ikeys)
+        self.alive[pos[inb]] = True
+        if (~inb).any():
+            self.extra = np.union1d(self.extra, ikeys[~inb])
+        for keyset, sign in ((dkeys, -1.0), (ikeys, 1.0)):
+            np.add.at(self.deg, keyset // n, sign)
+            np.add.at(self.deg, keyset % n, sign)
         return u, v
+
+
+def rmat_graph_torch(scale, edge_factor, seed, device="cuda", abcd=(0.57, 0.19, 0.19, 0.05)):
+    """R-MAT as rmat_graph, generated on a CUDA device with torch (Philox
+    stream seeded by ``seed``); returns host numpy arrays (n, (nindex, nlist)).
+    Used for the large benchmark graphs, which numpy builds too slowly."""
+    import torch
+
+    a, b, c, _ = abcd
+    n = 1 << scale
+    total = n * edge_factor
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    keys = []
+    chunk = 1 << 25
+    done = 0
+    while done < total:
+        cnt = min(chunk, total - done)
+        u = torch.zeros(cnt, dtype=torch.int64, device=device)
+        v = torch.zeros(cnt, dtype=torch.int64, device=device)
+        for lvl in range(scale):
+            r = torch.rand(cnt, generator=gen, device=device)
+            u |= (r >= (a + b)).to(torch.int64) << lvl
+            v |= (((r >= a) & (r < a + b)) | (r >= (a + b + c))).to(torch.int64) << lvl
+        keep = u != v
+        lo = torch.minimum(u[keep], v[keep])
+        hi = torch.maximum(u[keep], v[keep])
+        keys.append(torch.unique(lo * n + hi))
+        done += cnt
+    key = torch.unique(torch.cat(keys))
+    del keys
+    lo, hi = key // n, key % n
+    both = torch.sort(torch.cat([lo * n + hi, hi * n + lo])).values
+    src = both // n
+    dst = (both % n).to(torch.int32)
+    deg = torch.bincount(src, minlength=n)
+    nindex = torch.zeros(n + 1, dtype=torch.int64, device=device)
+    nindex[1:] = torch.cumsum(deg, 0)
+    return n, (nindex.cpu().numpy(), dst.cpu().numpy())
 
 
 def write_batch_file(path, u, v):

@@ -198,3 +198,41 @@ def test_bad_egr_files(gpu_lib, tmp_path):
     with pytest.raises(native.MisfitError) as e:
         native.Graph.open_egr(str(tmp_path / "missing.egr"))
     assert e.value.status == -2
+
+
+_SEQ_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+import oracle as O
+from misfit_gb300 import native, workloads as W
+n, (ni, nl) = W.rmat_graph(11, 8, 21)
+ts = W.ToggleStream(n, ni, nl, 22)
+bs = [ts.next_batch(600) for _ in range(3)]
+orc = O.Oracle.from_csr(ni, nl); gr = native.Graph.from_csr(ni, nl)
+mis = O.greedy_mis(ni, nl); orc.set_mis(mis); gr.set_mis(mis)
+seq = sys.argv[2] == "sequential"
+for u, v in bs:
+    ins = orc.flag_updates(u, v)
+    orc.apply_batch(u, v, ins); gr.apply_batch(u, v, ins)
+    assert np.array_equal(gr.get_mis(), orc.get_mis())
+    assert (gr.stats()["repair_rounds"] == 0) == seq
+print("ok")
+"""
+
+
+@pytest.mark.parametrize("mode,env", [("sequential", {"MISFIT_GB_REPAIR": "sequential"}),
+                                      ("grid", {"MISFIT_GB_BIG_THRESHOLD": "8"})])
+def test_repair_variants_match(mode, env, gpu_lib, tmp_path):
+    """The single-CTA sequential repair (the fallback after the round limit)
+    and the grid-wide hop-2 search (forced for every long search by a tiny
+    threshold) both give the oracle's results on a whole stream."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "variant.py"
+    script.write_text(_SEQ_SCRIPT)
+    out = subprocess.run([sys.executable, str(script), root, mode], env=dict(os.environ, **env),
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().endswith("ok")
