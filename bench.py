@@ -1,0 +1,309 @@
+"""Benchmark: MISFIT dynamic-MIS maintenance, plain per-batch loop.
+
+Workload (the plain method at scale): R-MAT scale 22 (4,194,304 vertices,
+16 undirected samples per vertex, a,b,c,d = .57/.19/.19/.05, symmetrised,
+de-duplicated, self-loops removed), seed 7, int32 .egr layout; batches of
+100,000 toggles, half deletes of uniformly sampled existing edges and half
+inserts of uniformly sampled non-adjacent pairs, drawn against the nominal
+graph as it evolves; parse-time flags against the base graph, as the
+reference CLI computes them.  Seeded synthetic data; the graph is built on
+the GPU with torch (input preparation only).
+
+One step = one batch through libmisfit_gb (overlay apply, split rule,
+neighbourhoods, clustering, repair).  `value` is updates/s with the batch
+inputs resident in HBM (mf_apply_batch_device); `e2e` is the same through
+the host-buffer C-ABI call (mf_apply_batch: host->device copy of the batch
+inside the timed region) plus a device->host read of the membership vector
+after every step.  Times come from CUDA events the library records on its
+own stream around each batch.
+
+--impl reference runs the oracle (the reference path restated on the CPU,
+OpenMP over all host cores) on bounded samples of the same workload.
+
+Multi-GPU: the path does not shard within one graph (replicas only); under
+torchrun every rank runs its own replica and `value` sums the ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "edge updates/s and p50/p99 batch latency, plain per-batch loop, 1 GB300"
+UNIT = "updates/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="misfit", choices=["misfit", "reference"])
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=100000)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(args):
+    return {
+        "workload": "R-MAT scale %d, %d samples/vertex, abcd .57/.19/.19/.05, seed %d; batches of %d toggles "
+                    "(50/50 delete existing / insert non-adjacent, uniform)" % (
+                        args.scale, args.edge_factor, args.seed, args.batch),
+        "vertices": 1 << args.scale,
+        "batch_updates": args.batch,
+        "parallelism": "replicas" if args.gpus > 1 else "single GPU",
+        "l2": "inputs larger than L2 (base CSR ~0.5 GB)",
+        "flags": "parse-time, against the base graph",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(args, device):
+    from misfit_gb300 import workloads as W
+    n, (nindex, nlist) = W.rmat_graph_torch(args.scale, args.edge_factor, args.seed, device=device)
+    stream = W.ToggleStream(n, nindex, nlist, args.seed)
+    return n, nindex, nlist, stream
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_sample(n, nindex, nlist, batch, ins, budget_s):
+    """Oracle on the first lines of `batch`, from the initial state, in chunks
+    that double until the budget is spent.  Returns (updates/s, lines, s)."""
+    import oracle as O
+    orc = O.Oracle.from_csr(nindex, nlist)
+    orc.set_mis(O.greedy_mis(nindex, nlist))
+    u, v = batch
+    done, spent, chunk = 0, 0.0, 16
+    while done < u.size and spent < budget_s:
+        k = min(chunk, u.size - done)
+        t = time.perf_counter()
+        orc.apply_batch(u[done:done + k], v[done:done + k], ins[done:done + k])
+        spent += time.perf_counter() - t
+        done += k
+        chunk *= 2
+    orc.close()
+    return done / spent, done, spent
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import torch
+    device = "cuda:%d" % int(os.environ.get("LOCAL_RANK", "0")) if torch.cuda.is_available() else "cpu"
+    n, nindex, nlist, stream = make_workload(args, device)
+    import oracle as O
+    orc0 = O.Oracle.from_csr(nindex, nlist)
+    cores = os.cpu_count()
+    rates, lat = [], []
+    steps = args.warmup + args.steps
+    budget = max(2.0, args.cpu_seconds / 2)
+    for i in range(steps):
+        u, v = stream.next_batch(args.batch)
+        ins = orc0.flag_updates(u, v)
+        rate, lines, spent = cpu_sample(n, nindex, nlist, (u, v), ins, budget)
+        if i >= args.warmup:
+            rates.append(rate)
+            lat.append(spent / lines * args.batch * 1e3)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.batch / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded R-MAT + toggle stream)", "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "oracle (reference path restated, OpenMP %d threads) on the leading lines "
+                                   "of each batch from the initial state, ~%.0f s per step" % (cores, budget)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "misfit" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    from misfit_gb300 import build, native
+    build.build()
+    n, nindex, nlist, stream = make_workload(args, "cuda:%d" % local)
+    g = native.Graph.from_csr(nindex, nlist, gpu=local)
+    g.set_mis(g.greedy_mis())
+    total = args.warmup + args.steps + (0 if args.no_e2e else args.steps)
+    batches = [stream.next_batch(args.batch) for _ in range(total)]
+    flags = [g.flag_updates(u, v) for u, v in batches]  # against the base graph, before any batch
+
+    dev = []
+    for (u, v), ins in zip(batches[: args.warmup + args.steps], flags):
+        dev.append((torch.from_numpy(u).cuda(), torch.from_numpy(v).cuda(), torch.from_numpy(ins).cuda()))
+    torch.cuda.synchronize()
+
+    def dist_barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for i in range(args.warmup):
+        du, dv, di = dev[i]
+        g.apply_batch_device(du.data_ptr(), dv.data_ptr(), di.data_ptr(), du.numel())
+
+    # ---- timed: inputs resident in HBM
+    g.profile(True)
+    g.profile_reset()
+    clocks = ClockSampler(local)
+    dist_barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = native.kernel_launches()
+    t0 = time.perf_counter()
+    lat = []
+    for i in range(args.warmup, args.warmup + args.steps):
+        du, dv, di = dev[i]
+        g.apply_batch_device(du.data_ptr(), dv.data_ptr(), di.data_ptr(), du.numel())
+        lat.append(g.stats()["device_ms"])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    launches = native.kernel_launches() - launches0
+    clk = clocks.stop()
+    dist_barrier()
+    prof = g.profile_read()
+    g.profile(False)
+    dev_ms = float(np.sum(lat))
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    value = world * args.steps * args.batch / (dev_ms / 1e3)
+
+    # ---- end to end through the host-buffer C-ABI call
+    e2e = None
+    if not args.no_e2e:
+        e2e_ms = []
+        base = args.warmup + args.steps
+        for i in range(base, base + args.steps):
+            u, v = batches[i]
+            t = time.perf_counter()
+            g.apply_batch(u, v, flags[i])
+            g.get_mis()
+            e2e_ms.append((time.perf_counter() - t) * 1e3)
+        e2e = {"value": world * args.steps * args.batch / (float(np.sum(e2e_ms)) / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": int(args.batch * 9), "d2h_bytes_per_step": int(n)}
+
+    # ---- roofline of the dominant byte-counted stage (the clustering push)
+    peak, peak_kind = measured_peaks()
+    stage = "cluster_write"
+    ms, calls, nbytes = prof[stage]
+    achieved = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    top = max(prof.items(), key=lambda kv: kv[1][0])
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": "cluster_write (k_lb_push_*)", "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": nbytes / max(calls, 1), "avg_launch_ms": ms / max(calls, 1)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded R-MAT + toggle stream)", "config": workload_config(args),
+        "p50_batch_ms": float(np.percentile(lat, 50)), "p99_batch_ms": float(np.percentile(lat, 99)),
+        "wall_s_timed": wall, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
+        "stage_ms": {k: round(v[0], 3) for k, v in prof.items()}, "slowest_stage": top[0],
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        u, v = batches[0]
+        rate, lines, spent = cpu_sample(n, nindex, nlist, (u, v), flags[0], args.cpu_seconds)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": "oracle on the first %d lines of batch 1 from the initial state "
+                                          "(%.1f s)" % (lines, spent)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    dist_barrier()
+
+
+if __name__ == "__main__":
+    main()

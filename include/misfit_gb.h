@@ -181,8 +181,10 @@ const char* mf_stage_name(int stage);
  * context's stream; times accumulate until mf_profile_reset. */
 int mf_profile_enable(mf_ctx* ctx, int on);
 int mf_profile_reset(mf_ctx* ctx);
-/* Accumulated device milliseconds and occurrences per stage (cap entries). */
-int mf_profile_read(mf_ctx* ctx, double* ms, int64_t* calls, int cap);
+/* Accumulated device milliseconds, occurrences and algorithmic bytes per
+ * stage (cap entries; bytes may be NULL).  Bytes are counted for the stages
+ * with a device work counter (hop1, cluster_write) and are 0 elsewhere. */
+int mf_profile_read(mf_ctx* ctx, double* ms, int64_t* calls, double* bytes, int cap);
 /* Kernels launched by this library in this process so far. */
 int64_t mf_kernel_launches(void);
 

@@ -85,6 +85,8 @@ void release_all(mf_ctx* c) {
   c->rp_vals2.release();
   c->rp_u8.release();
   c->rp_pos.release();
+  c->work.release();
+  c->lb_offs.release();
   for (auto* b : {&c->big_pos, &c->big_off, &c->big_nr, &c->big_chunks, &c->big_pre}) b->release();
   c->big_r.release();
   c->big_best.release();
@@ -128,6 +130,9 @@ void run_batch(mf_ctx* c, int64_t m) {
   c->stats = mf_batch_stats{};
   c->stats.updates = m;
   c->traces.clear();
+  c->work.reserve(2 * mf::kStCount);
+  c->touched_total = 0;
+  MF_CUDA(cudaMemsetAsync(c->work.p, 0, sizeof(unsigned long long) * 2 * mf::kStCount, s));
   MF_CUDA(cudaEventRecord(c->ev0, s));
   if (m > 0) {
     {
@@ -151,6 +156,16 @@ void run_batch(mf_ctx* c, int64_t m) {
   }
   c->ev_marks.clear();
   c->ev_used = 0;
+  if (c->profile) {
+    // algorithmic bytes per stage from the device work counters:
+    //   hop1: 4 B row entry + 8 B mark read-modify-write per element
+    //   push: 4 B row entry + 8 B max read-modify-write per element, plus
+    //         16 B per touched vertex to resolve its cluster id
+    unsigned long long w[2 * mf::kStCount];
+    MF_CUDA(cudaMemcpy(w, c->work.p, sizeof(w), cudaMemcpyDeviceToHost));
+    c->stage_bytes[mf::kStHop1] += 12.0 * (double)w[2 * mf::kStHop1];
+    c->stage_bytes[mf::kStPush] += 12.0 * (double)w[2 * mf::kStPush] + 16.0 * (double)c->touched_total;
+  }
 }
 
 __global__ void k_validate(const int32_t* u, const int32_t* v, int64_t m, int32_t n, unsigned long long* bad) {
@@ -725,16 +740,18 @@ int mf_profile_reset(mf_ctx* c) {
     for (int i = 0; i < mf::kStCount; ++i) {
       c->stage_ms[i] = 0;
       c->stage_calls[i] = 0;
+      c->stage_bytes[i] = 0;
     }
   });
 }
 
-int mf_profile_read(mf_ctx* c, double* ms, int64_t* calls, int cap) {
+int mf_profile_read(mf_ctx* c, double* ms, int64_t* calls, double* bytes, int cap) {
   return guarded([&] {
     need(c && ms && calls && cap >= 0, MF_EINVAL, "bad arguments");
     for (int i = 0; i < mf::kStCount && i < cap; ++i) {
       ms[i] = c->stage_ms[i];
       calls[i] = c->stage_calls[i];
+      if (bytes) bytes[i] = c->stage_bytes[i];
     }
   });
 }

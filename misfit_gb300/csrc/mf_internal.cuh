@@ -194,6 +194,67 @@ __device__ __forceinline__ void warp_row_each(const GraphView& g, int32_t x, F f
   for (int64_t k = ab + lane; k < ae; k += 32) f(g.aadj[k]);
 }
 
+// Load-balanced traversal of the rows of list[0..cnt): offs is the exclusive
+// prefix of the row position counts (base positions + added entries; a
+// count of 0 skips the row), cnt+1 entries.  Every warp takes chunks of
+// 256 consecutive positions, so a hub row is spread over many warps.
+// f(i, x, y) is called for every live element y of row(x = list[i]).
+// Returns the number of elements visited by the calling thread.
+template <class F>
+__device__ __forceinline__ int64_t lb_rows(const GraphView& g, const int32_t* list, const int64_t* offs, int64_t cnt,
+                                           F f) {
+  constexpr int64_t kChunk = 256;
+  const int64_t total = offs[cnt];
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int64_t visited = 0;
+  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kChunk; base < total;
+       base += nwarps * kChunk) {
+    int64_t i = 0;
+    if (lane == 0) {
+      int64_t lo = 0, hi = cnt;  // last i with offs[i] <= base
+      while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= base) lo = mid; else hi = mid;
+      }
+      i = lo;
+    }
+    i = __shfl_sync(0xffffffffu, i, 0);
+    const int64_t end = base + kChunk < total ? base + kChunk : total;
+    int64_t cur = -1, next_off = 0, row_off = 0, nb = 0, b0 = 0, a0 = 0;
+    int32_t x = 0;
+    bool filt = false;
+    for (int64_t e = base + lane; e < end; e += 32) {
+      if (cur < 0 || e >= next_off) {
+        while (offs[i + 1] <= e) ++i;
+        cur = i;
+        x = list[i];
+        row_off = offs[i];
+        next_off = offs[i + 1];
+        b0 = g.nindex[x];
+        nb = g.nindex[x + 1] - b0;
+        a0 = g.aoff[x];
+        filt = g.dead[x] != 0;
+      }
+      const int64_t j = e - row_off;
+      int32_t y;
+      if (j < nb) {
+        if (filt && !live_at(g.live, b0 + j)) continue;
+        y = __ldg(g.nlist + b0 + j);
+      } else {
+        y = g.aadj[a0 + (j - nb)];
+      }
+      ++visited;
+      f(i, x, y);
+    }
+  }
+  return visited;
+}
+
+__device__ __forceinline__ int64_t row_positions(const GraphView& g, int32_t x) {
+  return (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
+}
+
 // ---- primitives (mf_prims.cu) -----------------------------------------------
 
 struct Scratch;  // workspace for primitives
@@ -306,6 +367,11 @@ struct mf_ctx {
   std::vector<std::pair<int, size_t>> ev_marks;
   double stage_ms[mf::kStCount] = {};
   int64_t stage_calls[mf::kStCount] = {};
+  // device counters of algorithmic work (elements, rows) per stage
+  mf::DBuf<unsigned long long> work;   // 2 * kStCount entries
+  double stage_bytes[mf::kStCount] = {};
+  mf::DBuf<int64_t> lb_offs;           // row-position prefix for lb_rows
+  int64_t touched_total = 0;
 
   // pinned staging for host-input batches
   uint8_t* h_stage = nullptr;

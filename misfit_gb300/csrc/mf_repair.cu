@@ -110,14 +110,42 @@ __global__ void k_seed_compact(const int32_t* u, const int32_t* v, const uint8_t
 
 // ---- hop-1 set and candidates ---------------------------------------------------
 
-__global__ void k_mark_hop1(GraphView g, const int32_t* seeds, int64_t ns, uint32_t epoch, uint32_t* hmark,
-                            int32_t* hlist, unsigned long long* count) {
-  const int64_t w = warp_id();
-  if (w >= ns) return;
-  const int32_t s = seeds[w];
-  warp_row_each(g, s, [&](int32_t y) {
+// Row-position counts for lb_rows; rows that must not be visited count 0.
+enum CountKind : int { kCntAll = 0, kCntSeedRows, kCntCandRows, kCntSeedPushers, kCntHopPushers };
+
+__global__ void k_row_counts(GraphView g, const int32_t* list, int64_t cnt, int kind, const int32_t* rowcid,
+                             int64_t ns, const uint32_t* bval, uint32_t epoch, const int32_t* v2i, int64_t* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  const int32_t x = list[i];
+  bool use = true;
+  if (kind == kCntSeedRows) {
+    use = rowcid[i] != kSkip;
+  } else if (kind == kCntCandRows) {
+    use = rowcid[ns + i] != kSkip;
+  } else if (kind == kCntSeedPushers) {
+    use = (bval[x] >> kRowBits) == epoch;
+  } else if (kind == kCntHopPushers) {
+    use = (bval[x] >> kRowBits) == epoch;
+    const int32_t vi = v2i[x];
+    // seeds push in their own pass; a candidate row that writes its own tag
+    // over row(x) dominates bval[x] there (candidate tags are the larger)
+    if (vi >= 0 && ((int64_t)vi < ns || rowcid[vi] != kSkip)) use = false;
+  }
+  out[i] = use ? row_positions(g, x) : 0;
+}
+
+__device__ __forceinline__ void add_work(unsigned long long* work, int64_t visited) {
+  for (int o = 16; o > 0; o >>= 1) visited += __shfl_down_sync(0xffffffffu, visited, o);
+  if ((threadIdx.x & 31) == 0 && visited) atomicAdd(work, (unsigned long long)visited);
+}
+
+__global__ void k_lb_mark_hop1(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t epoch,
+                               uint32_t* hmark, int32_t* hlist, unsigned long long* count, unsigned long long* work) {
+  const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t, int32_t, int32_t y) {
     if (atomicExch(hmark + y, epoch) != epoch) hlist[atomicAdd(count, 1ull)] = y;
   });
+  add_work(work, vis);
 }
 
 __global__ void k_cand_flags(const uint32_t* hmark, const int32_t* v2i, int32_t n, uint32_t epoch, uint8_t* flags) {
@@ -287,14 +315,17 @@ __global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid) {
 }
 
 // Phase 1: bval[y] = max tag of the non-skipped seed rows with y in {s} u row(s).
-__global__ void k_push_seed(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* rowcid, uint32_t epoch,
-                            uint32_t* bval) {
-  const int64_t w = warp_id();
-  if (w >= ns || rowcid[w] == kSkip) return;
-  const int32_t s = seeds[w];
-  const uint32_t tag = (epoch << kRowBits) | (uint32_t)w;
-  if ((threadIdx.x & 31) == 0) atomicMax(bval + s, tag);
-  warp_row_each(g, s, [&](int32_t y) { atomicMax(bval + y, tag); });
+__global__ void k_seed_self(const int32_t* seeds, int64_t ns, const int32_t* rowcid, uint32_t epoch, uint32_t* bval) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ns && rowcid[i] != kSkip) atomicMax(bval + seeds[i], (epoch << kRowBits) | (uint32_t)i);
+}
+
+__global__ void k_lb_push_seed(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t epoch,
+                               uint32_t* bval, unsigned long long* work) {
+  const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
+    atomicMax(bval + y, (epoch << kRowBits) | (uint32_t)i);
+  });
+  add_work(work, vis);
 }
 
 __device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag, uint32_t epoch, int32_t* touched,
@@ -303,25 +334,33 @@ __device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag, 
   if ((old >> kRowBits) != epoch) touched[atomicAdd(tcount, 1ull)] = y;
 }
 
-// Phase 2: wval[y] = max over x with y in {x} u row(x) of bval[x] (2-hop reach
-// of the seed rows), then the candidate rows' own tags over row(c).
-__global__ void k_push_hop(GraphView g, const int32_t* list, int64_t cnt, uint32_t epoch, const uint32_t* bval,
-                           uint32_t* wval, int32_t* touched, unsigned long long* tcount) {
-  const int64_t w = warp_id();
-  if (w >= cnt) return;
-  const int32_t x = list[w];
+// Phase 2: wval[y] = max over x with y in {x} u row(x) of bval[x] (the 2-hop
+// reach of the seed rows), and the candidate rows' own tags over row(c).
+__global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, const uint32_t* bval, uint32_t* wval,
+                            int32_t* touched, unsigned long long* tcount) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  const int32_t x = list[i];
   const uint32_t t = bval[x];
-  if ((t >> kRowBits) != epoch) return;
-  if ((threadIdx.x & 31) == 0) push_w(wval, x, t, epoch, touched, tcount);
-  warp_row_each(g, x, [&](int32_t y) { push_w(wval, y, t, epoch, touched, tcount); });
+  if ((t >> kRowBits) == epoch) push_w(wval, x, t, epoch, touched, tcount);
 }
 
-__global__ void k_push_cand(GraphView g, const int32_t* cands, int64_t nct, int64_t ns, const int32_t* rowcid,
-                            uint32_t epoch, uint32_t* wval, int32_t* touched, unsigned long long* tcount) {
-  const int64_t w = warp_id();
-  if (w >= nct || rowcid[ns + w] == kSkip) return;
-  const uint32_t tag = (epoch << kRowBits) | (uint32_t)(ns + w);
-  warp_row_each(g, cands[w], [&](int32_t y) { push_w(wval, y, tag, epoch, touched, tcount); });
+__global__ void k_lb_push_hop(GraphView g, const int32_t* list, const int64_t* offs, int64_t cnt, uint32_t epoch,
+                              const uint32_t* bval, uint32_t* wval, int32_t* touched, unsigned long long* tcount,
+                              unsigned long long* work) {
+  const int64_t vis = lb_rows(g, list, offs, cnt, [&](int64_t, int32_t x, int32_t y) {
+    push_w(wval, y, bval[x], epoch, touched, tcount);
+  });
+  add_work(work, vis);
+}
+
+__global__ void k_lb_push_cand(GraphView g, const int32_t* cands, const int64_t* offs, int64_t nct, int64_t ns,
+                               uint32_t epoch, uint32_t* wval, int32_t* touched, unsigned long long* tcount,
+                               unsigned long long* work) {
+  const int64_t vis = lb_rows(g, cands, offs, nct, [&](int64_t i, int32_t, int32_t y) {
+    push_w(wval, y, (epoch << kRowBits) | (uint32_t)(ns + i), epoch, touched, tcount);
+  });
+  add_work(work, vis);
 }
 
 __global__ void k_finalize_cid(const int32_t* touched, int64_t cnt, const uint32_t* wval, const int32_t* rowcid,
@@ -958,6 +997,25 @@ std::vector<T> fetch(const T* d, int64_t cnt, cudaStream_t s) {
   return h;
 }
 
+unsigned lb_grid(mf_ctx* c) {
+  static int sms = 0;
+  if (sms == 0) {
+    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  }
+  return (unsigned)(sms * 8);  // 8 CTAs of 256 threads per SM
+}
+
+// Row-position prefix of list[0..cnt) for lb_rows into c->lb_offs.
+void row_offsets(mf_ctx* c, const int32_t* list, int64_t cnt, int kind, int64_t ns, uint32_t epoch) {
+  cudaStream_t s = c->stream;
+  c->lb_offs.reserve(2 * cnt + 2);
+  int64_t* counts = c->lb_offs.p + cnt + 1;
+  if (cnt > 0)
+    MF_K(k_row_counts<<<grid_for(cnt), kTB, 0, s>>>(c->view(), list, cnt, kind, c->rowcid.p, ns, c->bval.p, epoch,
+                                                   c->v2i.p, counts));
+  scan_exclusive_i64(counts, c->lb_offs.p, cnt, c->ws, s);
+}
+
 void next_epoch(mf_ctx* c) {
   if (c->epoch >= kMaxEpoch) {
     cudaStream_t s = c->stream;
@@ -1147,7 +1205,9 @@ void process_batch(mf_ctx* c, int64_t m) {
     next_epoch(c);
     const uint32_t ep = c->epoch;
     MF_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int64_t), s));
-    MF_K(k_mark_hop1<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->hmark.p, c->hlist.p, ucnt + 2));
+    row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
+    MF_K(k_lb_mark_hop1<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->hmark.p, c->hlist.p,
+                                                   ucnt + 2, c->work.p + 2 * kStHop1));
     MF_K(k_cand_flags<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->v2i.p, n, ep, c->u8a.p));
     scan_exclusive_u8(c->u8a.p, c->i64a.p, n, c->ws, s);
     const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
@@ -1205,16 +1265,27 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_K(k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p));
     MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     sc.emplace(c, kStPush);
-    MF_K(k_push_seed<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
+    unsigned long long* wk = c->work.p + 2 * kStPush;
+    MF_K(k_seed_self<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
+    row_offsets(c, c->seeds.p, ns, kCntSeedRows, ns, ep);
+    MF_K(k_lb_push_seed<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk));
     MF_CUDA(cudaMemsetAsync(cnt + 8, 0, sizeof(int64_t), s));
-    MF_K(k_push_hop<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
-    MF_K(k_push_hop<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
-    MF_K(k_push_cand<<<warps_grid(nct), kTB, 0, s>>>(g, c->cands.p, nct, ns, c->rowcid.p, ep, c->wval.p, c->touched.p,
-                                                ucnt + 8));
+    MF_K(k_self_push<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
+    MF_K(k_self_push<<<grid_for(nh), kTB, 0, s>>>(c->hlist.p, nh, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
+    row_offsets(c, c->seeds.p, ns, kCntSeedPushers, ns, ep);
+    MF_K(k_lb_push_hop<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, c->wval.p,
+                                                  c->touched.p, ucnt + 8, wk));
+    row_offsets(c, c->hlist.p, nh, kCntHopPushers, ns, ep);
+    MF_K(k_lb_push_hop<<<lb_grid(c), kTB, 0, s>>>(g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p, c->wval.p,
+                                                  c->touched.p, ucnt + 8, wk));
+    row_offsets(c, c->cands.p, nct, kCntCandRows, ns, ep);
+    MF_K(k_lb_push_cand<<<lb_grid(c), kTB, 0, s>>>(g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
+                                                   c->touched.p, ucnt + 8, wk));
     MF_CUDA(cudaMemcpyAsync(h + 8, cnt + 8, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t cc = h[7];
     const int64_t ntouched = h[8];
+    c->touched_total += ntouched;
     MF_K(k_finalize_cid<<<grid_for(ntouched), kTB, 0, s>>>(c->touched.p, ntouched, c->wval.p, c->rowcid.p, c->cid.p));
     MF_CUDA(cudaGetLastError());
 

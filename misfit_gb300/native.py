@@ -94,7 +94,7 @@ def _lib():
         "mf_stage_name": (C.c_char_p, [C.c_int]),
         "mf_profile_enable": (C.c_int, [_P, C.c_int]),
         "mf_profile_reset": (C.c_int, [_P]),
-        "mf_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), _I64P, C.c_int]),
+        "mf_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), _I64P, C.POINTER(C.c_double), C.c_int]),
         "mf_kernel_launches": (C.c_int64, []),
         "mf_trace_enable": (C.c_int, [_P, C.c_int]),
         "mf_trace_count": (C.c_int, [_P, _I64P]),
@@ -258,17 +258,18 @@ class Graph:
         _check(_lib().mf_profile_reset(self._h), "mf_profile_reset")
 
     def profile_read(self):
-        """{stage name: (device ms, occurrences)} accumulated since the last reset."""
+        """{stage: (device ms, occurrences, algorithmic bytes)} since the last reset."""
         k = 16
         ms = (C.c_double * k)()
         calls = (C.c_int64 * k)()
-        _check(_lib().mf_profile_read(self._h, ms, calls, k), "mf_profile_read")
+        nbytes = (C.c_double * k)()
+        _check(_lib().mf_profile_read(self._h, ms, calls, nbytes, k), "mf_profile_read")
         out = {}
         for i in range(k):
             name = _lib().mf_stage_name(i)
             if name is None:
                 break
-            out[name.decode()] = (ms[i], calls[i])
+            out[name.decode()] = (ms[i], calls[i], nbytes[i])
         return out
 
     def trace(self, on=True):
