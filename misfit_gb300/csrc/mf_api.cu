@@ -86,6 +86,13 @@ void release_all(mf_ctx* c) {
   c->rp_u8.release();
   c->rp_pos.release();
   c->work.release();
+  c->uacc.release();
+  c->heavy_slot.release();
+  c->heavy_list.release();
+  c->heavy_bits.release();
+  c->fpos.release();
+  for (auto* b : {&c->un_idx, &c->un_v, &c->need, &c->needv}) b->release();
+  c->un_cnt.release();
   c->lb_offs.release();
   for (auto* b : {&c->big_pos, &c->big_off, &c->big_nr, &c->big_chunks, &c->big_pre}) b->release();
   c->big_r.release();

@@ -255,6 +255,56 @@ __device__ __forceinline__ int64_t row_positions(const GraphView& g, int32_t x) 
   return (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
 }
 
+// Element k of row(x) (base positions first, then added), or -1 if tombstoned.
+__device__ __forceinline__ int32_t row_elem(const GraphView& g, int32_t x, int64_t k, int64_t nb) {
+  if (k < nb) {
+    const int64_t gk = g.nindex[x] + k;
+    if (g.dead[x] != 0 && !live_at(g.live, gk)) return -1;
+    return g.nlist[gk];
+  }
+  return g.aadj[g.aoff[x] + (k - nb)];
+}
+
+// As lb_rows, with the row position j of y passed too; positions start at
+// `skip` (offs counts the positions from `skip` on).  f(i, x, y, j).
+template <class F>
+__device__ __forceinline__ void lb_rows_pos(const GraphView& g, const int32_t* list, const int64_t* offs, int64_t cnt,
+                                            int64_t skip, F f) {
+  constexpr int64_t kChunk = 256;
+  const int64_t total = offs[cnt];
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kChunk; base < total;
+       base += nwarps * kChunk) {
+    int64_t i = 0;
+    if (lane == 0) {
+      int64_t lo = 0, hi = cnt;
+      while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= base) lo = mid; else hi = mid;
+      }
+      i = lo;
+    }
+    i = __shfl_sync(0xffffffffu, i, 0);
+    const int64_t end = base + kChunk < total ? base + kChunk : total;
+    int64_t cur = -1, next_off = 0, row_off = 0, nb = 0;
+    int32_t x = 0;
+    for (int64_t e = base + lane; e < end; e += 32) {
+      if (cur < 0 || e >= next_off) {
+        while (offs[i + 1] <= e) ++i;
+        cur = i;
+        x = list[i];
+        row_off = offs[i];
+        next_off = offs[i + 1];
+        nb = g.nindex[x + 1] - g.nindex[x];
+      }
+      const int64_t j = e - row_off + skip;
+      const int32_t y = row_elem(g, x, j, nb);
+      if (y >= 0) f(i, x, y, j);
+    }
+  }
+}
+
 // ---- primitives (mf_prims.cu) -----------------------------------------------
 
 struct Scratch;  // workspace for primitives
@@ -351,6 +401,13 @@ struct mf_ctx {
   mf::DBuf<uint32_t> bitmaps;   // per-CTA vertex bitmaps for exact 2-hop sizes
   int64_t bitmap_words = 0;
   int bitmap_ctas = 0;
+  mf::DBuf<unsigned long long> uacc;   // per-seed sums of the size bound
+  mf::DBuf<int32_t> heavy_slot, heavy_list;
+  mf::DBuf<uint32_t> heavy_bits;
+  int64_t heavy_cap = 0, heavy_used = 0;
+  mf::DBuf<unsigned long long> fpos;   // first-hit positions
+  mf::DBuf<int32_t> un_idx, un_v, need, needv;
+  mf::DBuf<int64_t> un_cnt;
   mf::DBuf<int64_t> counters;   // device counters
   int64_t* h_counters = nullptr;  // pinned mirror
   mf::Scratch ws;

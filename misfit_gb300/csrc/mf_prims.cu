@@ -133,10 +133,42 @@ __global__ void k_tile_scan(L load, int64_t n, const int64_t* offs, int64_t* out
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = offs[gridDim.x];
 }
 
+// One block scans the whole (small) input tile by tile with a carry.
+template <typename L>
+__global__ void k_scan_single(L load, int64_t n, int64_t* out) {
+  __shared__ int64_t sw[33];
+  int64_t carry = 0;
+  for (int64_t base = 0; base < n; base += kTile) {
+    int64_t v[kItems];
+    int64_t local = 0;
+    for (int k = 0; k < kItems; ++k) {
+      const int64_t i = base + (int64_t)threadIdx.x * kItems + k;
+      v[k] = i < n ? load(i) : 0;
+      local += v[k];
+    }
+    int64_t tot;
+    int64_t pre = block_exclusive(local, sw, &tot) + carry;
+    for (int k = 0; k < kItems; ++k) {
+      const int64_t i = base + (int64_t)threadIdx.x * kItems + k;
+      if (i < n) out[i] = pre;
+      pre += v[k];
+    }
+    carry += tot;
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+constexpr int64_t kSingleScanMax = 65536;
+
 template <typename L>
 void scan_exclusive(L load, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s) {
   if (n <= 0) {
     MF_CUDA(cudaMemsetAsync(out, 0, sizeof(int64_t), s));
+    return;
+  }
+  if (n <= kSingleScanMax) {
+    MF_K(k_scan_single<<<1, kThreads, 0, s>>>(load, n, out));
+    MF_CUDA(cudaGetLastError());
     return;
   }
   const int64_t nb = (n + kTile - 1) / kTile;
@@ -211,6 +243,73 @@ __global__ void k_radix_scatter(const uint64_t* keys, const uint32_t* vals, int6
   }
 }
 
+// Whole stable LSD sort of up to kSmallSort pairs in one block: every 8-bit
+// pass ranks the items with per-warp match_any counts, in shared memory.
+constexpr int kSmallSort = 1024;
+
+__global__ void __launch_bounds__(kThreads) k_radix_small(uint64_t* keys, uint32_t* vals, int n, int bits) {
+  __shared__ uint64_t sk[2][kSmallSort];
+  __shared__ uint32_t sv[2][kSmallSort];
+  __shared__ int32_t wcnt[kThreads / 32][256];
+  __shared__ int32_t dbase[256];
+  __shared__ int32_t itotal[256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    sk[0][i] = keys[i];
+    sv[0][i] = vals[i];
+  }
+  __syncthreads();
+  int cur = 0;
+  for (int shift = 0; shift < bits; shift += 8) {
+    // digit histogram -> exclusive digit bases
+    dbase[threadIdx.x] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += kThreads) atomicAdd(&dbase[(sk[cur][i] >> shift) & 255u], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      for (int d = 0; d < 256; ++d) { const int t = dbase[d]; dbase[d] = acc; acc += t; }
+    }
+    __syncthreads();
+    for (int base = 0; base < n; base += kThreads) {
+      for (int j = 0; j < kThreads / 32; ++j) wcnt[j][threadIdx.x] = 0;
+      __syncthreads();
+      const int i = base + threadIdx.x;
+      const bool valid = i < n;
+      int d = 256;
+      if (valid) d = (int)((sk[cur][i] >> shift) & 255u);
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      const int rank = __popc(peers & lt);
+      if (valid && rank == 0) wcnt[w][d] = __popc(peers);
+      __syncthreads();
+      {
+        int acc = 0;
+        for (int j = 0; j < kThreads / 32; ++j) {
+          const int t = wcnt[j][threadIdx.x];
+          wcnt[j][threadIdx.x] = acc;
+          acc += t;
+        }
+        itotal[threadIdx.x] = acc;
+      }
+      __syncthreads();
+      if (valid) {
+        const int pos = dbase[d] + wcnt[w][d] + rank;
+        sk[cur ^ 1][pos] = sk[cur][i];
+        sv[cur ^ 1][pos] = sv[cur][i];
+      }
+      __syncthreads();
+      dbase[threadIdx.x] += itotal[threadIdx.x];
+      __syncthreads();
+    }
+    cur ^= 1;
+  }
+  for (int i = threadIdx.x; i < n; i += kThreads) {
+    keys[i] = sk[cur][i];
+    vals[i] = sv[cur][i];
+  }
+}
+
 }  // namespace
 
 int bits_for(int64_t v) {
@@ -231,6 +330,11 @@ void scan_exclusive_u8(const uint8_t* in, int64_t* out, int64_t n, Scratch& ws, 
 
 void radix_sort_pairs(uint64_t* keys, uint32_t* vals, int64_t n, int bits, Scratch& ws, cudaStream_t s) {
   if (n <= 1) return;
+  if (n <= kSmallSort) {
+    MF_K(k_radix_small<<<1, kThreads, 0, s>>>(keys, vals, (int)n, bits));
+    MF_CUDA(cudaGetLastError());
+    return;
+  }
   const int nblocks = (int)((n + kTile - 1) / kTile);
   ws.keys_alt.reserve(n);
   ws.vals_alt.reserve(n);

@@ -165,81 +165,169 @@ __global__ void k_cand_compact(const uint8_t* flags, const int64_t* pos, int32_t
 
 // ---- packed sizes ---------------------------------------------------------------
 
-// Upper bound of the packed element count: 1 + len(s) + sum of len(h) per seed
-// (capped by n), plus the candidate row lengths.
-__global__ void k_size_bound(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct,
-                             unsigned long long* out) {
-  const int64_t w = warp_id();
-  const int lane = threadIdx.x & 31;
-  if (w < ns) {
-    const int32_t s = seeds[w];
-    int64_t acc = 0;
-    warp_row_each(g, s, [&](int32_t y) { acc += row_len(g, y); });
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) {
-      int64_t b = 1 + row_len(g, s) + acc;
-      if (b > g.n) b = g.n;
-      atomicAdd(out, (unsigned long long)b);
+// Upper bound of the packed element count: per seed 1 + len(s) + sum of
+// len(h) over row(s), capped by n; plus the candidate row lengths.  The sums
+// over row(s) use the load-balanced traversal (hub seeds have long rows).
+__global__ void k_lb_bound(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns,
+                           unsigned long long* uacc) {
+  int64_t cur = -1;
+  unsigned long long acc = 0;
+  lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
+    if (i != cur) {
+      if (cur >= 0 && acc) atomicAdd(uacc + cur, acc);
+      cur = i;
+      acc = 0;
     }
-  } else if (w < ns + nct) {
-    if (lane == 0) atomicAdd(out, (unsigned long long)row_len(g, cands[w - ns]));
+    acc += (unsigned long long)row_len(g, y);
+  });
+  if (cur >= 0 && acc) atomicAdd(uacc + cur, acc);
+}
+
+__global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct,
+                               const unsigned long long* uacc, unsigned long long* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long b = 0;
+  if (i < ns) {
+    b = 1ull + (unsigned long long)row_len(g, seeds[i]) + uacc[i];
+    if (b > (unsigned long long)g.n) b = (unsigned long long)g.n;
+  } else if (i < ns + nct) {
+    b = (unsigned long long)row_len(g, cands[i - ns]);
+  }
+  for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xffffffffu, b, o);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, b);
+}
+
+// ---- exact 2-hop list sizes ------------------------------------------------------
+// |2-hop list of s| = |union over h in N[s] of N[h]|, N[x] = {x} u row(x).
+// Heavy vertices (row length >= threshold) get a bitmap of N[h] built once per
+// batch (rows do not change between the sub-batches of a batch).  A seed with
+// heavy members ORs their bitmaps word-parallel into its CTA's private
+// bitmap, sets the bits of the light members' N[h] with atomics, and counts
+// with popcount; a seed with only light members and little volume sets bits
+// and counts newly set ones, then clears the words it touched.
+
+constexpr int kMaxHeavyPerSeed = 2048;
+
+__global__ void k_heavy_collect(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, int64_t thr,
+                                int32_t* slot, int32_t* list, unsigned long long* count) {
+  auto consider = [&](int32_t h) {
+    if (row_len(g, h) >= thr && slot[h] == -1 && atomicCAS(slot + h, -1, -2) == -1)
+      list[atomicAdd(count, 1ull)] = h;
+  };
+  lb_rows(g, seeds, offs, ns, [&](int64_t, int32_t, int32_t y) { consider(y); });
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (int64_t)gridDim.x * blockDim.x)
+    consider(seeds[i]);
+}
+
+__global__ void k_heavy_assign(const int32_t* list, int64_t from, int64_t to, int64_t cap, int32_t* slot) {
+  const int64_t k = from + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < to) slot[list[k]] = k < cap ? (int32_t)k : -3;
+}
+
+__global__ void k_heavy_reset(const int32_t* list, int64_t cnt, int32_t* slot) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < cnt) slot[list[k]] = -1;
+}
+
+// Bits of N[h] for the heavy vertices list[0..cnt) (their bitmaps are slots
+// from..from+cnt, zeroed before).
+__global__ void k_heavy_build(GraphView g, const int32_t* list, const int64_t* offs, int64_t cnt, int64_t from,
+                              int64_t words, uint32_t* bits) {
+  lb_rows(g, list, offs, cnt, [&](int64_t i, int32_t, int32_t y) {
+    atomicOr(bits + (from + i) * words + (y >> 5), 1u << (y & 31));
+  });
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t h = list[i];
+    atomicOr(bits + (from + i) * words + (h >> 5), 1u << (h & 31));
   }
 }
 
-// Exact |2-hop list| of each seed: each CTA owns a bitmap of n bits in global
-// memory, sets the bits of the virtual sequence, counts newly set bits, then
-// clears the words it touched.
-__global__ void __launch_bounds__(512) k_two_hop_sizes(GraphView g, const int32_t* seeds, int64_t ns,
-                                                       uint32_t* bitmaps, int64_t words, int64_t* lens) {
-  uint32_t* bm = bitmaps + (int64_t)blockIdx.x * words;
-  __shared__ unsigned long long s_cnt;
+__global__ void __launch_bounds__(512) k_exact_sizes(GraphView g, const int32_t* seeds, int64_t ns,
+                                                     const int32_t* slot, const uint32_t* hbits, int64_t words,
+                                                     uint32_t* privbm, int64_t dense_min, int64_t* lens) {
+  uint32_t* P = privbm + (int64_t)blockIdx.x * words;
+  __shared__ int32_t s_h[kMaxHeavyPerSeed];
+  __shared__ int s_nh, s_over;
+  __shared__ unsigned long long s_light, s_cnt;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int64_t i = blockIdx.x; i < ns; i += gridDim.x) {
     const int32_t s = seeds[i];
-    if (threadIdx.x == 0) s_cnt = 0;
+    if (threadIdx.x == 0) {
+      s_nh = 0;
+      s_over = 0;
+      s_light = 0;
+      s_cnt = 0;
+    }
     __syncthreads();
+    const int64_t nb = g.nindex[s + 1] - g.nindex[s];
+    const int64_t total = nb + (g.aoff[s + 1] - g.aoff[s]);
+    // classify N[s]; position -1 is s itself
+    for (int64_t k = (int64_t)threadIdx.x - 1; k < total; k += blockDim.x) {
+      const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
+      if (h < 0) continue;
+      const int32_t sl = slot[h];
+      if (sl >= 0) {
+        const int idx = atomicAdd(&s_nh, 1);
+        if (idx < kMaxHeavyPerSeed) s_h[idx] = sl; else s_over = 1;
+      } else {
+        atomicAdd(&s_light, (unsigned long long)(row_len(g, h) + 1));
+      }
+    }
+    __syncthreads();
+    const bool over = s_over != 0;
+    const int nh = over ? 0 : min(s_nh, kMaxHeavyPerSeed);
+    const bool dense = over || nh > 0 || (int64_t)s_light > dense_min;
     unsigned long long local = 0;
-    auto setbit = [&](int32_t y) {
-      const uint32_t bit = 1u << (y & 31);
-      const uint32_t old = atomicOr(bm + (y >> 5), bit);
-      if (!(old & bit)) ++local;
-    };
-    if (threadIdx.x == 0) setbit(s);
-    const int64_t b = g.nindex[s], e = g.nindex[s + 1];
-    const bool filt = g.dead[s] != 0;
-    const int64_t nb = e - b, na = g.aoff[s + 1] - g.aoff[s];
-    for (int64_t k = threadIdx.x; k < nb + na; k += blockDim.x) {
-      if (k < nb) {
-        if (!filt || live_at(g.live, b + k)) setbit(g.nlist[b + k]);
-      } else {
-        setbit(g.aadj[g.aoff[s] + (k - nb)]);
+    if (!dense) {
+      auto setbit = [&](int32_t y) {
+        const uint32_t bit = 1u << (y & 31);
+        if (!(atomicOr(P + (y >> 5), bit) & bit)) ++local;
+      };
+      if (threadIdx.x == 0) setbit(s);
+      for (int64_t k = threadIdx.x; k < total; k += blockDim.x) {
+        const int32_t h = row_elem(g, s, k, nb);
+        if (h >= 0) setbit(h);
       }
-    }
-    for (int64_t k = wid; k < nb + na; k += nw) {
-      int32_t h;
-      if (k < nb) {
-        if (filt && !live_at(g.live, b + k)) continue;
-        h = g.nlist[b + k];
-      } else {
-        h = g.aadj[g.aoff[s] + (k - nb)];
+      for (int64_t k = wid; k < total; k += nw) {
+        const int32_t h = row_elem(g, s, k, nb);
+        if (h >= 0) warp_row_each(g, h, setbit);
       }
-      warp_row_each(g, h, setbit);
+      atomicAdd(&s_cnt, local);
+      __syncthreads();
+      auto clr = [&](int32_t y) { P[y >> 5] = 0u; };
+      if (threadIdx.x == 0) clr(s);
+      for (int64_t k = threadIdx.x; k < total; k += blockDim.x) {
+        const int32_t h = row_elem(g, s, k, nb);
+        if (h >= 0) clr(h);
+      }
+      for (int64_t k = wid; k < total; k += nw) {
+        const int32_t h = row_elem(g, s, k, nb);
+        if (h >= 0) warp_row_each(g, h, clr);
+      }
+    } else {
+      for (int64_t w = threadIdx.x; w < words; w += blockDim.x) {
+        uint32_t v = 0;
+        for (int j = 0; j < nh; ++j) v |= __ldg(hbits + (int64_t)s_h[j] * words + w);
+        P[w] = v;
+      }
+      __syncthreads();
+      auto orbit = [&](int32_t y) { atomicOr(P + (y >> 5), 1u << (y & 31)); };
+      for (int64_t k = (int64_t)wid - 1; k < total; k += nw) {
+        const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
+        if (h < 0) continue;
+        if (!over && slot[h] >= 0) continue;  // covered by its bitmap
+        if (lane == 0) orbit(h);
+        warp_row_each(g, h, orbit);
+      }
+      __syncthreads();
+      for (int64_t w = threadIdx.x; w < words; w += blockDim.x) {
+        local += __popc(P[w]);
+        P[w] = 0u;
+      }
+      atomicAdd(&s_cnt, local);
     }
-    atomicAdd(&s_cnt, local);
     __syncthreads();
     if (threadIdx.x == 0) lens[i] = (int64_t)s_cnt;
-    // clear
-    auto clr = [&](int32_t y) { bm[y >> 5] = 0u; };
-    if (threadIdx.x == 0) clr(s);
-    for (int64_t k = threadIdx.x; k < nb + na; k += blockDim.x) {
-      if (k < nb) clr(g.nlist[b + k]);
-      else clr(g.aadj[g.aoff[s] + (k - nb)]);
-    }
-    for (int64_t k = wid; k < nb + na; k += nw) {
-      int32_t h = k < nb ? g.nlist[b + k] : g.aadj[g.aoff[s] + (k - nb)];
-      warp_row_each(g, h, clr);
-    }
-    (void)lane;
     __syncthreads();
   }
 }
@@ -274,39 +362,120 @@ __global__ void k_growth(const int64_t* pex, int64_t rows, int64_t* io) {
 
 // ---- clustering ------------------------------------------------------------------
 
-// f1[x] = cluster id of the first element of row(x) that has one (-1: none).
-__global__ void k_first_cid(GraphView g, const int32_t* list, int64_t cnt, const int32_t* cid, int32_t* f1) {
+// ---- first-hit row searches --------------------------------------------------------
+// First position j of row(x) (in order) whose element y satisfies a predicate,
+// for every x of a list.  A warp scans the first kFirstBound positions; rows
+// still unresolved are finished by a load-balanced pass that keeps the
+// minimum hit position per row (atomicMin), so hub rows are spread over the
+// GPU while short rows stop at their first hit.
+
+constexpr int64_t kFirstBound = 256;
+constexpr unsigned long long kNoPos = ~0ull;
+
+struct HasCid {   // the element already carries a cluster id
+  const int32_t* cid;
+  __device__ __forceinline__ bool operator()(int32_t y) const { return cid[y] != -1; }
+};
+struct HasF1 {    // the element's own row holds an element with a cluster id
+  const int32_t* f1;
+  __device__ __forceinline__ bool operator()(int32_t y) const { return f1[y] != -1; }
+};
+
+template <class P>
+__global__ void k_first_bounded(GraphView g, const int32_t* list, int64_t cnt, P pred, unsigned long long* firstpos,
+                                int32_t* unres_idx, int32_t* unres_v, int64_t* unres_cnt,
+                                unsigned long long* ucount) {
   const int64_t w = warp_id();
   if (w >= cnt) return;
+  const int lane = threadIdx.x & 31;
   const int32_t x = list[w];
-  int32_t y = -1;
-  const bool hit = warp_row_first(g, x, [&](int32_t z) { return cid[z] != -1; }, &y);
-  if ((threadIdx.x & 31) == 0) f1[x] = hit ? cid[y] : -1;
+  const int64_t nb = g.nindex[x + 1] - g.nindex[x];
+  const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
+  const int64_t lim = np < kFirstBound ? np : kFirstBound;
+  for (int64_t k0 = 0; k0 < lim; k0 += 32) {
+    const int64_t k = k0 + lane;
+    bool ok = false;
+    if (k < lim) {
+      const int32_t y = row_elem(g, x, k, nb);
+      ok = y >= 0 && pred(y);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (m) {
+      if (lane == 0) firstpos[w] = (unsigned long long)(k0 + __ffs(m) - 1);
+      return;
+    }
+  }
+  if (lane == 0) {
+    firstpos[w] = kNoPos;
+    if (np > kFirstBound) {
+      const unsigned long long u = atomicAdd(ucount, 1ull);
+      unres_idx[u] = (int32_t)w;
+      unres_v[u] = x;
+      unres_cnt[u] = np - kFirstBound;
+    }
+  }
+}
+
+template <class P>
+__global__ void k_first_rest(GraphView g, const int32_t* unres_idx, const int32_t* unres_v, const int64_t* offs,
+                             int64_t ucnt, P pred, unsigned long long* firstpos) {
+  lb_rows_pos(g, unres_v, offs, ucnt, kFirstBound, [&](int64_t i, int32_t, int32_t y, int64_t j) {
+    if (pred(y)) {
+      unsigned long long* fp = firstpos + unres_idx[i];
+      if ((unsigned long long)j < *fp) atomicMin(fp, (unsigned long long)j);
+    }
+  });
+}
+
+// f1[x] = cluster id of the first element of row(x) that has one, or -1.
+__global__ void k_f1_finish(GraphView g, const int32_t* list, int64_t cnt, const unsigned long long* firstpos,
+                            const int32_t* cid, int32_t* f1) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  const int32_t x = list[i];
+  const unsigned long long fp = firstpos[i];
+  f1[x] = fp == kNoPos ? -1 : cid[row_elem(g, x, (int64_t)fp, g.nindex[x + 1] - g.nindex[x])];
 }
 
 // Per row: early return when the row's own vertex already has an id
 // (src/misfit/misfit.cu:224), else the first existing id in row order or a
-// new one.  Seeds scan [s] ++ row(s) ++ row(h)...: f1(s), then f1(h) in order.
-__global__ void k_row_decide(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct,
-                             const int32_t* cid, const int32_t* f1, int32_t* rowcid, uint8_t* creates) {
-  const int64_t w = warp_id();
-  const int lane = threadIdx.x & 31;
-  if (w >= ns + nct) return;
-  const bool is_seed = w < ns;
-  const int32_t x = is_seed ? seeds[w] : cands[w - ns];
+// new one.  Candidates use f1(c); seeds scan [s] ++ row(s) ++ row(h)...,
+// i.e. f1(s), then f1(h) of the first h of row(s) that has one: those seeds
+// are listed in `need` for a first-hit search with HasF1.
+__global__ void k_row_decide_a(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, const int32_t* cid,
+                               const int32_t* f1, int32_t* rowcid, uint8_t* creates, int32_t* need,
+                               unsigned long long* nneed) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns + nct) return;
+  const bool seed = i < ns;
+  const int32_t x = seed ? seeds[i] : cands[i - ns];
   if (cid[x] != -1) {
-    if (lane == 0) { rowcid[w] = kSkip; creates[w] = 0; }
+    rowcid[i] = kSkip;
+    creates[i] = 0;
     return;
   }
-  int32_t fe = f1[x];
-  if (fe == -1 && is_seed) {
-    int32_t h = -1;
-    if (warp_row_first(g, x, [&](int32_t z) { return f1[z] != -1; }, &h)) fe = f1[h];
-  }
-  if (lane == 0) {
-    rowcid[w] = fe;
-    creates[w] = fe == -1 ? 1 : 0;
-  }
+  const int32_t fe = f1[x];
+  rowcid[i] = fe;
+  creates[i] = fe == -1 ? 1 : 0;
+  if (fe == -1 && seed) need[atomicAdd(nneed, 1ull)] = (int32_t)i;
+}
+
+__global__ void k_need_vertices(const int32_t* need, int64_t cnt, const int32_t* seeds, int32_t* out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < cnt) out[k] = seeds[need[k]];
+}
+
+__global__ void k_row_decide_b(GraphView g, const int32_t* need, const int32_t* needv, int64_t cnt,
+                               const unsigned long long* firstpos, const int32_t* f1, int32_t* rowcid,
+                               uint8_t* creates) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= cnt) return;
+  const unsigned long long fp = firstpos[k];
+  if (fp == kNoPos) return;
+  const int32_t s = needv[k];
+  const int32_t h = row_elem(g, s, (int64_t)fp, g.nindex[s + 1] - g.nindex[s]);
+  rowcid[need[k]] = f1[h];
+  creates[need[k]] = 0;
 }
 
 __global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid) {
@@ -422,16 +591,6 @@ __device__ bool eligible(const RepairArgs& a, int32_t w) {
   if (a.mis[w]) return false;
   if (a.v2i[w] < 0) return false;
   return !thread_any_member(a, w, -1);
-}
-
-// Element k of row(x) (base positions first, then added), or -1 if tombstoned.
-__device__ __forceinline__ int32_t row_elem(const GraphView& g, int32_t x, int64_t k, int64_t nb) {
-  if (k < nb) {
-    const int64_t gk = g.nindex[x] + k;
-    if (g.dead[x] != 0 && !live_at(g.live, gk)) return -1;
-    return g.nlist[gk];
-  }
-  return g.aadj[g.aoff[x] + (k - nb)];
 }
 
 // Single CTA walks the repair order; per chunk of 1024 edges it finds the next
@@ -737,7 +896,7 @@ __device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_
   int64_t vol = 0;
   for (int64_t k = lane; k < nr; k += 32) {
     const int32_t h = row_elem(g, r, k, nb);
-    if (h >= 0) vol += row_len(g, h);
+    if (h >= 0) vol += row_positions(g, h);   // positions, tombstoned ones included
   }
   for (int o = 16; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
   if (vol > a.big_threshold) {
@@ -751,7 +910,7 @@ __device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_
         int64_t len = 0;
         if (k < nr) {
           const int32_t h = row_elem(g, r, k, nb);
-          if (h >= 0) len = row_len(g, h);
+          if (h >= 0) len = row_positions(g, h);
         }
         int64_t inc = len;
         for (int o = 1; o < 32; o <<= 1) {
@@ -1016,6 +1175,88 @@ void row_offsets(mf_ctx* c, const int32_t* list, int64_t cnt, int kind, int64_t 
   scan_exclusive_i64(counts, c->lb_offs.p, cnt, c->ws, s);
 }
 
+// Exact 2-hop list sizes of the seeds into c->rowlens[0..ns).
+void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
+  cudaStream_t s = c->stream;
+  const int32_t n = c->n;
+  const GraphView g = c->view();
+  int64_t* h = c->h_counters;
+  const int64_t words = ((int64_t)n + 31) / 32;
+  if (c->bitmap_ctas == 0 || c->bitmap_words != words) {
+    c->bitmap_words = words;
+    int sms = 0;
+    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    const int64_t budget = (int64_t)1 << 31;  // bytes for the per-CTA private bitmaps
+    const int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 2, budget / (words * 4)));
+    c->bitmap_ctas = (int)ctas;
+    c->bitmaps.release();
+    c->bitmaps.reserve(ctas * words);
+    MF_CUDA(cudaMemsetAsync(c->bitmaps.p, 0, sizeof(uint32_t) * (size_t)(ctas * words), s));
+    // heavy-vertex bitmap cache: at most 2 GB and 4096 vertices
+    c->heavy_cap = std::max<int64_t>(0, std::min<int64_t>(4096, ((int64_t)1 << 31) / (words * 4)));
+    c->heavy_bits.release();
+    if (c->heavy_cap > 0) c->heavy_bits.reserve(c->heavy_cap * words);
+    c->heavy_list.reserve(std::max<int64_t>(n, 1));
+    c->heavy_slot.reserve(std::max<int64_t>(n, 1));
+    MF_CUDA(cudaMemsetAsync(c->heavy_slot.p, 0xFF, sizeof(int32_t) * (size_t)std::max<int32_t>(n, 1), s));
+    c->heavy_used = 0;
+  }
+  const int64_t thr = std::max<int64_t>(2048, words / 8);
+  // collect the heavy members of the seeds' closed neighbourhoods not cached yet
+  h[30] = c->heavy_used;
+  MF_CUDA(cudaMemcpyAsync(c->counters.p + 30, h + 30, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
+  MF_K(k_heavy_collect<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, thr, c->heavy_slot.p,
+                                                  c->heavy_list.p,
+                                                  reinterpret_cast<unsigned long long*>(c->counters.p) + 30));
+  MF_CUDA(cudaMemcpyAsync(h + 30, c->counters.p + 30, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
+  const int64_t total = h[30];
+  const int64_t from = c->heavy_used;
+  if (total > from) {
+    MF_K(k_heavy_assign<<<grid_for(total - from), kTB, 0, s>>>(c->heavy_list.p, from, total, c->heavy_cap,
+                                                               c->heavy_slot.p));
+    const int64_t build_to = std::min<int64_t>(total, c->heavy_cap);
+    if (build_to > from) {
+      MF_CUDA(cudaMemsetAsync(c->heavy_bits.p + from * words, 0,
+                              sizeof(uint32_t) * (size_t)((build_to - from) * words), s));
+      row_offsets(c, c->heavy_list.p + from, build_to - from, kCntAll, ns, ep);
+      MF_K(k_heavy_build<<<lb_grid(c), kTB, 0, s>>>(g, c->heavy_list.p + from, c->lb_offs.p, build_to - from, from,
+                                                     words, c->heavy_bits.p));
+    }
+    c->heavy_used = total;
+  }
+  if (ns > 0)
+    MF_K(k_exact_sizes<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ns), 512, 0, s>>>(
+        g, c->seeds.p, ns, c->heavy_slot.p, c->heavy_bits.p, words, c->bitmaps.p, words / 8, c->rowlens.p));
+  MF_CUDA(cudaGetLastError());
+}
+
+
+// First-hit search of `pred` over the rows of list[0..cnt) into c->fpos.
+template <class P>
+void first_hits(mf_ctx* c, const int32_t* list, int64_t cnt, P pred) {
+  cudaStream_t s = c->stream;
+  int64_t* h = c->h_counters;
+  c->fpos.reserve(std::max<int64_t>(cnt, 1));
+  c->un_idx.reserve(std::max<int64_t>(cnt, 1));
+  c->un_v.reserve(std::max<int64_t>(cnt, 1));
+  c->un_cnt.reserve(std::max<int64_t>(cnt, 1));
+  if (cnt == 0) return;
+  MF_CUDA(cudaMemsetAsync(c->counters.p + 32, 0, sizeof(int64_t), s));
+  MF_K(k_first_bounded<<<warps_grid(cnt), kTB, 0, s>>>(c->view(), list, cnt, pred, c->fpos.p, c->un_idx.p, c->un_v.p,
+                                                     c->un_cnt.p,
+                                                     reinterpret_cast<unsigned long long*>(c->counters.p) + 32));
+  MF_CUDA(cudaMemcpyAsync(h + 32, c->counters.p + 32, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
+  const int64_t un = h[32];
+  if (un == 0) return;
+  c->lb_offs.reserve(un + 1);
+  scan_exclusive_i64(c->un_cnt.p, c->lb_offs.p, un, c->ws, s);
+  MF_K(k_first_rest<<<lb_grid(c), kTB, 0, s>>>(c->view(), c->un_idx.p, c->un_v.p, c->lb_offs.p, un, pred,
+                                               c->fpos.p));
+}
+
 void next_epoch(mf_ctx* c) {
   if (c->epoch >= kMaxEpoch) {
     cudaStream_t s = c->stream;
@@ -1164,6 +1405,10 @@ void process_batch(mf_ctx* c, int64_t m) {
   MF_CUDA(cudaGetLastError());
   sc.reset();
 
+  if (c->heavy_used > 0) {
+    MF_K(k_heavy_reset<<<grid_for(c->heavy_used), kTB, 0, s>>>(c->heavy_list.p, c->heavy_used, c->heavy_slot.p));
+    c->heavy_used = 0;
+  }
   const int64_t big = 2 * std::min<int64_t>(m, kMaxBatchEdges) + (int64_t)n + 2;
   c->i64a.reserve(big);
   c->i64b.reserve(big);
@@ -1222,26 +1467,17 @@ void process_batch(mf_ctx* c, int64_t m) {
     // ---- packed sizes and MAX_CSR_ELEMENTS growth
     sc.emplace(c, kStSizes);
     MF_CUDA(cudaMemsetAsync(cnt + 4, 0, sizeof(int64_t), s));
-    MF_K(k_size_bound<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, ucnt + 4));
+    c->uacc.reserve(std::max<int64_t>(ns, 1));
+    MF_CUDA(cudaMemsetAsync(c->uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), s));
+    row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
+    MF_K(k_lb_bound<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, c->uacc.p));
+    MF_K(k_bound_finish<<<grid_for(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->uacc.p, ucnt + 4));
     MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     int64_t packed = -1;
     const bool exact = h[4] >= c->max_csr;
     if (exact) {
-      if (c->bitmap_ctas == 0 || c->bitmap_words != ((int64_t)n + 31) / 32) {
-        c->bitmap_words = ((int64_t)n + 31) / 32;
-        int sms = 0;
-        MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-        const int64_t budget = (int64_t)1 << 31;  // bytes for the per-CTA bitmaps
-        int64_t ctas = std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * 2, budget / (c->bitmap_words * 4)));
-        c->bitmap_ctas = (int)ctas;
-        c->bitmaps.release();
-        c->bitmaps.reserve(ctas * c->bitmap_words);
-        MF_CUDA(cudaMemsetAsync(c->bitmaps.p, 0, sizeof(uint32_t) * (size_t)(ctas * c->bitmap_words), s));
-      }
-      if (ns > 0)
-        MF_K(k_two_hop_sizes<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ns), 512, 0, s>>>(
-            g, c->seeds.p, ns, c->bitmaps.p, c->bitmap_words, c->rowlens.p));
+      exact_sizes(c, ns, ep);
       MF_K(k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns));
       scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
       h[5] = c->max_csr;
@@ -1257,10 +1493,24 @@ void process_batch(mf_ctx* c, int64_t m) {
 
     // ---- clustering (bulk-synchronous)
     sc.emplace(c, kStFirst);
-    MF_K(k_first_cid<<<warps_grid(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->cid.p, c->f1.p));
-    MF_K(k_first_cid<<<warps_grid(nh), kTB, 0, s>>>(g, c->hlist.p, nh, c->cid.p, c->f1.p));
-    MF_K(k_row_decide<<<warps_grid(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->f1.p,
-                                                  c->rowcid.p, c->creates.p));
+    first_hits(c, c->seeds.p, ns, HasCid{c->cid.p});
+    MF_K(k_f1_finish<<<grid_for(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->fpos.p, c->cid.p, c->f1.p));
+    first_hits(c, c->hlist.p, nh, HasCid{c->cid.p});
+    MF_K(k_f1_finish<<<grid_for(nh), kTB, 0, s>>>(g, c->hlist.p, nh, c->fpos.p, c->cid.p, c->f1.p));
+    MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t), s));
+    c->need.reserve(std::max<int64_t>(ns, 1));
+    c->needv.reserve(std::max<int64_t>(ns, 1));
+    MF_K(k_row_decide_a<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->f1.p,
+                                                        c->rowcid.p, c->creates.p, c->need.p, ucnt + 33));
+    MF_CUDA(cudaMemcpyAsync(h + 33, cnt + 33, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t nneed = h[33];
+    if (nneed > 0) {
+      MF_K(k_need_vertices<<<grid_for(nneed), kTB, 0, s>>>(c->need.p, nneed, c->seeds.p, c->needv.p));
+      first_hits(c, c->needv.p, nneed, HasF1{c->f1.p});
+      MF_K(k_row_decide_b<<<grid_for(nneed), kTB, 0, s>>>(g, c->need.p, c->needv.p, nneed, c->fpos.p, c->f1.p,
+                                                           c->rowcid.p, c->creates.p));
+    }
     scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
     MF_K(k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p));
     MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));

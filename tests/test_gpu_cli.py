@@ -1,0 +1,65 @@
+"""The drop-in binaries (misfit, misfit_async): same 5 arguments, same files,
+same stdout lines as the reference engines."""
+import hashlib
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from misfit_gb300 import build
+from misfit_gb300 import workloads as W
+from tests import _golden as G
+
+pytestmark = pytest.mark.gpu
+
+BIN = os.path.join(os.path.dirname(build.LIB), "..", "bin")
+
+
+def _setup(tmp_path, name="sample"):
+    g = G.load(name)
+    n = int(g["n"])
+    egr = tmp_path / (name + ".egr")
+    W.write_egr(str(egr), n, g["nindex"], g["nlist"], wide=bool(g["wide"]))
+    W.write_mis_file(str(tmp_path / "mis.txt"), g["mis0"])
+    folder = tmp_path / "batches"
+    W.write_batch_folder(str(folder), [(u, v) for u, v, _ in G.batches(g)])
+    return g, n, egr, folder
+
+
+@pytest.mark.parametrize("engine", ["misfit", "misfit_async"])
+def test_cli_final_mis_and_compaction(engine, gpu_lib, tmp_path):
+    g, n, egr, folder = _setup(tmp_path, "er1500")
+    nb = int(g["num_batches"])
+    exe = os.path.abspath(os.path.join(BIN, engine))
+    # 1) skip compaction: the .egr stays, the final MIS matches
+    env = dict(os.environ, MISFIT_SKIP_COMPACTION="1")
+    out = subprocess.run([exe, str(egr), str(tmp_path / "mis.txt"), str(folder), str(nb), "0"], cwd=str(tmp_path),
+                         env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    mis = W.read_mis_file(str(tmp_path / "datasets" / "Final_MISs" / "er1500_flash_final_mis.txt"), n)
+    assert np.array_equal(mis, g["b%d_mis_oracle" % (nb - 1)])
+    assert "Total processing time:" in out.stdout
+    assert re.search(r"Final MIS cardinality:\s+%d" % int(mis.sum()), out.stdout)
+    if engine == "misfit":
+        assert len(re.findall(r"Processing batch \d+/%d \| Edges: \d+" % nb, out.stdout)) == nb
+        assert out.stdout.count("Total Batch Time:") == nb
+    else:
+        assert len(re.findall(r"Batch \d+/%d \| edges=\d+ \| time=[0-9.]+ms" % nb, out.stdout)) == nb
+    before = egr.read_bytes()
+    # 2) with compaction: the input .egr is replaced by the merged graph
+    out = subprocess.run([exe, str(egr), str(tmp_path / "mis.txt"), str(folder), str(nb), "0"], cwd=str(tmp_path),
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    after = egr.read_bytes()
+    assert after != before
+    assert hashlib.sha256(after).digest() == bytes(g["compact_sha256"])
+
+
+def test_cli_usage_and_errors(gpu_lib, tmp_path):
+    exe = os.path.abspath(os.path.join(BIN, "misfit"))
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 1 and "Usage" in out.stderr
+    out = subprocess.run([exe, str(tmp_path / "none.egr"), "m", "b", "1", "0"], capture_output=True, text=True)
+    assert out.returncode == 1 and "ERROR" in out.stderr

@@ -216,12 +216,24 @@ for u, v in bs:
     orc.apply_batch(u, v, ins); gr.apply_batch(u, v, ins)
     assert np.array_equal(gr.get_mis(), orc.get_mis())
     assert (gr.stats()["repair_rounds"] == 0) == seq
+# free flags: tombstones in base rows and added entries at row ends
+n2 = 300
+ni2, nl2 = W.er_graph(n2, 6, 4)
+orc = O.Oracle.from_csr(ni2, nl2); gr = native.Graph.from_csr(ni2, nl2)
+mis = O.greedy_mis(ni2, nl2); orc.set_mis(mis); gr.set_mis(mis)
+rng = np.random.default_rng(9)
+for _ in range(12):
+    u = rng.integers(0, n2, 900).astype(np.int32); v = rng.integers(0, n2, 900).astype(np.int32)
+    keep = u != v; u, v = u[keep], v[keep]
+    ins = rng.integers(0, 2, u.size).astype(np.uint8)
+    orc.apply_batch(u, v, ins); gr.apply_batch(u, v, ins)
+    assert np.array_equal(gr.get_mis(), orc.get_mis())
 print("ok")
 """
 
 
 @pytest.mark.parametrize("mode,env", [("sequential", {"MISFIT_GB_REPAIR": "sequential"}),
-                                      ("grid", {"MISFIT_GB_BIG_THRESHOLD": "8"})])
+                                      ("grid", {"MISFIT_GB_BIG_THRESHOLD": "0"})])
 def test_repair_variants_match(mode, env, gpu_lib, tmp_path):
     """The single-CTA sequential repair (the fallback after the round limit)
     and the grid-wide hop-2 search (forced for every long search by a tiny
