@@ -24,8 +24,8 @@ thread_local std::string g_error;
 }
 
 std::atomic<long long> g_launches{0};
-const char* const kStageNames[kStCount] = {"overlay", "split", "seeds", "hop1", "sizes",
-                                           "cluster_read", "cluster_write", "assign", "repair", "clear"};
+const char* const kStageNames[kStCount] = {"overlay", "split",  "seeds", "hop1",  "sizes", "cluster_read",
+                                           "cluster_write", "assign", "repair", "clear", "exact", "repair_big"};
 
 void set_error(const std::string& msg) { g_error = msg; }
 const char* get_error() { return g_error.c_str(); }
@@ -91,6 +91,8 @@ void release_all(mf_ctx* c) {
   c->heavy_list.release();
   c->heavy_bits.release();
   c->fpos.release();
+  c->dense_bits.release();
+  for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();
   for (auto* b : {&c->un_idx, &c->un_v, &c->need, &c->needv}) b->release();
   c->un_cnt.release();
   c->lb_offs.release();
@@ -137,9 +139,9 @@ void run_batch(mf_ctx* c, int64_t m) {
   c->stats = mf_batch_stats{};
   c->stats.updates = m;
   c->traces.clear();
-  c->work.reserve(2 * mf::kStCount);
+  c->work.reserve(2 * mf::kStCount + 8);
   c->touched_total = 0;
-  MF_CUDA(cudaMemsetAsync(c->work.p, 0, sizeof(unsigned long long) * 2 * mf::kStCount, s));
+  MF_CUDA(cudaMemsetAsync(c->work.p, 0, sizeof(unsigned long long) * (2 * mf::kStCount + 8), s));
   MF_CUDA(cudaEventRecord(c->ev0, s));
   if (m > 0) {
     {
@@ -163,15 +165,25 @@ void run_batch(mf_ctx* c, int64_t m) {
   }
   c->ev_marks.clear();
   c->ev_used = 0;
+  static const bool debug = std::getenv("MISFIT_GB_DEBUG") != nullptr;
+  if (debug || c->profile) {
+    unsigned long long w[2 * mf::kStCount + 8];
+    MF_CUDA(cudaMemcpy(w, c->work.p, sizeof(w), cudaMemcpyDeviceToHost));
+    const unsigned long long* x = w + 2 * mf::kStCount;
+    c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + x[1] + x[2]);
+    if (debug)
+      std::fprintf(stderr, "[misfit_gb] batch: push elements seed %llu hop %llu cand %llu; sub-batches %lld\n", x[0],
+                   x[1], x[2], (long long)c->stats.sub_batches);
+  }
   if (c->profile) {
     // algorithmic bytes per stage from the device work counters:
     //   hop1: 4 B row entry + 8 B mark read-modify-write per element
     //   push: 4 B row entry + 8 B max read-modify-write per element, plus
-    //         16 B per touched vertex to resolve its cluster id
+    //         the cluster-id resolve pass: 4 B tag + 4 B id per vertex
     unsigned long long w[2 * mf::kStCount];
     MF_CUDA(cudaMemcpy(w, c->work.p, sizeof(w), cudaMemcpyDeviceToHost));
     c->stage_bytes[mf::kStHop1] += 12.0 * (double)w[2 * mf::kStHop1];
-    c->stage_bytes[mf::kStPush] += 12.0 * (double)w[2 * mf::kStPush] + 16.0 * (double)c->touched_total;
+    c->stage_bytes[mf::kStPush] += 8.0 * (double)c->touched_total;
   }
 }
 

@@ -72,12 +72,14 @@ enum Stage : int {
   kStSplit,         // previous-occurrence sort + split rule
   kStSeeds,         // seed compaction
   kStHop1,          // hop-1 marking + candidates
-  kStSizes,         // packed-size bound, exact 2-hop sizes, growth
+  kStSizes,         // packed-size upper bound
   kStFirst,         // clustering read pass (first existing ids, row decisions)
   kStPush,          // clustering write pass (2-hop max pushes, finalize)
   kStAssign,        // assignment + ordering sort
-  kStRepair,        // MIS repair
+  kStRepair,        // MIS repair: evaluation rounds and commits
   kStClear,         // clear of mapped vertices
+  kStExact,         // exact 2-hop sizes (heavy bitmaps) and limit growth
+  kStRepairBig,     // MIS repair: grid-wide hop-2 searches
   kStCount
 };
 extern const char* const kStageNames[kStCount];
@@ -313,6 +315,10 @@ struct Scratch;  // workspace for primitives
 void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s);
 void scan_exclusive_i32(const int32_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s);
 void scan_exclusive_u8(const uint8_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s);
+// Packed scan of the hop-1 marks: high 32 bits count marked vertices, low 32
+// bits marked vertices that are not seed rows (v2i < 0).
+void scan_exclusive_marks(const uint32_t* hmark, const int32_t* v2i, uint32_t epoch, int64_t* out, int64_t n,
+                          Scratch& ws, cudaStream_t s);
 // Stable LSD radix sort of (key, value) on key bits [0, bits); result in keys/vals.
 void radix_sort_pairs(uint64_t* keys, uint32_t* vals, int64_t n, int bits, Scratch& ws, cudaStream_t s);
 
@@ -354,6 +360,7 @@ struct mf_ctx {
   int64_t nnz = 0;
   uint64_t header_edges = 0;
   bool rows_sorted = true;
+  bool symmetric = false;   // every base entry has its reverse (then every overlay row too)
 
   mf::DBuf<int64_t> nindex;
   mf::DBuf<int32_t> nlist;
@@ -405,6 +412,8 @@ struct mf_ctx {
   mf::DBuf<int32_t> heavy_slot, heavy_list;
   mf::DBuf<uint32_t> heavy_bits;
   int64_t heavy_cap = 0, heavy_used = 0;
+  mf::DBuf<uint32_t> dense_bits;      // per dense seed bitmaps (exact sizes)
+  mf::DBuf<int32_t> dense_idx, dense_hl, pair_d, pair_h, todo;
   mf::DBuf<unsigned long long> fpos;   // first-hit positions
   mf::DBuf<int32_t> un_idx, un_v, need, needv;
   mf::DBuf<int64_t> un_cnt;

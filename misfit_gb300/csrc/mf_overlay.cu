@@ -36,11 +36,34 @@ __global__ void k_base_degree(const int64_t* nindex, int32_t n, int32_t* deg) {
 }
 
 // Rows non-decreasing?  (Sorted rows allow binary search for a neighbour.)
-__global__ void k_check_sorted(const int64_t* nindex, const int32_t* nlist, int32_t n, int* ok) {
-  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= n) return;
-  for (int64_t k = nindex[x] + 1; k < nindex[x + 1]; ++k)
-    if (nlist[k - 1] > nlist[k]) { atomicAnd(ok, 0); return; }
+// Load-balanced over all entries: each entry compares with its predecessor
+// in the same row.  flags[0] cleared on a descent.
+__global__ void k_check_sorted(GraphView g, const int32_t* list, const int64_t* offs, int32_t n, int* ok) {
+  lb_rows_pos(g, list, offs, n, 0, [&](int64_t, int32_t x, int32_t y, int64_t j) {
+    if (j > 0 && g.nlist[g.nindex[x] + j - 1] > y) atomicAnd(ok, 0);
+  });
+}
+
+// Every entry x -> y has its reverse y -> x (rows sorted: binary search).
+__global__ void k_check_symmetric(GraphView g, const int32_t* list, const int64_t* offs, int32_t n, int* ok) {
+  lb_rows(g, list, offs, n, [&](int64_t, int32_t x, int32_t y) {
+    int64_t lo = g.nindex[y], hi = g.nindex[y + 1];
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (g.nlist[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    if (lo >= g.nindex[y + 1] || g.nlist[lo] != x) atomicAnd(ok, 0);
+  });
+}
+
+__global__ void k_iota_n(int32_t* out, int32_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int32_t)i;
+}
+
+__global__ void k_base_positions(const int64_t* nindex, int32_t n, int64_t* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = nindex[i + 1] - nindex[i];
 }
 
 __global__ void k_check_ids(const int32_t* nlist, int64_t nnz, int32_t n, int* ok) {
@@ -377,10 +400,34 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   MF_CUDA(cudaMemcpy(ok, okp, sizeof(ok), cudaMemcpyDeviceToHost));
   if (!ok[0]) MF_FAIL(MF_EFORMAT, "nindex is not a valid offset array (non-monotone or outside [0, entries])");
   if (!ok[1]) MF_FAIL(MF_EFORMAT, "nlist holds a vertex id outside [0, nodes)");
-  if (n > 0) MF_K(k_check_sorted<<<grid_for(n), kTB, 0, s>>>(c->nindex.p, c->nlist.p, n, okp + 2));
-  MF_CUDA(cudaMemcpyAsync(ok, okp + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MF_CUDA(cudaStreamSynchronize(s));
-  c->rows_sorted = ok[0] != 0;
+  // sorted rows and symmetry (both enable the pull form of the clustering write)
+  if (n > 0) {
+    DBuf<int32_t> all;
+    DBuf<int64_t> offs;
+    all.reserve(n);
+    offs.reserve(2 * (int64_t)n + 1);
+    MF_K(k_iota_n<<<grid_for(n), kTB, 0, s>>>(all.p, n));
+    MF_K(k_base_positions<<<grid_for(n), kTB, 0, s>>>(c->nindex.p, n, offs.p + n + 1));
+    scan_exclusive_i64(offs.p + n + 1, offs.p, n, c->ws, s);
+    int sms = 0;
+    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    MF_K(k_check_sorted<<<(unsigned)(sms * 8), kTB, 0, s>>>(c->view(), all.p, offs.p, n, okp + 2));
+    MF_CUDA(cudaMemcpyAsync(ok, okp + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    c->rows_sorted = ok[0] != 0;
+    c->symmetric = false;
+    if (c->rows_sorted) {
+      MF_K(k_check_symmetric<<<(unsigned)(sms * 8), kTB, 0, s>>>(c->view(), all.p, offs.p, n, okp + 3));
+      MF_CUDA(cudaMemcpyAsync(ok, okp + 3, sizeof(int), cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaStreamSynchronize(s));
+      c->symmetric = ok[0] != 0;
+    }
+    all.release();
+    offs.release();
+  } else {
+    c->rows_sorted = true;
+    c->symmetric = true;
+  }
   c->max_csr = initial_max_csr(n, c->header_edges);
 }
 

@@ -141,26 +141,26 @@ __device__ __forceinline__ void add_work(unsigned long long* work, int64_t visit
 }
 
 __global__ void k_lb_mark_hop1(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t epoch,
-                               uint32_t* hmark, int32_t* hlist, unsigned long long* count, unsigned long long* work) {
-  const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t, int32_t, int32_t y) {
-    if (atomicExch(hmark + y, epoch) != epoch) hlist[atomicAdd(count, 1ull)] = y;
-  });
+                               uint32_t* hmark, unsigned long long* work) {
+  const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t, int32_t, int32_t y) { hmark[y] = epoch; });
   add_work(work, vis);
 }
 
-__global__ void k_cand_flags(const uint32_t* hmark, const int32_t* v2i, int32_t n, uint32_t epoch, uint8_t* flags) {
-  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x < n) flags[x] = (hmark[x] == epoch && v2i[x] < 0) ? 1 : 0;
-}
-
-__global__ void k_cand_compact(const uint8_t* flags, const int64_t* pos, int32_t n, int64_t cap, int64_t ns,
-                               int32_t* cands, int32_t* v2i) {
-  int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= n || !flags[x]) return;
-  const int64_t k = pos[x];
-  if (k >= cap) return;
-  cands[k] = (int32_t)x;
-  v2i[x] = (int32_t)(ns + k);
+// Both lists from the packed scan: hlist = marked vertices, cands = marked
+// vertices that are not seeds (ascending id, capped).
+__global__ void k_mark_compact(const uint32_t* hmark, const int64_t* pos, int32_t n, uint32_t epoch, int64_t cap,
+                               int64_t ns, int32_t* hlist, int32_t* cands, int32_t* v2i) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n || hmark[x] != epoch) return;
+  const int64_t pk = pos[x];
+  hlist[pk >> 32] = (int32_t)x;
+  if (v2i[x] < 0) {
+    const int64_t k = pk & 0xffffffffll;
+    if (k < cap) {
+      cands[k] = (int32_t)x;
+      v2i[x] = (int32_t)(ns + k);
+    }
+  }
 }
 
 // ---- packed sizes ---------------------------------------------------------------
@@ -242,26 +242,43 @@ __global__ void k_heavy_build(GraphView g, const int32_t* list, const int64_t* o
   }
 }
 
-__global__ void __launch_bounds__(512) k_exact_sizes(GraphView g, const int32_t* seeds, int64_t ns,
-                                                     const int32_t* slot, const uint32_t* hbits, int64_t words,
-                                                     uint32_t* privbm, int64_t dense_min, int64_t* lens) {
+// Classification pass, one CTA per seed: heavy members (cached bitmaps) and
+// the light volume of N[s].  Seeds with little light volume and no heavy
+// member are counted right here in the CTA's private bitmap (set bits,
+// count newly set ones, clear what was touched).  The others are "dense":
+// each gets a global bitmap (at most dmax of them per pass; the rest are
+// marked -2 for the next pass), its heavy slots and its light members go
+// to lists that the grid-wide passes below consume.
+struct DenseOut {
+  unsigned long long* ndense;     // dense seeds accepted
+  int32_t* dseed;                 // dense index -> seed index
+  int32_t* dhoff;                 // dense index -> offset in hlist
+  int32_t* dnh;                   // dense index -> heavy count
+  int32_t* hlist;                 // heavy slots of all dense seeds
+  unsigned long long* hused;
+  int32_t* pair_d;                // light members: dense index
+  int32_t* pair_h;                // light members: vertex
+  unsigned long long* npairs;
+  int64_t dmax, hcap, pcap;
+};
+
+__global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32_t* seeds, const int32_t* todo,
+                                                        int64_t ntodo, const int32_t* slot, int64_t words,
+                                                        uint32_t* privbm, int64_t dense_min, int64_t* lens,
+                                                        DenseOut o) {
   uint32_t* P = privbm + (int64_t)blockIdx.x * words;
   __shared__ int32_t s_h[kMaxHeavyPerSeed];
-  __shared__ int s_nh, s_over;
-  __shared__ unsigned long long s_light, s_cnt;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int64_t i = blockIdx.x; i < ns; i += gridDim.x) {
+  __shared__ int s_nh, s_over, s_d;
+  __shared__ unsigned long long s_light, s_lcount, s_cnt, s_pbase, s_pfill;
+  __shared__ int s_hoff;
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t t = blockIdx.x; t < ntodo; t += gridDim.x) {
+    const int64_t i = todo[t];
     const int32_t s = seeds[i];
-    if (threadIdx.x == 0) {
-      s_nh = 0;
-      s_over = 0;
-      s_light = 0;
-      s_cnt = 0;
-    }
+    if (threadIdx.x == 0) { s_nh = 0; s_over = 0; s_light = 0; s_lcount = 0; s_cnt = 0; s_pfill = 0; }
     __syncthreads();
     const int64_t nb = g.nindex[s + 1] - g.nindex[s];
     const int64_t total = nb + (g.aoff[s + 1] - g.aoff[s]);
-    // classify N[s]; position -1 is s itself
     for (int64_t k = (int64_t)threadIdx.x - 1; k < total; k += blockDim.x) {
       const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
       if (h < 0) continue;
@@ -271,14 +288,14 @@ __global__ void __launch_bounds__(512) k_exact_sizes(GraphView g, const int32_t*
         if (idx < kMaxHeavyPerSeed) s_h[idx] = sl; else s_over = 1;
       } else {
         atomicAdd(&s_light, (unsigned long long)(row_len(g, h) + 1));
+        atomicAdd(&s_lcount, 1ull);
       }
     }
     __syncthreads();
     const bool over = s_over != 0;
-    const int nh = over ? 0 : min(s_nh, kMaxHeavyPerSeed);
-    const bool dense = over || nh > 0 || (int64_t)s_light > dense_min;
-    unsigned long long local = 0;
+    const bool dense = over || s_nh > 0 || (int64_t)s_light > dense_min;
     if (!dense) {
+      unsigned long long local = 0;
       auto setbit = [&](int32_t y) {
         const uint32_t bit = 1u << (y & 31);
         if (!(atomicOr(P + (y >> 5), bit) & bit)) ++local;
@@ -304,32 +321,92 @@ __global__ void __launch_bounds__(512) k_exact_sizes(GraphView g, const int32_t*
         const int32_t h = row_elem(g, s, k, nb);
         if (h >= 0) warp_row_each(g, h, clr);
       }
+      __syncthreads();
+      if (threadIdx.x == 0) lens[i] = (int64_t)s_cnt;
     } else {
-      for (int64_t w = threadIdx.x; w < words; w += blockDim.x) {
-        uint32_t v = 0;
-        for (int j = 0; j < nh; ++j) v |= __ldg(hbits + (int64_t)s_h[j] * words + w);
-        P[w] = v;
+      const int nh = over ? 0 : s_nh;
+      const unsigned long long lc = over ? (unsigned long long)(total + 1) : s_lcount;
+      if (threadIdx.x == 0) {
+        s_d = -1;
+        const unsigned long long d = atomicAdd(o.ndense, 1ull);
+        const unsigned long long hoff = atomicAdd(o.hused, (unsigned long long)nh);
+        const unsigned long long pb = atomicAdd(o.npairs, lc);
+        if ((int64_t)d < o.dmax && (int64_t)(hoff + nh) <= o.hcap && (int64_t)(pb + lc) <= o.pcap) {
+          s_d = (int)d;
+          s_hoff = (int)hoff;
+          s_pbase = pb;
+          o.dseed[d] = (int32_t)i;
+          o.dhoff[d] = (int32_t)hoff;
+          o.dnh[d] = nh;
+          lens[i] = 0;
+        } else {
+          if ((int64_t)d < o.dmax) o.dseed[d] = -1;   // index taken but unused
+          lens[i] = -2;                                  // retried in the next pass
+        }
       }
       __syncthreads();
-      auto orbit = [&](int32_t y) { atomicOr(P + (y >> 5), 1u << (y & 31)); };
-      for (int64_t k = (int64_t)wid - 1; k < total; k += nw) {
-        const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
-        if (h < 0) continue;
-        if (!over && slot[h] >= 0) continue;  // covered by its bitmap
-        if (lane == 0) orbit(h);
-        warp_row_each(g, h, orbit);
+      const int d = s_d;
+      if (d >= 0) {
+        for (int j = threadIdx.x; j < nh; j += blockDim.x) o.hlist[s_hoff + j] = s_h[j];
+        for (int64_t k = (int64_t)threadIdx.x - 1; k < total; k += blockDim.x) {
+          const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
+          if (h < 0) continue;
+          if (!over && slot[h] >= 0) continue;
+          const unsigned long long q = s_pbase + atomicAdd(&s_pfill, 1ull);
+          o.pair_d[q] = d;
+          o.pair_h[q] = h;
+        }
       }
-      __syncthreads();
-      for (int64_t w = threadIdx.x; w < words; w += blockDim.x) {
-        local += __popc(P[w]);
-        P[w] = 0u;
-      }
-      atomicAdd(&s_cnt, local);
     }
     __syncthreads();
-    if (threadIdx.x == 0) lens[i] = (int64_t)s_cnt;
-    __syncthreads();
   }
+}
+
+// Dense bitmaps: P_d = OR of the heavy members' cached bitmaps.
+__global__ void k_dense_or(int64_t nd, const int32_t* dseed, const int32_t* dhoff, const int32_t* dnh,
+                           const int32_t* hlist, const uint32_t* hbits, int64_t words, uint32_t* dbits) {
+  const int64_t d = blockIdx.y;
+  if (d >= nd) return;
+  const int32_t nh = dseed[d] >= 0 ? dnh[d] : 0;
+  const int32_t* hl = hlist + dhoff[d];
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t v = 0;
+    for (int j = 0; j < nh; ++j) v |= __ldg(hbits + (int64_t)hl[j] * words + w);
+    dbits[d * words + w] = v;
+  }
+}
+
+// Dense bitmaps: bits of N[h] for every light member h (load-balanced).
+__global__ void k_dense_light(GraphView g, const int32_t* pair_d, const int32_t* pair_h, const int64_t* offs,
+                              int64_t np, int64_t words, uint32_t* dbits) {
+  lb_rows(g, pair_h, offs, np, [&](int64_t k, int32_t, int32_t y) {
+    atomicOr(dbits + (int64_t)pair_d[k] * words + (y >> 5), 1u << (y & 31));
+  });
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < np; k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t h = pair_h[k];
+    atomicOr(dbits + (int64_t)pair_d[k] * words + (h >> 5), 1u << (h & 31));
+  }
+}
+
+__global__ void k_dense_pop(int64_t nd, const int32_t* dseed, int64_t words, const uint32_t* dbits, int64_t* lens) {
+  const int64_t d = blockIdx.y;
+  if (d >= nd || dseed[d] < 0) return;
+  unsigned long long c = 0;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x)
+    c += __popc(dbits[d * words + w]);
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(reinterpret_cast<unsigned long long*>(lens + dseed[d]), c);
+}
+
+__global__ void k_todo_retry(const int64_t* lens, const int32_t* todo, int64_t ntodo, int32_t* out,
+                             unsigned long long* cnt) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ntodo && lens[todo[t]] == -2) out[atomicAdd(cnt, 1ull)] = todo[t];
+}
+
+__global__ void k_iota(int32_t* out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int32_t)i;
 }
 
 __global__ void k_cand_lens(GraphView g, const int32_t* cands, int64_t nct, int64_t* lens) {
@@ -497,47 +574,96 @@ __global__ void k_lb_push_seed(GraphView g, const int32_t* seeds, const int64_t*
   add_work(work, vis);
 }
 
-__device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag, uint32_t epoch, int32_t* touched,
-                                       unsigned long long* tcount) {
-  const uint32_t old = atomicMax(wval + y, tag);
-  if ((old >> kRowBits) != epoch) touched[atomicAdd(tcount, 1ull)] = y;
-}
+// The pushes are reductions whose results are not read back, so they issue
+// as fire-and-forget RED operations.
+__device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag) { atomicMax(wval + y, tag); }
 
 // Phase 2: wval[y] = max over x with y in {x} u row(x) of bval[x] (the 2-hop
 // reach of the seed rows), and the candidate rows' own tags over row(c).
-__global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, const uint32_t* bval, uint32_t* wval,
-                            int32_t* touched, unsigned long long* tcount) {
+__global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, const uint32_t* bval, uint32_t* wval) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cnt) return;
   const int32_t x = list[i];
   const uint32_t t = bval[x];
-  if ((t >> kRowBits) == epoch) push_w(wval, x, t, epoch, touched, tcount);
+  if ((t >> kRowBits) == epoch) push_w(wval, x, t);
 }
 
 __global__ void k_lb_push_hop(GraphView g, const int32_t* list, const int64_t* offs, int64_t cnt, uint32_t epoch,
-                              const uint32_t* bval, uint32_t* wval, int32_t* touched, unsigned long long* tcount,
-                              unsigned long long* work) {
-  const int64_t vis = lb_rows(g, list, offs, cnt, [&](int64_t, int32_t x, int32_t y) {
-    push_w(wval, y, bval[x], epoch, touched, tcount);
-  });
+                              const uint32_t* bval, uint32_t* wval, unsigned long long* work) {
+  const int64_t vis = lb_rows(g, list, offs, cnt, [&](int64_t, int32_t x, int32_t y) { push_w(wval, y, bval[x]); });
   add_work(work, vis);
 }
 
 __global__ void k_lb_push_cand(GraphView g, const int32_t* cands, const int64_t* offs, int64_t nct, int64_t ns,
-                               uint32_t epoch, uint32_t* wval, int32_t* touched, unsigned long long* tcount,
-                               unsigned long long* work) {
+                               uint32_t epoch, uint32_t* wval, unsigned long long* work) {
   const int64_t vis = lb_rows(g, cands, offs, nct, [&](int64_t i, int32_t, int32_t y) {
-    push_w(wval, y, (epoch << kRowBits) | (uint32_t)(ns + i), epoch, touched, tcount);
+    push_w(wval, y, (epoch << kRowBits) | (uint32_t)(ns + i));
   });
   add_work(work, vis);
 }
 
-__global__ void k_finalize_cid(const int32_t* touched, int64_t cnt, const uint32_t* wval, const int32_t* rowcid,
-                               int32_t* cid) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= cnt) return;
-  const int32_t y = touched[k];
-  cid[y] = rowcid[wval[y] & kRowMask];
+// Pull form of the candidate writes (symmetric graphs with sorted base rows).
+// The candidate rows that write are the non-skipped ones, and their tags
+// grow with the candidate's vertex id (candidates are packed in ascending
+// id), so the last writer of y among them is its largest-id non-skipped
+// candidate neighbour: the added part of row(y) is scanned, then the base
+// part from its end until the first such neighbour.  That tag dominates every
+// seed-row tag; without one, the pushed seed-row tag (wval) decides.
+__global__ void k_pull_cand(GraphView g, const int32_t* v2i, const int32_t* rowcid, int64_t ns, const uint32_t* wval,
+                            uint32_t epoch, int32_t* cid, unsigned long long* work) {
+  const int64_t yi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t visited = 0;
+  if (yi < g.n) {
+    const int32_t y = (int32_t)yi;
+    auto nonskip = [&](int32_t c) {
+      const int32_t vi = v2i[c];
+      return (int64_t)vi >= ns && rowcid[vi] != kSkip;
+    };
+    int32_t best = -1;
+    for (int64_t k = g.aoff[y]; k < g.aoff[y + 1]; ++k) {
+      const int32_t c = g.aadj[k];
+      ++visited;
+      if (c > best && nonskip(c)) best = c;
+    }
+    const int64_t b = g.nindex[y], e = g.nindex[y + 1];
+    const bool filt = g.dead[y] != 0;
+    for (int64_t k = e - 1; k >= b; --k) {
+      const int32_t c = __ldg(g.nlist + k);
+      ++visited;
+      if (c <= best) break;
+      if (filt && !live_at(g.live, k)) continue;
+      if (nonskip(c)) {
+        best = c;
+        break;
+      }
+    }
+    if (best >= 0) {
+      cid[y] = rowcid[v2i[best]];
+    } else {
+      const uint32_t t = wval[y];
+      if ((t >> kRowBits) == epoch) cid[y] = rowcid[t & kRowMask];
+    }
+  }
+  add_work(work, visited);
+}
+
+// cid[y] = id of the row that wrote y last, for every y tagged this epoch.
+__global__ void k_finalize_all(const uint32_t* wval, int32_t n, uint32_t epoch, const int32_t* rowcid, int32_t* cid) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t x0 = q * 4;
+  if (x0 >= n) return;
+  if (x0 + 4 <= n) {
+    const uint4 t = reinterpret_cast<const uint4*>(wval)[q];
+    if ((t.x >> kRowBits) == epoch) cid[x0 + 0] = rowcid[t.x & kRowMask];
+    if ((t.y >> kRowBits) == epoch) cid[x0 + 1] = rowcid[t.y & kRowMask];
+    if ((t.z >> kRowBits) == epoch) cid[x0 + 2] = rowcid[t.z & kRowMask];
+    if ((t.w >> kRowBits) == epoch) cid[x0 + 3] = rowcid[t.w & kRowMask];
+  } else {
+    for (int64_t x = x0; x < n; ++x) {
+      const uint32_t t = wval[x];
+      if ((t >> kRowBits) == epoch) cid[x] = rowcid[t & kRowMask];
+    }
+  }
 }
 
 // ---- assignment and order ------------------------------------------------------------
@@ -770,7 +896,7 @@ __global__ void __launch_bounds__(1024) k_repair_sequential(RepairArgs a) {
 // the sequential kernel.
 
 constexpr int kMaxRounds = 48;
-constexpr int64_t kBigThreshold = 4096;   // hop-2 volume above which the grid-wide search runs
+constexpr int64_t kBigThreshold = 256;    // hop-2 volume above which the grid-wide search runs
 
 struct View {
   const uint8_t* m;     // bit 0: committed membership; bit 1: pending writes exist
@@ -877,18 +1003,63 @@ __device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t e
   return false;
 }
 
+// Thread: 1 if row-of(x) holds a member (other than `except`), 0 if it holds
+// none, -1 if `budget` elements were read without an answer.
+__device__ int t_any_bounded(const SpecArgs& a, const Member& mem, int32_t x, int32_t except, int budget) {
+  int left = budget;
+  int res = 0;
+  auto hit = [&](int32_t z) {
+    if (z != except && mem(z) != 0) { res = 1; return true; }
+    if (--left <= 0) { res = -1; return true; }
+    return false;
+  };
+  if (!spec_seed(a, x)) {
+    thread_row_until(a.g, x, hit);
+    return res;
+  }
+  if (x != except && mem(x)) return 1;
+  if (thread_row_until(a.g, x, hit)) return res;
+  thread_row_until(a.g, x, [&](int32_t h) { return thread_row_until(a.g, h, hit); });
+  return res;
+}
+
+// Warp: first eligible element of row(x) in row order, or -1.  Every lane
+// checks its element with a short serial scan; the elements left undecided
+// (a long row without an early member) are settled by the whole warp, in
+// position order, so a hub element does not keep one lane scanning alone.
+__device__ int32_t w_first_eligible_row(const SpecArgs& a, const Member& mem, int32_t x) {
+  const GraphView& g = a.g;
+  const int lane = threadIdx.x & 31;
+  const int64_t nb = g.nindex[x + 1] - g.nindex[x];
+  const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
+  for (int64_t k0 = 0; k0 < np; k0 += 32) {
+    const int64_t k = k0 + lane;
+    const int32_t w = k < np ? row_elem(g, x, k, nb) : -1;
+    int state = 0;  // 0 not eligible, 1 eligible, 2 undecided
+    if (w >= 0 && !mem(w) && a.v2i[w] >= 0) {
+      const int r = t_any_bounded(a, mem, w, -1, 64);
+      state = r == 0 ? 1 : (r < 0 ? 2 : 0);
+    }
+    unsigned m = __ballot_sync(0xffffffffu, state != 0);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const int32_t ww = __shfl_sync(0xffffffffu, w, src);
+      const int st = __shfl_sync(0xffffffffu, state, src);
+      if (st == 1 || !w_any(a, mem, ww, -1)) return ww;
+    }
+  }
+  return -1;
+}
+
 // Warp: first eligible w of row-of(r) in order (src/misfit/misfit.cu:300-314), or -1.
 __device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_t r) {
   const GraphView& g = a.g;
   const int lane = threadIdx.x & 31;
   const bool seed = spec_seed(a, r);
-  if (seed) {
-    const int e = (lane == 0 && t_eligible(a, mem, r)) ? 1 : 0;
-    if (__shfl_sync(0xffffffffu, e, 0)) return r;
-  }
-  auto pred = [&](int32_t z) { return t_eligible(a, mem, z); };
-  int32_t w = -1;
-  if (warp_row_first(g, r, pred, &w)) return w;
+  if (seed && !mem(r) && a.v2i[r] >= 0 && !w_any(a, mem, r, -1)) return r;
+  int32_t w = w_first_eligible_row(a, mem, r);
+  if (w >= 0) return w;
   if (!seed) return -1;
   const int64_t nb = g.nindex[r + 1] - g.nindex[r];
   const int64_t nr = nb + (g.aoff[r + 1] - g.aoff[r]);
@@ -934,7 +1105,8 @@ __device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_
   for (int64_t k = 0; k < nr; ++k) {
     const int32_t h = row_elem(g, r, k, nb);
     if (h < 0) continue;
-    if (warp_row_first(g, h, pred, &w)) return w;
+    w = w_first_eligible_row(a, mem, h);
+    if (w >= 0) return w;
   }
   return -1;
 }
@@ -1226,9 +1398,54 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
     }
     c->heavy_used = total;
   }
-  if (ns > 0)
-    MF_K(k_exact_sizes<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ns), 512, 0, s>>>(
-        g, c->seeds.p, ns, c->heavy_slot.p, c->heavy_bits.p, words, c->bitmaps.p, words / 8, c->rowlens.p));
+  if (ns == 0) return;
+  // per-pass capacity of the dense bitmaps: 1 GB, at least one seed
+  const int64_t dmax = std::max<int64_t>(1, std::min<int64_t>(ns, ((int64_t)1 << 30) / (words * 4)));
+  c->dense_bits.reserve(dmax * words);
+  c->dense_idx.reserve(3 * dmax);
+  c->dense_hl.reserve(std::max<int64_t>(kMaxHeavyPerSeed, std::min<int64_t>(dmax * 64, (int64_t)1 << 22)));
+  const int64_t pcap = std::max<int64_t>(4096, std::min<int64_t>((int64_t)1 << 26, 2 * c->nnz + 1));
+  c->pair_d.reserve(pcap);
+  c->pair_h.reserve(pcap);
+  c->todo.reserve(2 * ns);
+  MF_K(k_iota<<<grid_for(ns), kTB, 0, s>>>(c->todo.p, ns));
+  int32_t* todo = c->todo.p;
+  int32_t* todo_next = c->todo.p + ns;
+  int64_t ntodo = ns;
+  unsigned long long* cnts = reinterpret_cast<unsigned long long*>(c->counters.p) + 40;
+  while (ntodo > 0) {
+    MF_CUDA(cudaMemsetAsync(cnts, 0, sizeof(unsigned long long) * 4, s));
+    DenseOut o{cnts + 0, c->dense_idx.p, c->dense_idx.p + dmax, c->dense_idx.p + 2 * dmax, c->dense_hl.p, cnts + 1,
+               c->pair_d.p, c->pair_h.p, cnts + 2, dmax, c->dense_hl.cap, pcap};
+    MF_K(k_exact_classify<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ntodo), 512, 0, s>>>(
+        g, c->seeds.p, todo, ntodo, c->heavy_slot.p, words, c->bitmaps.p, words / 8, c->rowlens.p, o));
+    MF_CUDA(cudaMemcpyAsync(h + 40, c->counters.p + 40, sizeof(int64_t) * 3, cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t nd = std::min<int64_t>((int64_t)h[40], dmax);
+    const int64_t np = std::min<int64_t>((int64_t)h[42], pcap);
+    if (nd > 0) {
+      const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(64, (words + 1023) / 1024));
+      MF_K(k_dense_or<<<dim3(gx, (unsigned)nd), 256, 0, s>>>(nd, c->dense_idx.p, c->dense_idx.p + dmax,
+                                                            c->dense_idx.p + 2 * dmax, c->dense_hl.p,
+                                                            c->heavy_bits.p, words, c->dense_bits.p));
+      if (np > 0) {
+        row_offsets(c, c->pair_h.p, np, kCntAll, ns, ep);
+        MF_K(k_dense_light<<<lb_grid(c), kTB, 0, s>>>(g, c->pair_d.p, c->pair_h.p, c->lb_offs.p, np, words,
+                                                       c->dense_bits.p));
+      }
+      MF_K(k_dense_pop<<<dim3(gx, (unsigned)nd), 256, 0, s>>>(nd, c->dense_idx.p, words, c->dense_bits.p,
+                                                             c->rowlens.p));
+    }
+    // seeds that did not fit this pass
+    MF_CUDA(cudaMemsetAsync(cnts + 3, 0, sizeof(unsigned long long), s));
+    MF_K(k_todo_retry<<<grid_for(ntodo), kTB, 0, s>>>(c->rowlens.p, todo, ntodo, todo_next, cnts + 3));
+    MF_CUDA(cudaMemcpyAsync(h + 43, c->counters.p + 43, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t left = h[43];
+    if (left >= ntodo) MF_FAIL(MF_ESTATE, "exact 2-hop sizes made no progress");
+    std::swap(todo, todo_next);
+    ntodo = left;
+  }
   MF_CUDA(cudaGetLastError());
 }
 
@@ -1324,6 +1541,8 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
   MF_CUDA(cudaMemsetAsync(c->rp_w1.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
   const int nbits = bits_for(std::max<int32_t>(c->n - 1, 1));
   int64_t p0 = 0, nview = 0, rounds = 0;
+  std::optional<StageScope> rsc;
+  rsc.emplace(c, kStRepair);
   while (p0 < nproc) {
     if (rounds >= kMaxRounds) {
       if (nview > 0) MF_K(k_spec_clear_flags<<<grid_for(nview), kTB, 0, s>>>(c->rp_keys.p, nview, c->mis.p));
@@ -1339,10 +1558,13 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
                View{c->mis.p, c->rp_keys.p, c->rp_vals.p, nview}, c->rp_n0.p, c->rp_n1.p,
                big_threshold(), ucnt + 24, c->big_pos.p, c->big_r.p, c->big_off.p, c->big_nr.p,
                c->big_pre.p, ucnt + 25, c->big_pre.cap};
+    rsc.emplace(c, kStRepair);
     MF_K(k_spec_eval<<<warps_grid(pending), kTB, 0, s>>>(a));
+    rsc.emplace(c, kStRepairBig);
     MF_K(k_big_prep<<<1, 1024, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
     MF_K(k_big_scan<<<(unsigned)c->big_grid, 256, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
     MF_K(k_big_finalize<<<grid_for(pending), kTB, 0, s>>>(a, c->big_best.p));
+    rsc.emplace(c, kStRepair);
     h[20] = (int64_t)nproc;
     MF_CUDA(cudaMemcpyAsync(c->counters.p + 20, h + 20, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     MF_K(k_spec_first_change<<<grid_for(pending), kTB, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0,
@@ -1449,17 +1671,17 @@ void process_batch(mf_ctx* c, int64_t m) {
     sc.emplace(c, kStHop1);
     next_epoch(c);
     const uint32_t ep = c->epoch;
-    MF_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int64_t), s));
     row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
-    MF_K(k_lb_mark_hop1<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->hmark.p, c->hlist.p,
-                                                   ucnt + 2, c->work.p + 2 * kStHop1));
-    MF_K(k_cand_flags<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->v2i.p, n, ep, c->u8a.p));
-    scan_exclusive_u8(c->u8a.p, c->i64a.p, n, c->ws, s);
+    MF_K(k_lb_mark_hop1<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->hmark.p,
+                                                   c->work.p + 2 * kStHop1));
+    scan_exclusive_marks(c->hmark.p, c->v2i.p, ep, c->i64a.p, n, c->ws, s);
     const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
-    MF_K(k_cand_compact<<<grid_for(n), kTB, 0, s>>>(c->u8a.p, c->i64a.p, n, capc, ns, c->cands.p, c->v2i.p));
-    MF_CUDA(cudaMemcpyAsync(h + 3, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    MF_CUDA(cudaMemcpyAsync(h + 2, cnt + 2, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_K(k_mark_compact<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->i64a.p, n, ep, capc, ns, c->hlist.p, c->cands.p,
+                                                    c->v2i.p));
+    MF_CUDA(cudaMemcpyAsync(h + 2, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
+    h[3] = h[2] & 0xffffffffll;
+    h[2] = h[2] >> 32;
     const int64_t nh = h[2];
     const int64_t nct = std::min<int64_t>(h[3], capc);
     const int64_t rows = ns + nct;
@@ -1477,6 +1699,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     int64_t packed = -1;
     const bool exact = h[4] >= c->max_csr;
     if (exact) {
+      sc.emplace(c, kStExact);
       exact_sizes(c, ns, ep);
       MF_K(k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns));
       scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
@@ -1515,28 +1738,30 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_K(k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p));
     MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     sc.emplace(c, kStPush);
-    unsigned long long* wk = c->work.p + 2 * kStPush;
+    unsigned long long* wk_extra = c->work.p + 2 * kStCount;   // [0] seed, [1] hop, [2] candidate pushes
     MF_K(k_seed_self<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedRows, ns, ep);
-    MF_K(k_lb_push_seed<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk));
-    MF_CUDA(cudaMemsetAsync(cnt + 8, 0, sizeof(int64_t), s));
-    MF_K(k_self_push<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
-    MF_K(k_self_push<<<grid_for(nh), kTB, 0, s>>>(c->hlist.p, nh, ep, c->bval.p, c->wval.p, c->touched.p, ucnt + 8));
+    MF_K(k_lb_push_seed<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk_extra + 0));
+    MF_K(k_self_push<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, ep, c->bval.p, c->wval.p));
+    MF_K(k_self_push<<<grid_for(nh), kTB, 0, s>>>(c->hlist.p, nh, ep, c->bval.p, c->wval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedPushers, ns, ep);
     MF_K(k_lb_push_hop<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, c->wval.p,
-                                                  c->touched.p, ucnt + 8, wk));
+                                                  wk_extra + 1));
     row_offsets(c, c->hlist.p, nh, kCntHopPushers, ns, ep);
     MF_K(k_lb_push_hop<<<lb_grid(c), kTB, 0, s>>>(g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p, c->wval.p,
-                                                  c->touched.p, ucnt + 8, wk));
-    row_offsets(c, c->cands.p, nct, kCntCandRows, ns, ep);
-    MF_K(k_lb_push_cand<<<lb_grid(c), kTB, 0, s>>>(g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
-                                                   c->touched.p, ucnt + 8, wk));
-    MF_CUDA(cudaMemcpyAsync(h + 8, cnt + 8, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                                                  wk_extra + 1));
+    if (c->symmetric && c->rows_sorted) {
+      MF_K(k_pull_cand<<<grid_for(n), kTB, 0, s>>>(g, c->v2i.p, c->rowcid.p, ns, c->wval.p, ep, c->cid.p,
+                                                   wk_extra + 2));
+    } else {
+      row_offsets(c, c->cands.p, nct, kCntCandRows, ns, ep);
+      MF_K(k_lb_push_cand<<<lb_grid(c), kTB, 0, s>>>(g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
+                                                     wk_extra + 2));
+      MF_K(k_finalize_all<<<grid_for(((int64_t)n + 3) / 4), kTB, 0, s>>>(c->wval.p, n, ep, c->rowcid.p, c->cid.p));
+    }
+    c->touched_total += n;
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t cc = h[7];
-    const int64_t ntouched = h[8];
-    c->touched_total += ntouched;
-    MF_K(k_finalize_cid<<<grid_for(ntouched), kTB, 0, s>>>(c->touched.p, ntouched, c->wval.p, c->rowcid.p, c->cid.p));
     MF_CUDA(cudaGetLastError());
 
     sc.reset();
@@ -1562,8 +1787,8 @@ void process_batch(mf_ctx* c, int64_t m) {
     const int64_t nproc = h[9];
     radix_sort_pairs(c->keys.p, c->vals.p, nproc, kRowBits + bits_for(std::max<int64_t>(limit, 1)), c->ws, s);
 
-    // ---- repair
-    sc.emplace(c, kStRepair);
+    // ---- repair (times itself: rounds vs grid-wide searches)
+    sc.reset();
     if (nproc > 0) c->stats.repair_rounds += repair(c, g, p, nproc, ns);
     sc.reset();
     if (tr) {

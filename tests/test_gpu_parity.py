@@ -248,3 +248,44 @@ def test_repair_variants_match(mode, env, gpu_lib, tmp_path):
                          capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     assert out.stdout.strip().endswith("ok")
+
+
+@pytest.mark.parametrize("layout", ["unsorted_rows", "asymmetric"])
+def test_general_graphs_use_push_form(layout, gpu_lib):
+    """Graphs that are not symmetric with sorted rows take the push form of
+    the clustering write; results still equal the oracle's."""
+    n, (ni, nl) = W.rmat_graph(10, 8, 31)
+    nl = nl.copy()
+    rng = np.random.default_rng(2)
+    if layout == "unsorted_rows":
+        for x in range(n):
+            seg = nl[ni[x]:ni[x + 1]]
+            nl[ni[x]:ni[x + 1]] = seg[rng.permutation(seg.size)]
+    else:
+        # drop one direction of some entries: rebuild CSR without them
+        deg = np.diff(ni)
+        src = np.repeat(np.arange(n), deg)
+        keep = ~((src < nl) & (rng.random(nl.size) < 0.1))
+        src, dst = src[keep], nl[keep]
+        ni = np.zeros(n + 1, np.int64)
+        np.cumsum(np.bincount(src, minlength=n), out=ni[1:])
+        nl = dst.astype(np.int32)
+    orc = O.Oracle.from_csr(ni, nl)
+    gr = native.Graph.from_csr(ni, nl)
+    mis = O.greedy_mis(ni, nl)
+    orc.set_mis(mis)
+    gr.set_mis(mis)
+    u = rng.integers(0, n, 1500).astype(np.int32)
+    v = rng.integers(0, n, 1500).astype(np.int32)
+    keep = u != v
+    u, v = u[keep], v[keep]
+    for k in range(3):
+        sl = slice(k * 400, (k + 1) * 400)
+        ins = orc.flag_updates(u[sl], v[sl])
+        assert np.array_equal(gr.flag_updates(u[sl], v[sl]), ins)
+        orc.trace(True)
+        gr.trace(True)
+        orc.apply_batch(u[sl], v[sl], ins)
+        gr.apply_batch(u[sl], v[sl], ins)
+        _assert_same_trace(gr.trace_records(), orc.trace_records(), n)
+        assert np.array_equal(gr.get_mis(), orc.get_mis())
