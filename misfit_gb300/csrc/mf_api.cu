@@ -92,8 +92,11 @@ void release_all(mf_ctx* c) {
   c->heavy_bits.release();
   c->fpos.release();
   c->dense_bits.release();
+  c->n2cache.release();
+  c->n2stamp.release();
   for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();
-  for (auto* b : {&c->un_idx, &c->un_v, &c->need, &c->needv}) b->release();
+  for (auto* b : {&c->un_idx, &c->un_v, &c->need, &c->needv, &c->live_i, &c->live_v, &c->nlist_need}) b->release();
+  c->nmark.release();
   c->un_cnt.release();
   c->lb_offs.release();
   for (auto* b : {&c->big_pos, &c->big_off, &c->big_nr, &c->big_chunks, &c->big_pre}) b->release();

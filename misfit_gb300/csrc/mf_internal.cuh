@@ -413,9 +413,13 @@ struct mf_ctx {
   mf::DBuf<uint32_t> heavy_bits;
   int64_t heavy_cap = 0, heavy_used = 0;
   mf::DBuf<uint32_t> dense_bits;      // per dense seed bitmaps (exact sizes)
+  mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
+  mf::DBuf<uint32_t> n2stamp;          // batch stamp of each cached size
+  uint32_t n2batch = 0;
   mf::DBuf<int32_t> dense_idx, dense_hl, pair_d, pair_h, todo;
   mf::DBuf<unsigned long long> fpos;   // first-hit positions
-  mf::DBuf<int32_t> un_idx, un_v, need, needv;
+  mf::DBuf<int32_t> un_idx, un_v, need, needv, live_i, live_v, nlist_need;
+  mf::DBuf<uint32_t> nmark;            // epoch marks: neighbours of seeds needing their hop-2 part
   mf::DBuf<int64_t> un_cnt;
   mf::DBuf<int64_t> counters;   // device counters
   int64_t* h_counters = nullptr;  // pinned mirror

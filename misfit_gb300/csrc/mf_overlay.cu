@@ -372,6 +372,8 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   c->bval.reserve(n);
   c->wval.reserve(n);
   c->f1.reserve(n);
+  c->nmark.reserve(n);
+  c->nlist_need.reserve(n);
   c->touched.reserve(n);
   c->hlist.reserve(n);
   c->acnt_new.reserve(n);
@@ -384,6 +386,7 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   MF_CUDA(cudaMemsetAsync(c->hmark.p, 0, sizeof(uint32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->bval.p, 0, sizeof(uint32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->wval.p, 0, sizeof(uint32_t) * (size_t)n, s));
+  MF_CUDA(cudaMemsetAsync(c->nmark.p, 0, sizeof(uint32_t) * (size_t)n, s));
   c->a_total = 0;
   c->epoch = 0;
   c->counters.reserve(64);

@@ -184,17 +184,44 @@ __global__ void k_lb_bound(GraphView g, const int32_t* seeds, const int64_t* off
 }
 
 __global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct,
-                               const unsigned long long* uacc, unsigned long long* out) {
+                               const unsigned long long* uacc, const int64_t* n2cache, const uint32_t* n2stamp,
+                               uint32_t stamp, unsigned long long* out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long b = 0;
   if (i < ns) {
-    b = 1ull + (unsigned long long)row_len(g, seeds[i]) + uacc[i];
-    if (b > (unsigned long long)g.n) b = (unsigned long long)g.n;
+    const int32_t s = seeds[i];
+    if (n2stamp[s] == stamp) {
+      b = (unsigned long long)n2cache[s];   // exact size known from an earlier sub-batch
+    } else {
+      b = 1ull + (unsigned long long)row_len(g, s) + uacc[i];
+      if (b > (unsigned long long)g.n) b = (unsigned long long)g.n;
+    }
   } else if (i < ns + nct) {
     b = (unsigned long long)row_len(g, cands[i - ns]);
   }
   for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xffffffffu, b, o);
   if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, b);
+}
+
+// Seeds whose exact size is cached for this batch take it; the others are
+// listed for computation.
+__global__ void k_exact_todo(const int32_t* seeds, int64_t ns, const int64_t* n2cache, const uint32_t* n2stamp,
+                             uint32_t stamp, int64_t* lens, int32_t* todo, unsigned long long* cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  const int32_t s = seeds[i];
+  if (n2stamp[s] == stamp) lens[i] = n2cache[s];
+  else todo[atomicAdd(cnt, 1ull)] = (int32_t)i;
+}
+
+__global__ void k_exact_store(const int32_t* seeds, const int32_t* list, int64_t cnt, const int64_t* lens,
+                              int64_t* n2cache, uint32_t* n2stamp, uint32_t stamp) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= cnt) return;
+  const int64_t i = list[k];
+  const int32_t s = seeds[i];
+  n2cache[s] = lens[i];
+  n2stamp[s] = stamp;
 }
 
 // ---- exact 2-hop list sizes ------------------------------------------------------
@@ -404,10 +431,6 @@ __global__ void k_todo_retry(const int64_t* lens, const int32_t* todo, int64_t n
   if (t < ntodo && lens[todo[t]] == -2) out[atomicAdd(cnt, 1ull)] = todo[t];
 }
 
-__global__ void k_iota(int32_t* out, int64_t n) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (int32_t)i;
-}
 
 __global__ void k_cand_lens(GraphView g, const int32_t* cands, int64_t nct, int64_t* lens) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -452,10 +475,6 @@ constexpr unsigned long long kNoPos = ~0ull;
 struct HasCid {   // the element already carries a cluster id
   const int32_t* cid;
   __device__ __forceinline__ bool operator()(int32_t y) const { return cid[y] != -1; }
-};
-struct HasF1 {    // the element's own row holds an element with a cluster id
-  const int32_t* f1;
-  __device__ __forceinline__ bool operator()(int32_t y) const { return f1[y] != -1; }
 };
 
 template <class P>
@@ -504,7 +523,56 @@ __global__ void k_first_rest(GraphView g, const int32_t* unres_idx, const int32_
   });
 }
 
-// f1[x] = cluster id of the first element of row(x) that has one, or -1.
+// Per row: early return when the row's own vertex already has an id
+// (src/misfit/misfit.cu:224); the other rows are listed (row index and
+// vertex) for the first-existing-id searches.
+__global__ void k_row_skip(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, const int32_t* cid,
+                           int32_t* rowcid, uint8_t* creates, int32_t* live_i, int32_t* live_v,
+                           unsigned long long* nlive) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns + nct) return;
+  const int32_t x = i < ns ? seeds[i] : cands[i - ns];
+  if (cid[x] != -1) {
+    rowcid[i] = kSkip;
+    creates[i] = 0;
+    return;
+  }
+  const unsigned long long k = atomicAdd(nlive, 1ull);
+  live_i[k] = (int32_t)i;
+  live_v[k] = x;
+}
+
+// The first existing id of row(x) in order, if any; seeds without one go on
+// to their hop-2 part (`need`), everything else without one creates a cluster.
+__global__ void k_live_decide(GraphView g, const int32_t* live_i, const int32_t* live_v, int64_t cnt, int64_t ns,
+                              const unsigned long long* firstpos, const int32_t* cid, int32_t* rowcid,
+                              uint8_t* creates, int32_t* need, unsigned long long* nneed) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= cnt) return;
+  const int32_t i = live_i[k];
+  const int32_t x = live_v[k];
+  const unsigned long long fp = firstpos[k];
+  if (fp != kNoPos) {
+    rowcid[i] = cid[row_elem(g, x, (int64_t)fp, g.nindex[x + 1] - g.nindex[x])];
+    creates[i] = 0;
+    return;
+  }
+  rowcid[i] = -1;
+  creates[i] = 1;
+  if (i < ns) need[atomicAdd(nneed, 1ull)] = i;
+}
+
+// A seed row is [s] ++ row(s) ++ row(h1) ++ row(h2) ++ ... (h over row(s) in
+// order): after row(s), its first existing id is f1(h) of the first h of
+// row(s) that has one, f1(h) being the id of the first element of row(h)
+// with an id.  f1 is computed for the neighbours of the seeds that need it.
+__global__ void k_lb_mark_need(GraphView g, const int32_t* needv, const int64_t* offs, int64_t cnt, uint32_t epoch,
+                               uint32_t* nmark, int32_t* list, unsigned long long* count) {
+  lb_rows(g, needv, offs, cnt, [&](int64_t, int32_t, int32_t y) {
+    if (nmark[y] != epoch && atomicExch(nmark + y, epoch) != epoch) list[atomicAdd(count, 1ull)] = y;
+  });
+}
+
 __global__ void k_f1_finish(GraphView g, const int32_t* list, int64_t cnt, const unsigned long long* firstpos,
                             const int32_t* cid, int32_t* f1) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -514,37 +582,19 @@ __global__ void k_f1_finish(GraphView g, const int32_t* list, int64_t cnt, const
   f1[x] = fp == kNoPos ? -1 : cid[row_elem(g, x, (int64_t)fp, g.nindex[x + 1] - g.nindex[x])];
 }
 
-// Per row: early return when the row's own vertex already has an id
-// (src/misfit/misfit.cu:224), else the first existing id in row order or a
-// new one.  Candidates use f1(c); seeds scan [s] ++ row(s) ++ row(h)...,
-// i.e. f1(s), then f1(h) of the first h of row(s) that has one: those seeds
-// are listed in `need` for a first-hit search with HasF1.
-__global__ void k_row_decide_a(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, const int32_t* cid,
-                               const int32_t* f1, int32_t* rowcid, uint8_t* creates, int32_t* need,
-                               unsigned long long* nneed) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ns + nct) return;
-  const bool seed = i < ns;
-  const int32_t x = seed ? seeds[i] : cands[i - ns];
-  if (cid[x] != -1) {
-    rowcid[i] = kSkip;
-    creates[i] = 0;
-    return;
-  }
-  const int32_t fe = f1[x];
-  rowcid[i] = fe;
-  creates[i] = fe == -1 ? 1 : 0;
-  if (fe == -1 && seed) need[atomicAdd(nneed, 1ull)] = (int32_t)i;
-}
+struct HasF1 {    // the element's own row holds an element with a cluster id
+  const int32_t* f1;
+  __device__ __forceinline__ bool operator()(int32_t y) const { return f1[y] != -1; }
+};
 
 __global__ void k_need_vertices(const int32_t* need, int64_t cnt, const int32_t* seeds, int32_t* out) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < cnt) out[k] = seeds[need[k]];
 }
 
-__global__ void k_row_decide_b(GraphView g, const int32_t* need, const int32_t* needv, int64_t cnt,
-                               const unsigned long long* firstpos, const int32_t* f1, int32_t* rowcid,
-                               uint8_t* creates) {
+__global__ void k_need_decide(GraphView g, const int32_t* need, const int32_t* needv, int64_t cnt,
+                              const unsigned long long* firstpos, const int32_t* f1, int32_t* rowcid,
+                              uint8_t* creates) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= cnt) return;
   const unsigned long long fp = firstpos[k];
@@ -1407,11 +1457,20 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
   const int64_t pcap = std::max<int64_t>(4096, std::min<int64_t>((int64_t)1 << 26, 2 * c->nnz + 1));
   c->pair_d.reserve(pcap);
   c->pair_h.reserve(pcap);
-  c->todo.reserve(2 * ns);
-  MF_K(k_iota<<<grid_for(ns), kTB, 0, s>>>(c->todo.p, ns));
+  c->todo.reserve(3 * ns);
+  MF_CUDA(cudaMemsetAsync(c->counters.p + 44, 0, sizeof(int64_t), s));
+  MF_K(k_exact_todo<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, c->n2cache.p, c->n2stamp.p, c->n2batch,
+                                                 c->rowlens.p, c->todo.p,
+                                                 reinterpret_cast<unsigned long long*>(c->counters.p) + 44));
+  MF_CUDA(cudaMemcpyAsync(h + 44, c->counters.p + 44, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
+  const int64_t nnew = h[44];
+  int32_t* computed = c->todo.p + 2 * ns;   // the seeds computed here, for the cache
+  if (nnew > 0)
+    MF_CUDA(cudaMemcpyAsync(computed, c->todo.p, sizeof(int32_t) * (size_t)nnew, cudaMemcpyDeviceToDevice, s));
   int32_t* todo = c->todo.p;
   int32_t* todo_next = c->todo.p + ns;
-  int64_t ntodo = ns;
+  int64_t ntodo = nnew;
   unsigned long long* cnts = reinterpret_cast<unsigned long long*>(c->counters.p) + 40;
   while (ntodo > 0) {
     MF_CUDA(cudaMemsetAsync(cnts, 0, sizeof(unsigned long long) * 4, s));
@@ -1446,6 +1505,9 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
     std::swap(todo, todo_next);
     ntodo = left;
   }
+  if (nnew > 0)
+    MF_K(k_exact_store<<<grid_for(nnew), kTB, 0, s>>>(c->seeds.p, computed, nnew, c->rowlens.p, c->n2cache.p,
+                                                      c->n2stamp.p, c->n2batch));
   MF_CUDA(cudaGetLastError());
 }
 
@@ -1480,6 +1542,7 @@ void next_epoch(mf_ctx* c) {
     MF_CUDA(cudaMemsetAsync(c->hmark.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
     MF_CUDA(cudaMemsetAsync(c->bval.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
     MF_CUDA(cudaMemsetAsync(c->wval.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
+    MF_CUDA(cudaMemsetAsync(c->nmark.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
     c->epoch = 0;
   }
   ++c->epoch;
@@ -1631,6 +1694,14 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_K(k_heavy_reset<<<grid_for(c->heavy_used), kTB, 0, s>>>(c->heavy_list.p, c->heavy_used, c->heavy_slot.p));
     c->heavy_used = 0;
   }
+  // exact 2-hop sizes stay valid for the rows of this batch only
+  c->n2cache.reserve(std::max<int32_t>(n, 1));
+  c->n2stamp.reserve(std::max<int32_t>(n, 1));
+  if (c->n2batch == 0 || c->n2batch == 0xffffffffu) {
+    MF_CUDA(cudaMemsetAsync(c->n2stamp.p, 0, sizeof(uint32_t) * (size_t)std::max<int32_t>(n, 1), s));
+    c->n2batch = 0;
+  }
+  ++c->n2batch;
   const int64_t big = 2 * std::min<int64_t>(m, kMaxBatchEdges) + (int64_t)n + 2;
   c->i64a.reserve(big);
   c->i64b.reserve(big);
@@ -1693,7 +1764,8 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_CUDA(cudaMemsetAsync(c->uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), s));
     row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
     MF_K(k_lb_bound<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, c->uacc.p));
-    MF_K(k_bound_finish<<<grid_for(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->uacc.p, ucnt + 4));
+    MF_K(k_bound_finish<<<grid_for(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->uacc.p, c->n2cache.p,
+                                                        c->n2stamp.p, c->n2batch, ucnt + 4));
     MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     int64_t packed = -1;
@@ -1716,23 +1788,40 @@ void process_batch(mf_ctx* c, int64_t m) {
 
     // ---- clustering (bulk-synchronous)
     sc.emplace(c, kStFirst);
-    first_hits(c, c->seeds.p, ns, HasCid{c->cid.p});
-    MF_K(k_f1_finish<<<grid_for(ns), kTB, 0, s>>>(g, c->seeds.p, ns, c->fpos.p, c->cid.p, c->f1.p));
-    first_hits(c, c->hlist.p, nh, HasCid{c->cid.p});
-    MF_K(k_f1_finish<<<grid_for(nh), kTB, 0, s>>>(g, c->hlist.p, nh, c->fpos.p, c->cid.p, c->f1.p));
-    MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t), s));
+    c->live_i.reserve(std::max<int64_t>(rows, 1));
+    c->live_v.reserve(std::max<int64_t>(rows, 1));
     c->need.reserve(std::max<int64_t>(ns, 1));
-    c->needv.reserve(std::max<int64_t>(ns, 1));
-    MF_K(k_row_decide_a<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->f1.p,
-                                                        c->rowcid.p, c->creates.p, c->need.p, ucnt + 33));
+    MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t) * 2, s));
+    MF_K(k_row_skip<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->rowcid.p,
+                                                    c->creates.p, c->live_i.p, c->live_v.p, ucnt + 33));
     MF_CUDA(cudaMemcpyAsync(h + 33, cnt + 33, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
-    const int64_t nneed = h[33];
-    if (nneed > 0) {
-      MF_K(k_need_vertices<<<grid_for(nneed), kTB, 0, s>>>(c->need.p, nneed, c->seeds.p, c->needv.p));
-      first_hits(c, c->needv.p, nneed, HasF1{c->f1.p});
-      MF_K(k_row_decide_b<<<grid_for(nneed), kTB, 0, s>>>(g, c->need.p, c->needv.p, nneed, c->fpos.p, c->f1.p,
-                                                           c->rowcid.p, c->creates.p));
+    const int64_t nlive = h[33];
+    if (nlive > 0) {
+      first_hits(c, c->live_v.p, nlive, HasCid{c->cid.p});
+      MF_K(k_live_decide<<<grid_for(nlive), kTB, 0, s>>>(g, c->live_i.p, c->live_v.p, nlive, ns, c->fpos.p, c->cid.p,
+                                                          c->rowcid.p, c->creates.p, c->need.p, ucnt + 34));
+      MF_CUDA(cudaMemcpyAsync(h + 34, cnt + 34, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaStreamSynchronize(s));
+      const int64_t nneed = h[34];
+      if (nneed > 0) {
+        c->needv.reserve(nneed);
+        MF_K(k_need_vertices<<<grid_for(nneed), kTB, 0, s>>>(c->need.p, nneed, c->seeds.p, c->needv.p));
+        row_offsets(c, c->needv.p, nneed, kCntAll, ns, ep);
+        MF_CUDA(cudaMemsetAsync(cnt + 35, 0, sizeof(int64_t), s));
+        MF_K(k_lb_mark_need<<<lb_grid(c), kTB, 0, s>>>(g, c->needv.p, c->lb_offs.p, nneed, ep, c->nmark.p,
+                                                       c->nlist_need.p, ucnt + 35));
+        MF_CUDA(cudaMemcpyAsync(h + 35, cnt + 35, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        MF_CUDA(cudaStreamSynchronize(s));
+        const int64_t nn = h[35];
+        if (nn > 0) {
+          first_hits(c, c->nlist_need.p, nn, HasCid{c->cid.p});
+          MF_K(k_f1_finish<<<grid_for(nn), kTB, 0, s>>>(g, c->nlist_need.p, nn, c->fpos.p, c->cid.p, c->f1.p));
+          first_hits(c, c->needv.p, nneed, HasF1{c->f1.p});
+          MF_K(k_need_decide<<<grid_for(nneed), kTB, 0, s>>>(g, c->need.p, c->needv.p, nneed, c->fpos.p, c->f1.p,
+                                                              c->rowcid.p, c->creates.p));
+        }
+      }
     }
     scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
     MF_K(k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p));
