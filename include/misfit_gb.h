@@ -106,6 +106,34 @@ int mf_greedy_mis(mf_ctx* ctx, uint8_t* out, int64_t n);
  * for every batch before any batch is applied). */
 int mf_flag_updates(mf_ctx* ctx, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out);
 
+/* Largest m that mf_flag_updates_noalloc accepts. */
+#define MF_NOALLOC_MAX_UPDATES 65536
+
+/* mf_flag_updates for callers that must not allocate device memory.  This
+ * entry point has no counterpart in the reference.
+ * mf_flag_updates stages the endpoints in per-context device buffers that
+ * grow to the largest batch seen, and growing one means a cudaFree plus a
+ * cudaMalloc.  Two kinds of caller cannot accept that:
+ *   - a process that has committed the device's memory to its graphs and
+ *     overlays, where a growth can fail with MF_ENOMEM part way through a
+ *     stream of batches;
+ *   - a process with work in flight on other streams of the device, which
+ *     the cudaFree waits for.
+ * This variant allocates nothing.  Its scratch is one fixed device array of
+ * 590,080 bytes (room for MF_NOALLOC_MAX_UPDATES pairs and their flags).
+ *   - The first call on a device finds the array's address once
+ *     (cudaGetSymbolAddress).  Make that first call, which may have
+ *     m = 0, before any stream capture.
+ *   - m > MF_NOALLOC_MAX_UPDATES returns MF_ELIMIT and does nothing.
+ *   - Each call zeroes the array's invalid-pair counter itself.
+ *   - Invalid endpoints return MF_EINVAL without writing ins_out, as in
+ *     mf_flag_updates.
+ *   - All contexts on one device share the array.  Calls that overlap in
+ *     time, from several host threads or on several contexts of one
+ *     device, race on it: the caller must serialise them.
+ * The flags are the same as those of mf_flag_updates on the same graph. */
+int mf_flag_updates_noalloc(mf_ctx* ctx, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out);
+
 /* Process one batch: conditional overlay insert/delete in file order, the
  * sub-batch split, 2-hop neighbourhoods, clustering and MIS repair.
  * Replaces processBatchGPUVertexClustering (src/misfit/misfit.cu:704-730)

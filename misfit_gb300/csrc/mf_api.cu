@@ -481,6 +481,14 @@ int mf_flag_updates(mf_ctx* c, const int32_t* u, const int32_t* v, int64_t m, ui
   });
 }
 
+int mf_flag_updates_noalloc(mf_ctx* c, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out) {
+  return guarded([&] {
+    need(c && m >= 0 && (m == 0 || (u && v && ins_out)), MF_EINVAL, "bad arguments");
+    bind(c);
+    mf::flag_updates_noalloc(c, u, v, m, ins_out);
+  });
+}
+
 int mf_apply_batch(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
   return guarded([&] {
     need(c && m >= 0 && (m == 0 || (u && v && ins)), MF_EINVAL, "bad arguments");

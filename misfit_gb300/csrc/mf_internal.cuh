@@ -484,6 +484,8 @@ struct StageScope {
 void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nlist, int64_t nnz);
 void apply_overlay(mf_ctx* c, int64_t m);          // uses c->bu/bv/bins
 void flag_updates(mf_ctx* c, int64_t m);           // c->bu/bv -> c->bins
+// host u/v -> host ins_out through a fixed device array; m <= MF_NOALLOC_MAX_UPDATES
+void flag_updates_noalloc(mf_ctx* c, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out);
 void compact_graph(mf_ctx* c, std::vector<int64_t>& nindex_out, std::vector<int32_t>& nlist_out);
 void rebase(mf_ctx* c);
 void greedy_mis(mf_ctx* c, uint8_t* d_out);

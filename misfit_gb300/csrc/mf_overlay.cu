@@ -14,6 +14,7 @@
 // three-state machine none / added / tombstoned that insertEdge, removeEdge,
 // un_tombstone and forget_delta_edge implement, core/FlashGraph.h:196-275).
 #include <algorithm>
+#include <mutex>
 
 #include "mf_internal.cuh"
 
@@ -254,6 +255,27 @@ __global__ void k_flags(GraphView g, bool sorted, const int32_t* u, const int32_
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const int32_t x = u[i], y = v[i];
+  bool adj = added_find(g, x, y) >= 0;
+  if (!adj) {
+    int32_t l, d;
+    base_copies(g, sorted, x, y, &l, &d);
+    adj = l > 0;
+  }
+  ins[i] = adj ? 0 : 1;
+}
+
+// k_flags with the endpoint check folded in, for flag_updates_noalloc: a pair
+// with an endpoint outside [0, n) or u == v is counted into *bad and gets no
+// flag (the host then reports the batch as invalid and copies nothing out).
+__global__ void k_flags_checked(GraphView g, bool sorted, const int32_t* u, const int32_t* v, int64_t m,
+                                uint8_t* ins, unsigned long long* bad) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int32_t x = u[i], y = v[i];
+  if (x < 0 || x >= g.n || y < 0 || y >= g.n || x == y) {
+    atomicAdd(bad, 1ull);
+    return;
+  }
   bool adj = added_find(g, x, y) >= 0;
   if (!adj) {
     int32_t l, d;
@@ -575,6 +597,78 @@ void rebase(mf_ctx* c) {
   MF_CUDA(cudaStreamSynchronize(s));
   mis_keep.release();
   cid_keep.release();
+}
+
+}  // namespace mf
+
+// ---- update flags without allocation ------------------------------------------
+// mf_flag_updates stages the endpoints in the context's buffers, which grow
+// to the largest batch seen (cudaFree of the old buffer + cudaMalloc).  This
+// variant stages them in one fixed device array instead, so that it never
+// allocates: every call on a device uses the same array, found once per
+// device with cudaGetSymbolAddress.
+//
+// Layout of the array (byte offsets, each part 256-byte aligned):
+//   [0, 256)                     invalid-pair counter (u64; zeroed every call)
+//   [256, 256 + 4K)              u endpoints (int32, K = MF_NOALLOC_MAX_UPDATES)
+//   [256 + 4K, 256 + 8K)         v endpoints
+//   [256 + 8K, 256 + 9K)         flags (u8)
+// K = 65536 gives 590,080 bytes.
+namespace {
+constexpr size_t kNaCounterBytes = 256;
+constexpr size_t kNaEndpointBytes = sizeof(int32_t) * (size_t)MF_NOALLOC_MAX_UPDATES;
+constexpr size_t kNaScratchBytes = kNaCounterBytes + 2 * kNaEndpointBytes + (size_t)MF_NOALLOC_MAX_UPDATES;
+constexpr int kNaMaxDevices = 64;
+static_assert(kNaEndpointBytes % 256 == 0, "each part of the scratch starts on a 256-byte boundary");
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaScratchBytes];
+
+namespace mf {
+namespace {
+
+std::mutex g_na_mutex;
+unsigned char* g_na_base[kNaMaxDevices] = {};
+
+// Device address of the scratch array on the current device (which must be
+// `device`).  The first call for a device looks it up; later calls read the
+// table.
+unsigned char* noalloc_scratch(int device) {
+  if (device < 0 || device >= kNaMaxDevices) MF_FAIL(MF_ELIMIT, "device id beyond the no-allocation table (64)");
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (g_na_base[device] == nullptr) {
+    void* p = nullptr;
+    MF_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    if (p == nullptr) MF_FAIL(MF_ECUDA, "cudaGetSymbolAddress returned a null scratch address");
+    g_na_base[device] = static_cast<unsigned char*>(p);
+  }
+  return g_na_base[device];
+}
+
+}  // namespace
+
+void flag_updates_noalloc(mf_ctx* c, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out) {
+  if (m > (int64_t)MF_NOALLOC_MAX_UPDATES)
+    MF_FAIL(MF_ELIMIT, "mf_flag_updates_noalloc takes at most 65536 updates per call");
+  unsigned char* base = noalloc_scratch(c->device);
+  if (m <= 0) return;
+  cudaStream_t s = c->stream;
+  auto* bad = reinterpret_cast<unsigned long long*>(base);
+  auto* du = reinterpret_cast<int32_t*>(base + kNaCounterBytes);
+  auto* dv = reinterpret_cast<int32_t*>(base + kNaCounterBytes + kNaEndpointBytes);
+  auto* dins = base + kNaCounterBytes + 2 * kNaEndpointBytes;
+  // the counter is the only part read before it is written
+  MF_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s));
+  MF_CUDA(cudaMemcpyAsync(du, u, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, s));
+  MF_CUDA(cudaMemcpyAsync(dv, v, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, s));
+  MF_K(k_flags_checked<<<grid_for(m), kTB, 0, s>>>(c->view(), c->rows_sorted, du, dv, m, dins, bad));
+  MF_CUDA(cudaGetLastError());
+  unsigned long long nbad = 0;
+  MF_CUDA(cudaMemcpyAsync(&nbad, bad, sizeof(nbad), cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
+  if (nbad != 0) MF_FAIL(MF_EINVAL, "update endpoints must be distinct vertex ids in [0, n)");
+  MF_CUDA(cudaMemcpyAsync(ins_out, dins, (size_t)m, cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace mf

@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libmisfit_gb.so")
 EXPORTS = [
     "mf_version", "mf_status_string", "mf_last_error", "mf_open_egr", "mf_open_csr", "mf_close",
     "mf_num_nodes", "mf_num_base_entries", "mf_set_mis", "mf_get_mis", "mf_mis_size", "mf_greedy_mis",
-    "mf_flag_updates", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_sync",
+    "mf_flag_updates", "mf_flag_updates_noalloc", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_sync",
     "mf_last_batch_stats", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
     "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_compact", "mf_read_mis_file",
     "mf_write_mis_file", "mf_read_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
@@ -46,6 +46,8 @@ class MisfitError(RuntimeError):
 
 _LIB = None
 
+NOALLOC_MAX_UPDATES = 65536  # MF_NOALLOC_MAX_UPDATES
+
 _P = C.c_void_p
 _I32P = C.POINTER(C.c_int32)
 _I64P = C.POINTER(C.c_int64)
@@ -73,6 +75,7 @@ def _lib():
         "mf_mis_size": (C.c_int, [_P, _I64P]),
         "mf_greedy_mis": (C.c_int, [_P, _U8P, C.c_int64]),
         "mf_flag_updates": (C.c_int, [_P, _I32P, _I32P, C.c_int64, _U8P]),
+        "mf_flag_updates_noalloc": (C.c_int, [_P, _I32P, _I32P, C.c_int64, _U8P]),
         "mf_apply_batch": (C.c_int, [_P, _I32P, _I32P, _U8P, C.c_int64]),
         "mf_apply_batch_device": (C.c_int, [_P, _P, _P, _P, C.c_int64]),
         "mf_apply_batch_async": (C.c_int, [_P, _I32P, _I32P, _U8P, C.c_int64]),
@@ -194,6 +197,14 @@ class Graph:
         out = np.zeros(u.size, dtype=np.uint8)
         _check(_lib().mf_flag_updates(self._h, _ptr(u, C.c_int32), _ptr(v, C.c_int32), u.size,
                                       _ptr(out, C.c_uint8)), "mf_flag_updates")
+        return out
+
+    def flag_updates_noalloc(self, u, v):
+        """mf_flag_updates_noalloc: at most NOALLOC_MAX_UPDATES pairs, no device allocation."""
+        u, v = _i32(u), _i32(v)
+        out = np.zeros(u.size, dtype=np.uint8)
+        _check(_lib().mf_flag_updates_noalloc(self._h, _ptr(u, C.c_int32), _ptr(v, C.c_int32), u.size,
+                                              _ptr(out, C.c_uint8)), "mf_flag_updates_noalloc")
         return out
 
     def apply_batch(self, u, v, ins):
