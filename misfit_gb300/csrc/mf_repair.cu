@@ -19,6 +19,7 @@
 //   highest row writes last); assignment by ascending sub-batch index (lists
 //   walked descending); clusters processed in ascending id.
 #include <algorithm>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <optional>
@@ -1007,20 +1008,6 @@ __device__ __forceinline__ bool spec_seed(const SpecArgs& a, int32_t x) {
   return i >= 0 && (int64_t)i < a.ns;
 }
 
-__device__ bool t_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t except) {
-  auto hit = [&](int32_t z) { return z != except && mem(z) != 0; };
-  if (!spec_seed(a, x)) return thread_row_until(a.g, x, hit);
-  if (hit(x)) return true;
-  if (thread_row_until(a.g, x, hit)) return true;
-  return thread_row_until(a.g, x, [&](int32_t h) { return thread_row_until(a.g, h, hit); });
-}
-
-__device__ bool t_eligible(const SpecArgs& a, const Member& mem, int32_t w) {
-  if (mem(w)) return false;
-  if (a.v2i[w] < 0) return false;
-  return !t_any(a, mem, w, -1);
-}
-
 // Warp: does row-of(x) hold a member other than `except`?
 __device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t except) {
   const GraphView& g = a.g;
@@ -1189,14 +1176,14 @@ __global__ void k_spec_eval(SpecArgs a) {
   }
 }
 
-constexpr int64_t kBigChunk = 2048;
+constexpr int kBigChunk = 256;  // positions per chunk = threads per block of k_big_scan
 
 // Chunk prefix over the deferred edges (one block): chunk_pre[i] = first chunk
 // of deferred edge i, chunk_pre[nbig] = total; best[i] = none.
 __global__ void k_big_prep(SpecArgs a, int64_t* chunk_pre, unsigned long long* best, unsigned long long* queue) {
   const int64_t nbig = (int64_t)*a.big_count;
   __shared__ int64_t s_carry;
-  if (threadIdx.x == 0) { s_carry = 0; *queue = 0; }
+  if (threadIdx.x == 0) { s_carry = 0; queue[0] = 0; queue[1] = 0; }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __shared__ int64_t s_w[32];
@@ -1229,14 +1216,27 @@ __global__ void k_big_prep(SpecArgs a, int64_t* chunk_pre, unsigned long long* b
 }
 
 // Grid-wide first-eligible search over the flattened hop-2 sequences of the
-// deferred edges; chunks are handed out in increasing position order.
-__global__ void __launch_bounds__(256) k_big_scan(SpecArgs a, const int64_t* chunk_pre, unsigned long long* best,
-                                                  unsigned long long* queue) {
+// deferred edges; chunks of kBigChunk positions (one per thread) are handed
+// out in increasing position order.  The row index of each position comes
+// from a binary search in a shared copy of the prefix entries that cover the
+// chunk (one global search per chunk).  Each thread checks its element with a
+// bounded serial scan (64 reads); elements that scan leaves undecided (a long
+// row-of without an early member) are settled afterwards by whole warps, so
+// that no single thread walks a hub row alone.  The chunk's answer is the
+// smallest eligible position.
+__global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_t* chunk_pre,
+                                                        unsigned long long* best, unsigned long long* queue) {
   const GraphView& g = a.g;
   const int64_t nbig = (int64_t)*a.big_count;
   const int64_t total = chunk_pre[nbig];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __shared__ unsigned long long s_chunk;
   __shared__ unsigned long long s_best;
+  __shared__ int s_live, s_nu;
+  __shared__ int64_t s_k0;
+  __shared__ int64_t s_pre[kBigChunk + 1];
+  __shared__ int64_t s_uq[kBigChunk];
+  __shared__ int32_t s_uz[kBigChunk];
   while (true) {
     if (threadIdx.x == 0) s_chunk = atomicAdd(queue, 1ull);
     __syncthreads();
@@ -1253,21 +1253,72 @@ __global__ void __launch_bounds__(256) k_big_scan(SpecArgs a, const int64_t* chu
     const int64_t nr = a.big_nr[i];
     const int64_t vol = pre[nr];
     const int32_t r = a.big_r[i];
-    if (threadIdx.x == 0) s_best = ~0ull;
-    __syncthreads();
-    if ((unsigned long long)p0 < best[i]) {
-      Member mem{&a.view, (uint32_t)a.big_pos[i], r};
-      const int64_t rb = g.nindex[r + 1] - g.nindex[r];
-      for (int64_t q = p0 + threadIdx.x; q < p0 + kBigChunk && q < vol; q += blockDim.x) {
-        int64_t klo = 0, khi = nr;  // last k with pre[k] <= q
+    if (threadIdx.x == 0) {
+      s_best = ~0ull;
+      s_nu = 0;
+      s_live = (unsigned long long)p0 < best[i] ? 1 : 0;  // an earlier chunk may have answered already
+      if (s_live) {
+        atomicAdd(queue + 1, 1ull);                       // chunks scanned (the rest were skipped)
+        int64_t klo = 0, khi = nr;                        // last k with pre[k] <= p0
         while (khi - klo > 1) {
           const int64_t mid = (klo + khi) >> 1;
-          if (pre[mid] <= q) klo = mid; else khi = mid;
+          if (pre[mid] <= p0) klo = mid; else khi = mid;
         }
-        const int32_t h = row_elem(g, r, klo, rb);
-        if (h < 0) continue;
-        const int32_t z = row_elem(g, h, q - pre[klo], g.nindex[h + 1] - g.nindex[h]);
-        if (z >= 0 && t_eligible(a, mem, z)) atomicMin(&s_best, (unsigned long long)q);
+        s_k0 = klo;
+      }
+    }
+    __syncthreads();
+    if (s_live) {
+      // prefix entries k0 .. k0 + kBigChunk (clamped to nr); the positions of
+      // the chunk lie in rows k0 .. k0 + kBigChunk - 1 unless rows are empty
+      const int64_t k0 = s_k0;
+      const int64_t kn = min((int64_t)kBigChunk, nr - k0);
+      for (int64_t t = threadIdx.x; t <= kn; t += blockDim.x) s_pre[t] = pre[k0 + t];
+      __syncthreads();
+      const int64_t q = p0 + threadIdx.x;
+      if (q < vol) {
+        int64_t k;
+        if (q < s_pre[kn]) {
+          int lo2 = 0, hi2 = (int)kn;  // last t with s_pre[t] <= q
+          while (hi2 - lo2 > 1) {
+            const int mid = (lo2 + hi2) >> 1;
+            if (s_pre[mid] <= q) lo2 = mid; else hi2 = mid;
+          }
+          k = k0 + lo2;
+        } else {
+          int64_t klo = k0 + kn, khi = nr;  // beyond the shared window (empty rows): global search
+          while (khi - klo > 1) {
+            const int64_t mid = (klo + khi) >> 1;
+            if (pre[mid] <= q) klo = mid; else khi = mid;
+          }
+          k = klo;
+        }
+        Member mem{&a.view, (uint32_t)a.big_pos[i], r};
+        const int32_t h = row_elem(g, r, k, g.nindex[r + 1] - g.nindex[r]);
+        if (h >= 0) {
+          const int32_t z = row_elem(g, h, q - pre[k], g.nindex[h + 1] - g.nindex[h]);
+          if (z >= 0 && !mem(z) && a.v2i[z] >= 0) {
+            const int res = t_any_bounded(a, mem, z, -1, 64);
+            if (res == 0) {
+              atomicMin(&s_best, (unsigned long long)q);
+            } else if (res < 0) {
+              const int u = atomicAdd(&s_nu, 1);  // at most one entry per thread
+              s_uq[u] = q;
+              s_uz[u] = z;
+            }
+          }
+        }
+      }
+      __syncthreads();
+      const int nu = s_nu;
+      Member mem{&a.view, (uint32_t)a.big_pos[i], r};
+      for (int u = wid; u < nu; u += nw) {
+        const unsigned long long qq = (unsigned long long)s_uq[u];
+        unsigned long long cur = 0;
+        if (lane == 0) cur = atomicAdd(&s_best, 0ull);
+        cur = __shfl_sync(0xffffffffu, cur, 0);
+        if (qq >= cur) continue;  // a smaller eligible position is known
+        if (!w_any(a, mem, s_uz[u], -1) && lane == 0) atomicMin(&s_best, qq);
       }
     }
     __syncthreads();
@@ -1557,6 +1608,11 @@ int64_t big_threshold() {
   return v;
 }
 
+bool debug_counters() {
+  static const bool on = std::getenv("MISFIT_GB_DEBUG") != nullptr;
+  return on;
+}
+
 bool sequential_repair_forced() {
   static const bool forced = [] {
     const char* e = std::getenv("MISFIT_GB_REPAIR");
@@ -1604,6 +1660,7 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
   MF_CUDA(cudaMemsetAsync(c->rp_w1.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
   const int nbits = bits_for(std::max<int32_t>(c->n - 1, 1));
   int64_t p0 = 0, nview = 0, rounds = 0;
+  int64_t dbg_big = 0, dbg_chunks = 0, dbg_scanned = 0;
   std::optional<StageScope> rsc;
   rsc.emplace(c, kStRepair);
   while (p0 < nproc) {
@@ -1625,7 +1682,7 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     MF_K(k_spec_eval<<<warps_grid(pending), kTB, 0, s>>>(a));
     rsc.emplace(c, kStRepairBig);
     MF_K(k_big_prep<<<1, 1024, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
-    MF_K(k_big_scan<<<(unsigned)c->big_grid, 256, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
+    MF_K(k_big_scan<<<(unsigned)c->big_grid, kBigChunk, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
     MF_K(k_big_finalize<<<grid_for(pending), kTB, 0, s>>>(a, c->big_best.p));
     rsc.emplace(c, kStRepair);
     h[20] = (int64_t)nproc;
@@ -1643,6 +1700,15 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t f = h[20];          // first changed position, nproc when none
     const int64_t nk = h[21];
+    if (debug_counters()) {
+      unsigned long long q[4];
+      MF_CUDA(cudaMemcpy(q, c->counters.p + 24, sizeof(q), cudaMemcpyDeviceToHost));
+      int64_t tot = 0;
+      if (q[0] > 0) MF_CUDA(cudaMemcpy(&tot, c->big_chunks.p + q[0], sizeof(tot), cudaMemcpyDeviceToHost));
+      dbg_big += (int64_t)q[0];
+      dbg_chunks += tot;
+      dbg_scanned += (int64_t)q[3];
+    }
     radix_sort_pairs(c->rp_keys2.p, c->rp_vals2.p, nk, 32 + nbits, c->ws, s);
     if (nview > 0) MF_K(k_spec_clear_flags<<<grid_for(nview), kTB, 0, s>>>(c->rp_keys.p, nview, c->mis.p));
     const uint64_t last = (uint64_t)std::min<int64_t>(f, nproc - 1);
@@ -1663,6 +1729,10 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     p0 = f + 1;
   }
   MF_CUDA(cudaGetLastError());
+  if (debug_counters() && dbg_scanned > 0)
+    std::fprintf(stderr, "[misfit_gb] repair: nproc %lld rounds %lld deferred %lld chunks %lld scanned %lld\n",
+                 (long long)nproc, (long long)rounds, (long long)dbg_big, (long long)dbg_chunks,
+                 (long long)dbg_scanned);
   return rounds;
 }
 
