@@ -5,6 +5,9 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <chrono>
+#include <map>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -24,6 +27,59 @@ thread_local std::string g_error;
 }
 
 std::atomic<long long> g_launches{0};
+
+namespace {
+struct KTimes {
+  std::mutex mu;
+  std::map<std::string, std::pair<long long, double>> by_name;
+  ~KTimes() {
+    if (by_name.empty()) return;
+    std::vector<std::pair<double, std::string>> rows;
+    double total = 0.0;
+    for (const auto& kv : by_name) {
+      rows.emplace_back(kv.second.second, kv.first);
+      total += kv.second.second;
+    }
+    std::sort(rows.rbegin(), rows.rend());
+    std::fprintf(stderr, "[misfit_gb] per-kernel host-timed ms (synchronised launches), total %.3f\n", total);
+    for (const auto& r : rows)
+      std::fprintf(stderr, "  %-28s %9lld %12.3f %6.1f%%\n", r.second.c_str(), by_name[r.second].first, r.first,
+                   total > 0 ? 100.0 * r.first / total : 0.0);
+  }
+};
+KTimes g_ktimes;
+
+double ktime_now() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+bool ktime_on() {
+  static const bool on = [] {
+    const char* e = std::getenv("MISFIT_GB_KTIME");
+    return e != nullptr && std::strcmp(e, "1") == 0;
+  }();
+  return on;
+}
+
+double ktime_begin() {
+  cudaDeviceSynchronize();
+  return ktime_now();
+}
+
+void ktime_end(const char* launch_text, double t0) {
+  cudaDeviceSynchronize();
+  const double dt = ktime_now() - t0;
+  std::string name(launch_text);
+  const size_t cut = name.find("<<<");
+  if (cut != std::string::npos) name.resize(cut);
+  while (!name.empty() && (name.back() == ' ' || name.back() == '\n')) name.pop_back();
+  std::lock_guard<std::mutex> lock(g_ktimes.mu);
+  auto& e = g_ktimes.by_name[name];
+  e.first += 1;
+  e.second += dt;
+}
+
 const char* const kStageNames[kStCount] = {"overlay", "split",  "seeds", "hop1",  "sizes", "cluster_read",
                                            "cluster_write", "assign", "repair", "clear", "exact", "repair_big"};
 
@@ -92,6 +148,9 @@ void release_all(mf_ctx* c) {
   c->heavy_bits.release();
   c->fpos.release();
   c->dense_bits.release();
+  c->dense_light.release();
+  c->pull_long.release();
+  c->ncbits.release();
   c->n2cache.release();
   c->n2stamp.release();
   for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();

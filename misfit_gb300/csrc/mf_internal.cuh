@@ -60,10 +60,21 @@ struct Failure {
 // launches can be reported (mf_kernel_launches).
 extern std::atomic<long long> g_launches;
 inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
-#define MF_K(...)            \
-  do {                       \
-    __VA_ARGS__;             \
-    ::mf::note_launch();     \
+// Per-kernel timing (MISFIT_GB_KTIME=1): the device is synchronised around
+// every launch and the host-timed milliseconds are summed per kernel name and
+// printed to stderr at exit.  Off by default; it slows everything down and is
+// only a breakdown tool.
+bool ktime_on();
+double ktime_begin();
+void ktime_end(const char* launch_text, double t0);
+
+#define MF_K(...)                                              \
+  do {                                                         \
+    const bool kt_ = ::mf::ktime_on();                         \
+    const double t_ = kt_ ? ::mf::ktime_begin() : 0.0;         \
+    __VA_ARGS__;                                               \
+    ::mf::note_launch();                                       \
+    if (kt_) ::mf::ktime_end(#__VA_ARGS__, t_);                \
   } while (0)
 
 // Stages timed by the optional profiler (mf_profile_enable).
@@ -413,6 +424,9 @@ struct mf_ctx {
   mf::DBuf<uint32_t> heavy_bits;
   int64_t heavy_cap = 0, heavy_used = 0;
   mf::DBuf<uint32_t> dense_bits;      // per dense seed bitmaps (exact sizes)
+  mf::DBuf<int64_t> dense_light;      // per dense seed light volume (size bound)
+  mf::DBuf<int32_t> pull_long;        // vertices with long rows for the warp pull pass
+  mf::DBuf<uint32_t> ncbits;          // non-skipped candidate bits for the pull pass
   mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
   mf::DBuf<uint32_t> n2stamp;          // batch stamp of each cached size
   uint32_t n2batch = 0;

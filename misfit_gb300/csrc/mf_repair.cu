@@ -19,10 +19,13 @@
 //   highest row writes last); assignment by ascending sub-batch index (lists
 //   walked descending); clusters processed in ascending id.
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <optional>
+#include <unordered_map>
 
 #include "mf_internal.cuh"
 
@@ -287,6 +290,7 @@ struct DenseOut {
   int32_t* pair_d;                // light members: dense index
   int32_t* pair_h;                // light members: vertex
   unsigned long long* npairs;
+  int64_t* dlight;                // dense index -> light volume (sum of |N[h]| over light members)
   int64_t dmax, hcap, pcap;
 };
 
@@ -297,26 +301,42 @@ __global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32
   uint32_t* P = privbm + (int64_t)blockIdx.x * words;
   __shared__ int32_t s_h[kMaxHeavyPerSeed];
   __shared__ int s_nh, s_over, s_d;
-  __shared__ unsigned long long s_light, s_lcount, s_cnt, s_pbase, s_pfill;
+  __shared__ unsigned long long s_light, s_lcount, s_acount, s_cnt, s_pbase, s_pfill;
   __shared__ int s_hoff;
   const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int64_t t = blockIdx.x; t < ntodo; t += gridDim.x) {
     const int64_t i = todo[t];
     const int32_t s = seeds[i];
-    if (threadIdx.x == 0) { s_nh = 0; s_over = 0; s_light = 0; s_lcount = 0; s_cnt = 0; s_pfill = 0; }
+    if (threadIdx.x == 0) { s_nh = 0; s_over = 0; s_light = 0; s_lcount = 0; s_acount = 0; s_cnt = 0; s_pfill = 0; }
     __syncthreads();
     const int64_t nb = g.nindex[s + 1] - g.nindex[s];
     const int64_t total = nb + (g.aoff[s + 1] - g.aoff[s]);
-    for (int64_t k = (int64_t)threadIdx.x - 1; k < total; k += blockDim.x) {
-      const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
-      if (h < 0) continue;
-      const int32_t sl = slot[h];
-      if (sl >= 0) {
-        const int idx = atomicAdd(&s_nh, 1);
-        if (idx < kMaxHeavyPerSeed) s_h[idx] = sl; else s_over = 1;
-      } else {
-        atomicAdd(&s_light, (unsigned long long)(row_len(g, h) + 1));
-        atomicAdd(&s_lcount, 1ull);
+    {
+      unsigned long long lsum = 0, lcnt = 0, acnt = 0;
+      for (int64_t k = (int64_t)threadIdx.x - 1; k < total; k += blockDim.x) {
+        const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
+        if (h < 0) continue;
+        ++acnt;
+        const int32_t sl = slot[h];
+        if (sl >= 0) {
+          const int idx = atomicAdd(&s_nh, 1);
+          if (idx < kMaxHeavyPerSeed) s_h[idx] = sl; else s_over = 1;
+        } else {
+          lsum += (unsigned long long)(row_len(g, h) + 1);
+          lcnt += 1;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+        lcnt += __shfl_xor_sync(0xffffffffu, lcnt, o);
+        acnt += __shfl_xor_sync(0xffffffffu, acnt, o);
+      }
+      if ((threadIdx.x & 31) == 0) {
+        if (lcnt) {
+          atomicAdd(&s_light, lsum);
+          atomicAdd(&s_lcount, lcnt);
+        }
+        if (acnt) atomicAdd(&s_acount, acnt);
       }
     }
     __syncthreads();
@@ -353,7 +373,9 @@ __global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32
       if (threadIdx.x == 0) lens[i] = (int64_t)s_cnt;
     } else {
       const int nh = over ? 0 : s_nh;
-      const unsigned long long lc = over ? (unsigned long long)(total + 1) : s_lcount;
+      // pair slots: one per member written below (all live members when the
+      // heavy list overflowed, else the light ones)
+      const unsigned long long lc = over ? s_acount : s_lcount;
       if (threadIdx.x == 0) {
         s_d = -1;
         const unsigned long long d = atomicAdd(o.ndense, 1ull);
@@ -366,6 +388,7 @@ __global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32
           o.dseed[d] = (int32_t)i;
           o.dhoff[d] = (int32_t)hoff;
           o.dnh[d] = nh;
+          o.dlight[d] = over ? (int64_t)g.n : (int64_t)s_light;
           lens[i] = 0;
         } else {
           if ((int64_t)d < o.dmax) o.dseed[d] = -1;   // index taken but unused
@@ -376,13 +399,26 @@ __global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32
       const int d = s_d;
       if (d >= 0) {
         for (int j = threadIdx.x; j < nh; j += blockDim.x) o.hlist[s_hoff + j] = s_h[j];
-        for (int64_t k = (int64_t)threadIdx.x - 1; k < total; k += blockDim.x) {
-          const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
-          if (h < 0) continue;
-          if (!over && slot[h] >= 0) continue;
-          const unsigned long long q = s_pbase + atomicAdd(&s_pfill, 1ull);
-          o.pair_d[q] = d;
-          o.pair_h[q] = h;
+        // one shared atomic per warp and round: the lanes with a light member
+        // take consecutive slots
+        const int lane = threadIdx.x & 31;
+        for (int64_t k0 = -1; k0 < total; k0 += blockDim.x) {
+          const int64_t k = k0 + threadIdx.x;
+          int32_t h = -1;
+          if (k < total) {
+            h = k < 0 ? s : row_elem(g, s, k, nb);
+            if (h >= 0 && !over && slot[h] >= 0) h = -1;
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, h >= 0);
+          if (m == 0) continue;
+          unsigned long long base = 0;
+          if (lane == 0) base = atomicAdd(&s_pfill, (unsigned long long)__popc(m));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (h >= 0) {
+            const unsigned long long q = s_pbase + base + __popc(m & ((1u << lane) - 1u));
+            o.pair_d[q] = d;
+            o.pair_h[q] = h;
+          }
         }
       }
     }
@@ -390,14 +426,20 @@ __global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32
   }
 }
 
-// Dense bitmaps: P_d = OR of the heavy members' cached bitmaps.
+// Dense bitmaps: P_d = OR of the heavy members' cached bitmaps.  Grid
+// (dense seeds, word tiles) with the seed index fastest, so that the seeds
+// sharing a heavy member read its tile while it is still in L2.
+constexpr int kDenseTile = 2048;  // words per block (256 threads x 8)
+
 __global__ void k_dense_or(int64_t nd, const int32_t* dseed, const int32_t* dhoff, const int32_t* dnh,
                            const int32_t* hlist, const uint32_t* hbits, int64_t words, uint32_t* dbits) {
-  const int64_t d = blockIdx.y;
+  const int64_t d = blockIdx.x;
   if (d >= nd) return;
   const int32_t nh = dseed[d] >= 0 ? dnh[d] : 0;
   const int32_t* hl = hlist + dhoff[d];
-  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t w0 = (int64_t)blockIdx.y * kDenseTile;
+  const int64_t w1 = min(words, w0 + kDenseTile);
+  for (int64_t w = w0 + threadIdx.x; w < w1; w += blockDim.x) {
     uint32_t v = 0;
     for (int j = 0; j < nh; ++j) v |= __ldg(hbits + (int64_t)hl[j] * words + w);
     dbits[d * words + w] = v;
@@ -417,13 +459,23 @@ __global__ void k_dense_light(GraphView g, const int32_t* pair_d, const int32_t*
 }
 
 __global__ void k_dense_pop(int64_t nd, const int32_t* dseed, int64_t words, const uint32_t* dbits, int64_t* lens) {
-  const int64_t d = blockIdx.y;
+  const int64_t d = blockIdx.x;
   if (d >= nd || dseed[d] < 0) return;
+  const int64_t w0 = (int64_t)blockIdx.y * kDenseTile;
+  const int64_t w1 = min(words, w0 + kDenseTile);
   unsigned long long c = 0;
-  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x)
-    c += __popc(dbits[d * words + w]);
+  for (int64_t w = w0 + threadIdx.x; w < w1; w += blockDim.x) c += __popc(dbits[d * words + w]);
   for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(reinterpret_cast<unsigned long long*>(lens + dseed[d]), c);
+}
+
+// Upper bound of a dense seed's 2-hop size without the light members' bits:
+// |union of the heavy N[h]| + sum of |N[h]| over the light members, at most n.
+__global__ void k_dense_bound(int64_t nd, const int32_t* dseed, const int64_t* dlight, int32_t n, int64_t* lens) {
+  const int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nd || dseed[d] < 0) return;
+  int64_t* l = lens + dseed[d];
+  *l = min((int64_t)n, *l + dlight[d]);
 }
 
 __global__ void k_todo_retry(const int64_t* lens, const int32_t* todo, int64_t ntodo, int32_t* out,
@@ -660,42 +712,122 @@ __global__ void k_lb_push_cand(GraphView g, const int32_t* cands, const int64_t*
 // candidate neighbour: the added part of row(y) is scanned, then the base
 // part from its end until the first such neighbour.  That tag dominates every
 // seed-row tag; without one, the pushed seed-row tag (wval) decides.
-__global__ void k_pull_cand(GraphView g, const int32_t* v2i, const int32_t* rowcid, int64_t ns, const uint32_t* wval,
-                            uint32_t epoch, int32_t* cid, unsigned long long* work) {
+// One thread per vertex; rows longer than kPullLong positions go to a list
+// that k_pull_cand_long finishes with one warp per row.
+constexpr int64_t kPullLong = 2048;
+
+struct PullArgs {
+  GraphView g;
+  const int32_t* v2i;
+  const int32_t* rowcid;
+  const uint32_t* ncbits;         // bit c set <=> c is a non-skipped candidate
+  int64_t ns;
+  const uint32_t* wval;
+  uint32_t epoch;
+  int32_t* cid;
+  int32_t* longv;                 // rows left for the warp pass
+  unsigned long long* nlong;
+  unsigned long long* work;
+};
+
+__device__ __forceinline__ bool pull_nonskip(const PullArgs& a, int32_t c) {
+  return (__ldg(a.ncbits + (c >> 5)) >> (c & 31)) & 1u;
+}
+
+// Bits of the non-skipped candidates (rows ns .. ns+nct-1) for the pull pass.
+__global__ void k_cand_bits(const int32_t* cands, int64_t nct, int64_t ns, const int32_t* rowcid, uint32_t* bits) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nct || rowcid[ns + i] == kSkip) return;
+  const int32_t c = cands[i];
+  atomicOr(bits + (c >> 5), 1u << (c & 31));
+}
+
+__device__ __forceinline__ void pull_finish(const PullArgs& a, int32_t y, int32_t best) {
+  if (best >= 0) {
+    a.cid[y] = a.rowcid[a.v2i[best]];
+  } else {
+    const uint32_t t = a.wval[y];
+    if ((t >> kRowBits) == a.epoch) a.cid[y] = a.rowcid[t & kRowMask];
+  }
+}
+
+__global__ void k_pull_cand(PullArgs a) {
+  const GraphView& g = a.g;
   const int64_t yi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t visited = 0;
   if (yi < g.n) {
     const int32_t y = (int32_t)yi;
-    auto nonskip = [&](int32_t c) {
-      const int32_t vi = v2i[c];
-      return (int64_t)vi >= ns && rowcid[vi] != kSkip;
-    };
-    int32_t best = -1;
-    for (int64_t k = g.aoff[y]; k < g.aoff[y + 1]; ++k) {
-      const int32_t c = g.aadj[k];
-      ++visited;
-      if (c > best && nonskip(c)) best = c;
-    }
     const int64_t b = g.nindex[y], e = g.nindex[y + 1];
-    const bool filt = g.dead[y] != 0;
-    for (int64_t k = e - 1; k >= b; --k) {
-      const int32_t c = __ldg(g.nlist + k);
-      ++visited;
-      if (c <= best) break;
-      if (filt && !live_at(g.live, k)) continue;
-      if (nonskip(c)) {
-        best = c;
-        break;
-      }
-    }
-    if (best >= 0) {
-      cid[y] = rowcid[v2i[best]];
+    const int64_t ab = g.aoff[y], ae = g.aoff[y + 1];
+    if ((e - b) + (ae - ab) > kPullLong) {
+      a.longv[atomicAdd(a.nlong, 1ull)] = y;
     } else {
-      const uint32_t t = wval[y];
-      if ((t >> kRowBits) == epoch) cid[y] = rowcid[t & kRowMask];
+      int32_t best = -1;
+      for (int64_t k = ab; k < ae; ++k) {
+        const int32_t c = g.aadj[k];
+        ++visited;
+        if (c > best && pull_nonskip(a, c)) best = c;
+      }
+      const bool filt = g.dead[y] != 0;
+      for (int64_t k = e - 1; k >= b; --k) {
+        const int32_t c = __ldg(g.nlist + k);
+        ++visited;
+        if (c <= best) break;
+        if (filt && !live_at(g.live, k)) continue;
+        if (pull_nonskip(a, c)) {
+          best = c;
+          break;
+        }
+      }
+      pull_finish(a, y, best);
     }
   }
-  add_work(work, visited);
+  add_work(a.work, visited);
+}
+
+// The long rows: the warp takes the maximum over the added part, then walks
+// the sorted base part from its end 32 positions at a time.  Scanning from
+// the end, the positions with c > best form a prefix of the lanes; the
+// first of them (lowest lane) that is live and non-skipped is the answer,
+// and a prefix shorter than 32 lanes ends the walk.
+__global__ void k_pull_cand_long(PullArgs a) {
+  const GraphView& g = a.g;
+  const int lane = threadIdx.x & 31;
+  const int64_t nl = (int64_t)*a.nlong;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int64_t visited = 0;
+  for (int64_t w = warp_id(); w < nl; w += nw) {
+    const int32_t y = a.longv[w];
+    const int64_t b = g.nindex[y], e = g.nindex[y + 1];
+    const int64_t ab = g.aoff[y], ae = g.aoff[y + 1];
+    int32_t best = -1;
+    for (int64_t k = ab + lane; k < ae; k += 32) {
+      const int32_t c = g.aadj[k];
+      ++visited;
+      if (c > best && pull_nonskip(a, c)) best = c;
+    }
+    for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    const bool filt = g.dead[y] != 0;
+    for (int64_t k0 = e - 1; k0 >= b; k0 -= 32) {
+      const int64_t k = k0 - lane;
+      int32_t c = -1;
+      bool above = false, hit = false;
+      if (k >= b) {
+        c = __ldg(g.nlist + k);
+        ++visited;
+        above = c > best;
+        hit = above && (!filt || live_at(g.live, k)) && pull_nonskip(a, c);
+      }
+      const unsigned hm = __ballot_sync(0xffffffffu, hit);
+      if (hm) {
+        best = __shfl_sync(0xffffffffu, c, __ffs(hm) - 1);
+        break;
+      }
+      if (__ballot_sync(0xffffffffu, above) != 0xffffffffu) break;  // the rest is <= best
+    }
+    if (lane == 0) pull_finish(a, y, best);
+  }
+  add_work(a.work, visited);
 }
 
 // cid[y] = id of the row that wrote y last, for every y tagged this epoch.
@@ -1429,12 +1561,22 @@ std::vector<T> fetch(const T* d, int64_t cnt, cudaStream_t s) {
   return h;
 }
 
-unsigned lb_grid(mf_ctx* c) {
-  static int sms = 0;
-  if (sms == 0) {
-    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-  }
-  return (unsigned)(sms * 8);  // 8 CTAs of 256 threads per SM
+// Grid of a load-balanced (grid-stride) kernel: as many 256-thread CTAs as
+// can be resident at once, so that no CTA waits for a second wave.
+template <class K>
+unsigned lb_grid(mf_ctx* c, K kernel) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, unsigned> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const void* key = reinterpret_cast<const void*>(kernel);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int sms = 0, per = 0;
+  MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  MF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kTB, 0));
+  const unsigned g = (unsigned)(sms * std::max(per, 1));
+  cache.emplace(key, g);
+  return g;
 }
 
 // Row-position prefix of list[0..cnt) for lb_rows into c->lb_offs.
@@ -1448,8 +1590,19 @@ void row_offsets(mf_ctx* c, const int32_t* list, int64_t cnt, int kind, int64_t 
   scan_exclusive_i64(counts, c->lb_offs.p, cnt, c->ws, s);
 }
 
+double host_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+bool debug_counters() {
+  static const bool on = std::getenv("MISFIT_GB_DEBUG") != nullptr;
+  return on;
+}
+
 // Exact 2-hop list sizes of the seeds into c->rowlens[0..ns).
-void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
+// With bound_only, dense seeds get an upper bound (k_dense_bound) instead of
+// their exact size and nothing is cached.
+void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
   cudaStream_t s = c->stream;
   const int32_t n = c->n;
   const GraphView g = c->view();
@@ -1479,7 +1632,7 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
   h[30] = c->heavy_used;
   MF_CUDA(cudaMemcpyAsync(c->counters.p + 30, h + 30, sizeof(int64_t), cudaMemcpyHostToDevice, s));
   row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
-  MF_K(k_heavy_collect<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, thr, c->heavy_slot.p,
+  MF_K(k_heavy_collect<<<lb_grid(c, k_heavy_collect), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, thr, c->heavy_slot.p,
                                                   c->heavy_list.p,
                                                   reinterpret_cast<unsigned long long*>(c->counters.p) + 30));
   MF_CUDA(cudaMemcpyAsync(h + 30, c->counters.p + 30, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -1494,7 +1647,7 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
       MF_CUDA(cudaMemsetAsync(c->heavy_bits.p + from * words, 0,
                               sizeof(uint32_t) * (size_t)((build_to - from) * words), s));
       row_offsets(c, c->heavy_list.p + from, build_to - from, kCntAll, ns, ep);
-      MF_K(k_heavy_build<<<lb_grid(c), kTB, 0, s>>>(g, c->heavy_list.p + from, c->lb_offs.p, build_to - from, from,
+      MF_K(k_heavy_build<<<lb_grid(c, k_heavy_build), kTB, 0, s>>>(g, c->heavy_list.p + from, c->lb_offs.p, build_to - from, from,
                                                      words, c->heavy_bits.p));
     }
     c->heavy_used = total;
@@ -1504,6 +1657,7 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
   const int64_t dmax = std::max<int64_t>(1, std::min<int64_t>(ns, ((int64_t)1 << 30) / (words * 4)));
   c->dense_bits.reserve(dmax * words);
   c->dense_idx.reserve(3 * dmax);
+  c->dense_light.reserve(dmax);
   c->dense_hl.reserve(std::max<int64_t>(kMaxHeavyPerSeed, std::min<int64_t>(dmax * 64, (int64_t)1 << 22)));
   const int64_t pcap = std::max<int64_t>(4096, std::min<int64_t>((int64_t)1 << 26, 2 * c->nnz + 1));
   c->pair_d.reserve(pcap);
@@ -1526,25 +1680,33 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
   while (ntodo > 0) {
     MF_CUDA(cudaMemsetAsync(cnts, 0, sizeof(unsigned long long) * 4, s));
     DenseOut o{cnts + 0, c->dense_idx.p, c->dense_idx.p + dmax, c->dense_idx.p + 2 * dmax, c->dense_hl.p, cnts + 1,
-               c->pair_d.p, c->pair_h.p, cnts + 2, dmax, c->dense_hl.cap, pcap};
+               c->pair_d.p, c->pair_h.p, cnts + 2, c->dense_light.p, dmax, c->dense_hl.cap, pcap};
     MF_K(k_exact_classify<<<(unsigned)std::min<int64_t>(c->bitmap_ctas, ntodo), 512, 0, s>>>(
         g, c->seeds.p, todo, ntodo, c->heavy_slot.p, words, c->bitmaps.p, words / 8, c->rowlens.p, o));
     MF_CUDA(cudaMemcpyAsync(h + 40, c->counters.p + 40, sizeof(int64_t) * 3, cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t nd = std::min<int64_t>((int64_t)h[40], dmax);
     const int64_t np = std::min<int64_t>((int64_t)h[42], pcap);
+    const bool dbg = debug_counters();
+    double dbg_t0 = dbg ? host_ms() : 0.0;
     if (nd > 0) {
-      const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(64, (words + 1023) / 1024));
-      MF_K(k_dense_or<<<dim3(gx, (unsigned)nd), 256, 0, s>>>(nd, c->dense_idx.p, c->dense_idx.p + dmax,
-                                                            c->dense_idx.p + 2 * dmax, c->dense_hl.p,
-                                                            c->heavy_bits.p, words, c->dense_bits.p));
-      if (np > 0) {
+      const dim3 grid((unsigned)nd, (unsigned)((words + kDenseTile - 1) / kDenseTile));
+      MF_K(k_dense_or<<<grid, 256, 0, s>>>(nd, c->dense_idx.p, c->dense_idx.p + dmax, c->dense_idx.p + 2 * dmax,
+                                           c->dense_hl.p, c->heavy_bits.p, words, c->dense_bits.p));
+      if (np > 0 && !bound_only) {
         row_offsets(c, c->pair_h.p, np, kCntAll, ns, ep);
-        MF_K(k_dense_light<<<lb_grid(c), kTB, 0, s>>>(g, c->pair_d.p, c->pair_h.p, c->lb_offs.p, np, words,
+        MF_K(k_dense_light<<<lb_grid(c, k_dense_light), kTB, 0, s>>>(g, c->pair_d.p, c->pair_h.p, c->lb_offs.p, np, words,
                                                        c->dense_bits.p));
       }
-      MF_K(k_dense_pop<<<dim3(gx, (unsigned)nd), 256, 0, s>>>(nd, c->dense_idx.p, words, c->dense_bits.p,
-                                                             c->rowlens.p));
+      MF_K(k_dense_pop<<<grid, 256, 0, s>>>(nd, c->dense_idx.p, words, c->dense_bits.p, c->rowlens.p));
+      if (bound_only)
+        MF_K(k_dense_bound<<<grid_for(nd), kTB, 0, s>>>(nd, c->dense_idx.p, c->dense_light.p, n, c->rowlens.p));
+    }
+    if (dbg) {
+      MF_CUDA(cudaStreamSynchronize(s));
+      std::fprintf(stderr, "[misfit_gb] %s pass: seeds %lld dense %lld heavy-slots %lld light-pairs %lld "
+                   "dense-ms %.3f\n", bound_only ? "bound" : "exact", (long long)ntodo, (long long)nd,
+                   (long long)h[41], (long long)np, host_ms() - dbg_t0);
     }
     // seeds that did not fit this pass
     MF_CUDA(cudaMemsetAsync(cnts + 3, 0, sizeof(unsigned long long), s));
@@ -1556,7 +1718,7 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep) {
     std::swap(todo, todo_next);
     ntodo = left;
   }
-  if (nnew > 0)
+  if (nnew > 0 && !bound_only)
     MF_K(k_exact_store<<<grid_for(nnew), kTB, 0, s>>>(c->seeds.p, computed, nnew, c->rowlens.p, c->n2cache.p,
                                                       c->n2stamp.p, c->n2batch));
   MF_CUDA(cudaGetLastError());
@@ -1583,7 +1745,7 @@ void first_hits(mf_ctx* c, const int32_t* list, int64_t cnt, P pred) {
   if (un == 0) return;
   c->lb_offs.reserve(un + 1);
   scan_exclusive_i64(c->un_cnt.p, c->lb_offs.p, un, c->ws, s);
-  MF_K(k_first_rest<<<lb_grid(c), kTB, 0, s>>>(c->view(), c->un_idx.p, c->un_v.p, c->lb_offs.p, un, pred,
+  MF_K(k_first_rest<<<lb_grid(c, k_first_rest<P>), kTB, 0, s>>>(c->view(), c->un_idx.p, c->un_v.p, c->lb_offs.p, un, pred,
                                                c->fpos.p));
 }
 
@@ -1606,11 +1768,6 @@ int64_t big_threshold() {
     return e ? std::max<int64_t>(0, std::atoll(e)) : kBigThreshold;
   }();
   return v;
-}
-
-bool debug_counters() {
-  static const bool on = std::getenv("MISFIT_GB_DEBUG") != nullptr;
-  return on;
 }
 
 bool sequential_repair_forced() {
@@ -1813,7 +1970,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     next_epoch(c);
     const uint32_t ep = c->epoch;
     row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
-    MF_K(k_lb_mark_hop1<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->hmark.p,
+    MF_K(k_lb_mark_hop1<<<lb_grid(c, k_lb_mark_hop1), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->hmark.p,
                                                    c->work.p + 2 * kStHop1));
     scan_exclusive_marks(c->hmark.p, c->v2i.p, ep, c->i64a.p, n, c->ws, s);
     const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
@@ -1833,7 +1990,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     c->uacc.reserve(std::max<int64_t>(ns, 1));
     MF_CUDA(cudaMemsetAsync(c->uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), s));
     row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
-    MF_K(k_lb_bound<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, c->uacc.p));
+    MF_K(k_lb_bound<<<lb_grid(c, k_lb_bound), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, c->uacc.p));
     MF_K(k_bound_finish<<<grid_for(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->uacc.p, c->n2cache.p,
                                                         c->n2stamp.p, c->n2batch, ucnt + 4));
     MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -1841,18 +1998,27 @@ void process_batch(mf_ctx* c, int64_t m) {
     int64_t packed = -1;
     const bool exact = h[4] >= c->max_csr;
     if (exact) {
+      // The limit grows only if the packed total reaches it.  A tighter upper
+      // bound (exact sizes except for the light part of dense seeds) settles
+      // most of these sub-batches; the exact sizes follow only if it does not.
       sc.emplace(c, kStExact);
-      exact_sizes(c, ns, ep);
+      exact_sizes(c, ns, ep, true);
       MF_K(k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns));
       scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
-      h[5] = c->max_csr;
-      MF_CUDA(cudaMemcpyAsync(cnt + 5, h + 5, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-      MF_K(k_growth<<<1, 32, 0, s>>>(c->i64a.p, rows, cnt + 5));
-      MF_CUDA(cudaMemcpyAsync(h + 5, cnt + 5, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaMemcpyAsync(h + 6, c->i64a.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
       MF_CUDA(cudaStreamSynchronize(s));
-      c->max_csr = h[5];
-      packed = h[6];
-      c->stats.exact_sizes += 1;
+      if (h[6] >= c->max_csr) {
+        exact_sizes(c, ns, ep, false);
+        scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
+        h[5] = c->max_csr;
+        MF_CUDA(cudaMemcpyAsync(cnt + 5, h + 5, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        MF_K(k_growth<<<1, 32, 0, s>>>(c->i64a.p, rows, cnt + 5));
+        MF_CUDA(cudaMemcpyAsync(h + 5, cnt + 5, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
+        MF_CUDA(cudaStreamSynchronize(s));
+        c->max_csr = h[5];
+        packed = h[6];
+        c->stats.exact_sizes += 1;
+      }
     }
     MF_CUDA(cudaGetLastError());
 
@@ -1879,7 +2045,7 @@ void process_batch(mf_ctx* c, int64_t m) {
         MF_K(k_need_vertices<<<grid_for(nneed), kTB, 0, s>>>(c->need.p, nneed, c->seeds.p, c->needv.p));
         row_offsets(c, c->needv.p, nneed, kCntAll, ns, ep);
         MF_CUDA(cudaMemsetAsync(cnt + 35, 0, sizeof(int64_t), s));
-        MF_K(k_lb_mark_need<<<lb_grid(c), kTB, 0, s>>>(g, c->needv.p, c->lb_offs.p, nneed, ep, c->nmark.p,
+        MF_K(k_lb_mark_need<<<lb_grid(c, k_lb_mark_need), kTB, 0, s>>>(g, c->needv.p, c->lb_offs.p, nneed, ep, c->nmark.p,
                                                        c->nlist_need.p, ucnt + 35));
         MF_CUDA(cudaMemcpyAsync(h + 35, cnt + 35, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         MF_CUDA(cudaStreamSynchronize(s));
@@ -1900,21 +2066,30 @@ void process_batch(mf_ctx* c, int64_t m) {
     unsigned long long* wk_extra = c->work.p + 2 * kStCount;   // [0] seed, [1] hop, [2] candidate pushes
     MF_K(k_seed_self<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedRows, ns, ep);
-    MF_K(k_lb_push_seed<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk_extra + 0));
+    MF_K(k_lb_push_seed<<<lb_grid(c, k_lb_push_seed), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk_extra + 0));
     MF_K(k_self_push<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, ep, c->bval.p, c->wval.p));
     MF_K(k_self_push<<<grid_for(nh), kTB, 0, s>>>(c->hlist.p, nh, ep, c->bval.p, c->wval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedPushers, ns, ep);
-    MF_K(k_lb_push_hop<<<lb_grid(c), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, c->wval.p,
+    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, c->wval.p,
                                                   wk_extra + 1));
     row_offsets(c, c->hlist.p, nh, kCntHopPushers, ns, ep);
-    MF_K(k_lb_push_hop<<<lb_grid(c), kTB, 0, s>>>(g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p, c->wval.p,
+    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p, c->wval.p,
                                                   wk_extra + 1));
     if (c->symmetric && c->rows_sorted) {
-      MF_K(k_pull_cand<<<grid_for(n), kTB, 0, s>>>(g, c->v2i.p, c->rowcid.p, ns, c->wval.p, ep, c->cid.p,
-                                                   wk_extra + 2));
+      c->pull_long.reserve(std::max<int32_t>(n, 1));
+      const int64_t nwords = ((int64_t)n + 31) / 32;
+      c->ncbits.reserve(std::max<int64_t>(nwords, 1));
+      MF_CUDA(cudaMemsetAsync(c->ncbits.p, 0, sizeof(uint32_t) * (size_t)nwords, s));
+      MF_CUDA(cudaMemsetAsync(cnt + 36, 0, sizeof(int64_t), s));
+      if (nct > 0)
+        MF_K(k_cand_bits<<<grid_for(nct), kTB, 0, s>>>(c->cands.p, nct, ns, c->rowcid.p, c->ncbits.p));
+      const PullArgs pa{g,  c->v2i.p, c->rowcid.p, c->ncbits.p, ns, c->wval.p, ep, c->cid.p, c->pull_long.p,
+                        ucnt + 36, wk_extra + 2};
+      MF_K(k_pull_cand<<<grid_for(n), kTB, 0, s>>>(pa));
+      MF_K(k_pull_cand_long<<<lb_grid(c, k_pull_cand_long), kTB, 0, s>>>(pa));
     } else {
       row_offsets(c, c->cands.p, nct, kCntCandRows, ns, ep);
-      MF_K(k_lb_push_cand<<<lb_grid(c), kTB, 0, s>>>(g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
+      MF_K(k_lb_push_cand<<<lb_grid(c, k_lb_push_cand), kTB, 0, s>>>(g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
                                                      wk_extra + 2));
       MF_K(k_finalize_all<<<grid_for(((int64_t)n + 3) / 4), kTB, 0, s>>>(c->wval.p, n, ep, c->rowcid.p, c->cid.p));
     }
@@ -1933,7 +2108,7 @@ void process_batch(mf_ctx* c, int64_t m) {
       tr->seeds = fetch(c->seeds.p, ns, s);
       tr->cands = fetch(c->cands.p, nct, s);
       tr->cid_after = fetch(c->cid.p, n, s);
-      if (exact) tr->row_len = fetch(c->rowlens.p, rows, s);
+      if (packed >= 0) tr->row_len = fetch(c->rowlens.p, rows, s);
     }
 
     // ---- assignment + order (cluster ascending, index descending)
