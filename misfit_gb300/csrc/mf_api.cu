@@ -151,6 +151,9 @@ void release_all(mf_ctx* c) {
   c->dense_light.release();
   c->pull_long.release();
   c->ncbits.release();
+  for (auto* b : {&c->plan_cuts, &c->plan_ests, &c->plan_send, &c->plan_pos}) b->release();
+  c->plan_flags.release();
+  c->seeds_all.release();
   c->n2cache.release();
   c->n2stamp.release();
   for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();

@@ -427,6 +427,10 @@ struct mf_ctx {
   mf::DBuf<int64_t> dense_light;      // per dense seed light volume (size bound)
   mf::DBuf<int32_t> pull_long;        // vertices with long rows for the warp pull pass
   mf::DBuf<uint32_t> ncbits;          // non-skipped candidate bits for the pull pass
+  // sub-batch plan of the current batch: cuts, estimates, seed lists
+  mf::DBuf<int64_t> plan_cuts, plan_ests, plan_send, plan_pos;
+  mf::DBuf<uint8_t> plan_flags;
+  mf::DBuf<int32_t> seeds_all;
   mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
   mf::DBuf<uint32_t> n2stamp;          // batch stamp of each cached size
   uint32_t n2batch = 0;

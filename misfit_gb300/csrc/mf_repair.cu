@@ -74,42 +74,114 @@ __global__ void k_prev(const uint64_t* keys, const uint32_t* vals, int64_t cnt, 
   prev[slot] = pe;
 }
 
-// Estimate added by each edge of a sub-batch starting at p
-// (src/misfit/misfit.cu:501-507): deg * 1000 for each endpoint not seen yet.
-__global__ void k_contrib(const int32_t* u, const int32_t* v, const int32_t* prev, const int32_t* deg,
-                          int64_t p, int64_t len, int64_t* out) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= len) return;
-  const int64_t j = p + t;
-  int64_t c = 0;
-  if (prev[2 * j] < p) c += (int64_t)deg[u[j]] * kEstimateWeight;
-  if (prev[2 * j + 1] < p) c += (int64_t)deg[v[j]] * kEstimateWeight;
-  out[t] = c;
+// ---- sub-batch plan ---------------------------------------------------------------
+// The split and the seed lists depend only on the batch, the degrees and
+// MAX_CSR_ELEMENTS, not on the clustering or repair of earlier sub-batches,
+// so they are planned for the whole batch (from p0) at once.
+
+// Cuts of all sub-batches from p0 (src/misfit/misfit.cu:494-523): each edge
+// adds deg * 1000 for every endpoint not seen yet in its sub-batch
+// (:501-507), and the sub-batch ends before the first edge t >= 1 whose
+// running estimate reaches MAX_CSR_ELEMENTS (:509-511).  One CTA:
+// per sub-batch the estimates of a window of 1024 edges are scanned in shared
+// memory; the cut is the first t >= 1 whose running estimate reaches maxcsr,
+// else the length (min(m - p, MAX_BATCH_SIZE)).  cuts[k] = end of sub-batch
+// k, ests[k] = estimate of the edges before the cut.
+constexpr int kCutThreads = 1024;
+
+__global__ void __launch_bounds__(kCutThreads) k_cuts(const int32_t* u, const int32_t* v, const int32_t* prev,
+                                                      const int32_t* deg, int64_t m, int64_t p0, int64_t maxcsr,
+                                                      int64_t* cuts, int64_t* ests, unsigned long long* count) {
+  __shared__ int64_t s_warp[kCutThreads / 32];
+  __shared__ int64_t s_total;
+  __shared__ int64_t s_cut, s_est;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  int64_t p = p0, k = 0;
+  while (p < m) {
+    const int64_t len = min(m - p, kMaxBatchEdges);
+    int64_t acc = 0;
+    if (tid == 0) { s_cut = len; s_est = -1; }
+    __syncthreads();
+    for (int64_t t0 = 0; t0 < len; t0 += kCutThreads) {
+      const int64_t t = t0 + tid;
+      int64_t c = 0;
+      if (t < len) {
+        const int64_t j = p + t;
+        if (prev[2 * j] < p) c += (int64_t)deg[u[j]] * kEstimateWeight;
+        if (prev[2 * j + 1] < p) c += (int64_t)deg[v[j]] * kEstimateWeight;
+      }
+      int64_t inc = c;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+      }
+      if (lane == 31) s_warp[wid] = inc;
+      __syncthreads();
+      if (tid == 0) {
+        int64_t run = 0;
+        for (int w = 0; w < kCutThreads / 32; ++w) { const int64_t y = s_warp[w]; s_warp[w] = run; run += y; }
+        s_total = run;
+      }
+      __syncthreads();
+      const int64_t incl = acc + s_warp[wid] + inc;  // estimate of edges 0..t
+      if (t >= 1 && t < len && incl >= maxcsr) atomicMin((unsigned long long*)&s_cut, (unsigned long long)t);
+      __syncthreads();
+      if (t == s_cut) s_est = incl - c;
+      acc += s_total;
+      __syncthreads();
+      if (s_cut < len) break;
+    }
+    const int64_t cut = s_cut;
+    if (tid == 0) {
+      cuts[k] = p + cut;
+      ests[k] = s_est >= 0 ? s_est : acc;
+    }
+    __syncthreads();
+    p += cut;
+    ++k;
+  }
+  if (tid == 0) *count = (unsigned long long)k;
 }
 
-// First edge t >= 1 whose running estimate reaches MAX_CSR_ELEMENTS
-// (src/misfit/misfit.cu:509-511); pex is the exclusive scan (len+1 entries).
-__global__ void k_find_cut(const int64_t* pex, int64_t len, int64_t maxcsr, unsigned long long* out) {
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < 1 || t >= len) return;
-  if (pex[t + 1] >= maxcsr) atomicMin(out, (unsigned long long)t);
+// Seed flag of every endpoint slot from 2*p0: first appearance within its own
+// sub-batch (the sub-batch of edge j starts at the last cut <= j).
+__global__ void k_plan_seed_flags(const int32_t* prev, const int64_t* cuts, const unsigned long long* count, int64_t m,
+                                  int64_t p0, uint8_t* flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * (m - p0)) return;
+  const int64_t slot = 2 * p0 + i;
+  const int64_t j = slot >> 1;
+  int64_t lo = 0, hi = (int64_t)*count;  // first k with cuts[k] > j
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (cuts[mid] <= j) lo = mid + 1; else hi = mid;
+  }
+  const int64_t start = lo == 0 ? p0 : cuts[lo - 1];
+  flags[i] = prev[slot] < start ? 1 : 0;
 }
 
-__global__ void k_seed_flags(const int32_t* prev, int64_t p, int64_t q, uint8_t* flags) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 2 * (q - p)) return;
-  flags[i] = prev[2 * p + i] < p ? 1 : 0;
+__global__ void k_plan_seed_compact(const int32_t* u, const int32_t* v, const uint8_t* flags, const int64_t* pos,
+                                    int64_t m, int64_t p0, int32_t* seeds_all) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * (m - p0) || !flags[i]) return;
+  const int64_t slot = 2 * p0 + i;
+  seeds_all[pos[i]] = (slot & 1) ? v[slot >> 1] : u[slot >> 1];
 }
 
-__global__ void k_seed_compact(const int32_t* u, const int32_t* v, const uint8_t* flags, const int64_t* pos,
-                               int64_t p, int64_t q, int32_t* seeds, int32_t* v2i) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 2 * (q - p) || !flags[i]) return;
-  const int64_t slot = 2 * p + i;
-  const int32_t x = (slot & 1) ? v[slot >> 1] : u[slot >> 1];
-  const int64_t k = pos[i];
-  seeds[k] = x;
-  v2i[x] = (int32_t)k;
+// seed_end[k] = number of seeds of sub-batches 0..k.
+__global__ void k_plan_seed_ends(const int64_t* cuts, const unsigned long long* count, const int64_t* pos, int64_t p0,
+                                 int64_t* seed_end) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < (int64_t)*count) seed_end[k] = pos[2 * (cuts[k] - p0)];
+}
+
+// Seeds of one sub-batch into their rows: seeds[i], v2i[seeds[i]] = i.
+__global__ void k_seed_rows(const int32_t* seeds_all, int64_t ns, int32_t* seeds, int32_t* v2i) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  const int32_t x = seeds_all[i];
+  seeds[i] = x;
+  v2i[x] = (int32_t)i;
 }
 
 // ---- hop-1 set and candidates ---------------------------------------------------
@@ -187,21 +259,29 @@ __global__ void k_lb_bound(GraphView g, const int32_t* seeds, const int64_t* off
   if (cur >= 0 && acc) atomicAdd(uacc + cur, acc);
 }
 
-__global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct,
-                               const unsigned long long* uacc, const int64_t* n2cache, const uint32_t* n2stamp,
-                               uint32_t stamp, unsigned long long* out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// The candidate count comes from the hop-1 compaction on the device (low 32
+// bits of *hop_counts, capped at capc), so the bound needs no host round trip
+// after the hop-1 stage.  Grid-stride over the ns + nct rows.
+__global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands,
+                               const int64_t* hop_counts, int64_t capc, const unsigned long long* uacc,
+                               const int64_t* n2cache, const uint32_t* n2stamp, uint32_t stamp,
+                               unsigned long long* out) {
+  const int64_t nct = min((int64_t)(*hop_counts & 0xffffffffll), capc);
+  const int64_t rows = ns + nct;
   unsigned long long b = 0;
-  if (i < ns) {
-    const int32_t s = seeds[i];
-    if (n2stamp[s] == stamp) {
-      b = (unsigned long long)n2cache[s];   // exact size known from an earlier sub-batch
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+    if (i < ns) {
+      const int32_t s = seeds[i];
+      if (n2stamp[s] == stamp) {
+        b += (unsigned long long)n2cache[s];   // exact size known from an earlier sub-batch
+      } else {
+        unsigned long long e = 1ull + (unsigned long long)row_len(g, s) + uacc[i];
+        if (e > (unsigned long long)g.n) e = (unsigned long long)g.n;
+        b += e;
+      }
     } else {
-      b = 1ull + (unsigned long long)row_len(g, s) + uacc[i];
-      if (b > (unsigned long long)g.n) b = (unsigned long long)g.n;
+      b += (unsigned long long)row_len(g, cands[i - ns]);
     }
-  } else if (i < ns + nct) {
-    b = (unsigned long long)row_len(g, cands[i - ns]);
   }
   for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xffffffffu, b, o);
   if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, b);
@@ -851,10 +931,13 @@ __global__ void k_finalize_all(const uint32_t* wval, int32_t n, uint32_t epoch, 
 
 // ---- assignment and order ------------------------------------------------------------
 
+// The cluster count (*ccp, the new-id scan total) comes from the device; ids
+// at or beyond min(cluster_count, MAX_BATCH_SIZE) are dropped.
 __global__ void k_assign(const int32_t* u, const int32_t* v, int64_t p, int64_t len, const int32_t* cid,
-                         int64_t limit, uint64_t* keys, uint32_t* vals, unsigned long long* count) {
+                         const int64_t* ccp, uint64_t* keys, uint32_t* vals, unsigned long long* count) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= len) return;
+  const int64_t limit = min(*ccp, kMaxBatchEdges);
   const int64_t j = p + t;
   int32_t c = cid[u[j]];
   if (c == -1) c = cid[v[j]];
@@ -1939,31 +2022,59 @@ void process_batch(mf_ctx* c, int64_t m) {
   c->creates.reserve(kMaxRows + 2 * std::min<int64_t>(m, kMaxBatchEdges));
   c->rowlens.reserve(kMaxRows + 2 * std::min<int64_t>(m, kMaxBatchEdges) + 1);
 
+  // ---- sub-batch plan: cuts, estimates and seed lists of the whole batch
+  // from p0 (re-planned from the next sub-batch when MAX_CSR_ELEMENTS grows)
+  c->plan_cuts.reserve(std::max<int64_t>(m, 1));
+  c->plan_ests.reserve(std::max<int64_t>(m, 1));
+  c->plan_send.reserve(std::max<int64_t>(m, 1));
+  c->plan_flags.reserve(2 * m);
+  c->plan_pos.reserve(2 * m + 1);
+  c->seeds_all.reserve(2 * m);
+  std::vector<int64_t> cuts, ests, seed_end;
+  size_t kidx = 0;
+  int64_t seed_base = 0;
+  auto plan = [&](int64_t p0) {
+    sc.emplace(c, kStSplit);
+    unsigned long long* kcount = ucnt + 37;
+    MF_K(k_cuts<<<1, kCutThreads, 0, s>>>(c->bu.p, c->bv.p, c->prev.p, c->deg.p, m, p0, c->max_csr,
+                                          c->plan_cuts.p, c->plan_ests.p, kcount));
+    const int64_t nslots = 2 * (m - p0);
+    MF_K(k_plan_seed_flags<<<grid_for(nslots), kTB, 0, s>>>(c->prev.p, c->plan_cuts.p, kcount, m, p0,
+                                                              c->plan_flags.p));
+    scan_exclusive_u8(c->plan_flags.p, c->plan_pos.p, nslots, c->ws, s);
+    MF_K(k_plan_seed_compact<<<grid_for(nslots), kTB, 0, s>>>(c->bu.p, c->bv.p, c->plan_flags.p, c->plan_pos.p, m,
+                                                                p0, c->seeds_all.p));
+    MF_K(k_plan_seed_ends<<<grid_for(m - p0), kTB, 0, s>>>(c->plan_cuts.p, kcount, c->plan_pos.p, p0,
+                                                             c->plan_send.p));
+    MF_CUDA(cudaMemcpyAsync(h + 37, cnt + 37, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t nk = h[37];
+    cuts.resize((size_t)nk);
+    ests.resize((size_t)nk);
+    seed_end.resize((size_t)nk);
+    MF_CUDA(cudaMemcpyAsync(cuts.data(), c->plan_cuts.p, sizeof(int64_t) * (size_t)nk, cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaMemcpyAsync(ests.data(), c->plan_ests.p, sizeof(int64_t) * (size_t)nk, cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaMemcpyAsync(seed_end.data(), c->plan_send.p, sizeof(int64_t) * (size_t)nk, cudaMemcpyDeviceToHost,
+                            s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    kidx = 0;
+    seed_base = 0;
+    sc.reset();
+  };
+  plan(0);
+
   int64_t p = 0;
   while (p < m) {
-    const int64_t len = std::min<int64_t>(m - p, kMaxBatchEdges);
-    // ---- split
-    sc.emplace(c, kStSplit);
-    MF_K(k_contrib<<<grid_for(len), kTB, 0, s>>>(c->bu.p, c->bv.p, c->prev.p, c->deg.p, p, len, c->i64a.p));
-    scan_exclusive_i64(c->i64a.p, c->i64b.p, len, c->ws, s);
-    const int64_t lenv = len;
-    MF_CUDA(cudaMemcpyAsync(cnt, &lenv, sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    MF_K(k_find_cut<<<grid_for(len), kTB, 0, s>>>(c->i64b.p, len, c->max_csr, ucnt));
-    MF_CUDA(cudaMemcpyAsync(h, cnt, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    MF_CUDA(cudaStreamSynchronize(s));
-    const int64_t q = p + h[0];
-    int64_t est = 0;
-    MF_CUDA(cudaMemcpyAsync(&est, c->i64b.p + (q - p), sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    if (kidx >= cuts.size()) MF_FAIL(MF_ESTATE, "sub-batch plan ended before the batch");
+    const int64_t q = cuts[kidx];
+    const int64_t est = ests[kidx];
+    const int64_t ns = seed_end[kidx] - seed_base;
 
-    // ---- seeds (first appearance)
+    // ---- seeds (first appearance) of this sub-batch into their rows
     sc.emplace(c, kStSeeds);
-    const int64_t nslots = 2 * (q - p);
-    MF_K(k_seed_flags<<<grid_for(nslots), kTB, 0, s>>>(c->prev.p, p, q, c->u8a.p));
-    scan_exclusive_u8(c->u8a.p, c->i64a.p, nslots, c->ws, s);
-    MF_K(k_seed_compact<<<grid_for(nslots), kTB, 0, s>>>(c->bu.p, c->bv.p, c->u8a.p, c->i64a.p, p, q, c->seeds.p, c->v2i.p));
-    MF_CUDA(cudaMemcpyAsync(h + 1, c->i64a.p + nslots, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    MF_CUDA(cudaStreamSynchronize(s));
-    const int64_t ns = h[1];
+    if (ns > 0)
+      MF_K(k_seed_rows<<<grid_for(ns), kTB, 0, s>>>(c->seeds_all.p + seed_base, ns, c->seeds.p, c->v2i.p));
+    const int64_t max_before = c->max_csr;
 
     // ---- hop-1 set, candidates in ascending id
     sc.emplace(c, kStHop1);
@@ -1976,25 +2087,26 @@ void process_batch(mf_ctx* c, int64_t m) {
     const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
     MF_K(k_mark_compact<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->i64a.p, n, ep, capc, ns, c->hlist.p, c->cands.p,
                                                     c->v2i.p));
-    MF_CUDA(cudaMemcpyAsync(h + 2, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    MF_CUDA(cudaStreamSynchronize(s));
-    h[3] = h[2] & 0xffffffffll;
-    h[2] = h[2] >> 32;
-    const int64_t nh = h[2];
-    const int64_t nct = std::min<int64_t>(h[3], capc);
-    const int64_t rows = ns + nct;
 
-    // ---- packed sizes and MAX_CSR_ELEMENTS growth
+    // ---- packed sizes (upper bound) and MAX_CSR_ELEMENTS growth; one host
+    // round trip for the hop-1 counts and the bound
     sc.emplace(c, kStSizes);
     MF_CUDA(cudaMemsetAsync(cnt + 4, 0, sizeof(int64_t), s));
     c->uacc.reserve(std::max<int64_t>(ns, 1));
     MF_CUDA(cudaMemsetAsync(c->uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), s));
     row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
     MF_K(k_lb_bound<<<lb_grid(c, k_lb_bound), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, c->uacc.p));
-    MF_K(k_bound_finish<<<grid_for(rows), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, nct, c->uacc.p, c->n2cache.p,
-                                                        c->n2stamp.p, c->n2batch, ucnt + 4));
+    MF_K(k_bound_finish<<<lb_grid(c, k_bound_finish), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, c->i64a.p + n,
+                                                                   capc, c->uacc.p, c->n2cache.p, c->n2stamp.p,
+                                                                   c->n2batch, ucnt + 4));
+    MF_CUDA(cudaMemcpyAsync(h + 2, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
+    h[3] = h[2] & 0xffffffffll;
+    h[2] = h[2] >> 32;
+    const int64_t nh = h[2];
+    const int64_t nct = std::min<int64_t>(h[3], capc);
+    const int64_t rows = ns + nct;
     int64_t packed = -1;
     const bool exact = h[4] >= c->max_csr;
     if (exact) {
@@ -2094,8 +2206,6 @@ void process_batch(mf_ctx* c, int64_t m) {
       MF_K(k_finalize_all<<<grid_for(((int64_t)n + 3) / 4), kTB, 0, s>>>(c->wval.p, n, ep, c->rowcid.p, c->cid.p));
     }
     c->touched_total += n;
-    MF_CUDA(cudaStreamSynchronize(s));
-    const int64_t cc = h[7];
     MF_CUDA(cudaGetLastError());
 
     sc.reset();
@@ -2104,7 +2214,7 @@ void process_batch(mf_ctx* c, int64_t m) {
       c->traces.emplace_back();
       tr = &c->traces.back();
       tr->hdr[0] = p; tr->hdr[1] = q; tr->hdr[2] = ns; tr->hdr[3] = nct; tr->hdr[4] = packed;
-      tr->hdr[5] = c->max_csr; tr->hdr[6] = cc; tr->hdr[8] = rows; tr->hdr[9] = est;
+      tr->hdr[5] = c->max_csr; tr->hdr[8] = rows; tr->hdr[9] = est;   // hdr[6] after the assignment
       tr->seeds = fetch(c->seeds.p, ns, s);
       tr->cands = fetch(c->cands.p, nct, s);
       tr->cid_after = fetch(c->cid.p, n, s);
@@ -2113,12 +2223,15 @@ void process_batch(mf_ctx* c, int64_t m) {
 
     // ---- assignment + order (cluster ascending, index descending)
     sc.emplace(c, kStAssign);
-    const int64_t limit = std::min<int64_t>(cc, kMaxBatchEdges);
     MF_CUDA(cudaMemsetAsync(cnt + 9, 0, sizeof(int64_t), s));
-    MF_K(k_assign<<<grid_for(q - p), kTB, 0, s>>>(c->bu.p, c->bv.p, p, q - p, c->cid.p, limit, c->keys.p, c->vals.p, ucnt + 9));
+    MF_K(k_assign<<<grid_for(q - p), kTB, 0, s>>>(c->bu.p, c->bv.p, p, q - p, c->cid.p, c->i64b.p + rows, c->keys.p,
+                                                  c->vals.p, ucnt + 9));
     MF_CUDA(cudaMemcpyAsync(h + 9, cnt + 9, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
+    const int64_t cc = h[7];
+    const int64_t limit = std::min<int64_t>(cc, kMaxBatchEdges);
     const int64_t nproc = h[9];
+    if (tr) tr->hdr[6] = cc;
     radix_sort_pairs(c->keys.p, c->vals.p, nproc, kRowBits + bits_for(std::max<int64_t>(limit, 1)), c->ws, s);
 
     // ---- repair (times itself: rounds vs grid-wide searches)
@@ -2145,6 +2258,9 @@ void process_batch(mf_ctx* c, int64_t m) {
     c->stats.clusters += cc;
     c->stats.processed_edges += nproc;
     p = q;
+    seed_base = seed_end[kidx];
+    ++kidx;
+    if (c->max_csr != max_before && p < m) plan(p);  // the cuts after a growth follow the new limit
   }
   c->stats.max_csr = c->max_csr;
 }
