@@ -39,6 +39,14 @@ sys.path.insert(0, ROOT)
 METRIC = "edge updates/s and p50/p99 batch latency, plain per-batch loop, 1 GB300"
 UNIT = "updates/s"
 
+# DRAM bytes (read + write) per pushed element of k_lb_push_hop, measured by
+# ncu on the R-MAT scale-20, 20,000-update case: dram__bytes_read.sum +
+# dram__bytes_write.sum over launches 6-9 of the kernel (71,991,808 bytes)
+# divided by their pushed elements (3,619,180, printed with
+# MISFIT_GB_DEBUG=2).  ncu flushes the caches before each launch, so this is
+# a cold-L2 figure.
+PUSH_HOP_DRAM_BYTES_PER_ELEMENT = 19.89
+
 
 def parse_args():
     ap = argparse.ArgumentParser()
@@ -280,15 +288,23 @@ def main():
         e2e = {"value": world * args.steps * args.batch / (float(np.sum(e2e_ms)) / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": int(args.batch * 9), "d2h_bytes_per_step": int(n)}
 
-    # ---- roofline of the dominant byte-counted stage (the clustering push)
+    # ---- roofline of the dominant kernel, k_lb_push_hop (the hop-2 reach of
+    # the clustering write): algorithmic bytes = 12 B per pushed element
+    # (4 B row entry read + 4 B state read + 4 B cid write), timed by CUDA
+    # events around each of its launches on the library's stream.
     peak, peak_kind = measured_peaks()
-    stage = "cluster_write"
-    ms, calls, nbytes = prof[stage]
+    ms, calls, nbytes = prof["push_hop"]
     achieved = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
-    top = max(prof.items(), key=lambda kv: kv[1][0])
+    per_launch = nbytes / max(calls, 1)
+    elements = per_launch / 12.0
+    traffic = None if PUSH_HOP_DRAM_BYTES_PER_ELEMENT is None else PUSH_HOP_DRAM_BYTES_PER_ELEMENT * elements
+    top = max(((k, v) for k, v in prof.items() if k != "push_hop"), key=lambda kv: kv[1][0])
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "cluster_write (k_lb_push_*)", "peak_kind": peak_kind,
-            "algorithmic_bytes_per_launch": nbytes / max(calls, 1), "avg_launch_ms": ms / max(calls, 1)}
+            "traffic": traffic, "kernel": "k_lb_push_hop", "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": ms / max(calls, 1),
+            "launches": int(calls),
+            "traffic_note": "DRAM bytes per pushed element from an ncu capture of the R-MAT scale-20 case, "
+                            "times this workload's elements per launch"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -202,7 +202,7 @@ void mf_free(void* p);
 /* ---- profiling ----------------------------------------------------------- */
 
 /* Number of stages the profiler distinguishes. */
-#define MF_NUM_STAGES 12
+#define MF_NUM_STAGES 13
 /* Name of stage i (0 <= i < MF_NUM_STAGES), NULL otherwise. */
 const char* mf_stage_name(int stage);
 /* When on, every later batch records CUDA events around each stage on the

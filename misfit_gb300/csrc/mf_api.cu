@@ -81,7 +81,8 @@ void ktime_end(const char* launch_text, double t0) {
 }
 
 const char* const kStageNames[kStCount] = {"overlay", "split",  "seeds", "hop1",  "sizes", "cluster_read",
-                                           "cluster_write", "assign", "repair", "clear", "exact", "repair_big"};
+                                           "cluster_write", "assign", "repair", "clear", "exact", "repair_big",
+                                           "push_hop"};
 
 void set_error(const std::string& msg) { g_error = msg; }
 const char* get_error() { return g_error.c_str(); }
@@ -235,7 +236,9 @@ void run_batch(mf_ctx* c, int64_t m) {
     unsigned long long w[2 * mf::kStCount + 8];
     MF_CUDA(cudaMemcpy(w, c->work.p, sizeof(w), cudaMemcpyDeviceToHost));
     const unsigned long long* x = w + 2 * mf::kStCount;
-    c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + x[1] + x[2]);
+    // 4 B row entry + 8 B state read and cid write per pushed element
+    c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + x[2]);
+    c->stage_bytes[mf::kStPushHop] += 12.0 * (double)x[1];
     if (debug)
       std::fprintf(stderr, "[misfit_gb] batch: push elements seed %llu hop %llu cand %llu; sub-batches %lld\n", x[0],
                    x[1], x[2], (long long)c->stats.sub_batches);

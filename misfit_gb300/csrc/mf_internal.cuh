@@ -91,6 +91,7 @@ enum Stage : int {
   kStClear,         // clear of mapped vertices
   kStExact,         // exact 2-hop sizes (heavy bitmaps) and limit growth
   kStRepairBig,     // MIS repair: grid-wide hop-2 searches
+  kStPushHop,       // the k_lb_push_hop launches alone (part of the clustering write)
   kStCount
 };
 extern const char* const kStageNames[kStCount];

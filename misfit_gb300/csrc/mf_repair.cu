@@ -1682,6 +1682,30 @@ bool debug_counters() {
   return on;
 }
 
+// MISFIT_GB_DEBUG=2: also the elements of every k_lb_push_hop launch.
+bool debug_launches() {
+  static const bool on = [] {
+    const char* e = std::getenv("MISFIT_GB_DEBUG");
+    return e != nullptr && std::atoi(e) >= 2;
+  }();
+  return on;
+}
+
+// Counter value before a k_lb_push_hop launch (debug only).
+unsigned long long debug_counter(mf_ctx* c, const unsigned long long* counter) {
+  unsigned long long v = 0;
+  MF_CUDA(cudaStreamSynchronize(c->stream));
+  MF_CUDA(cudaMemcpy(&v, counter, sizeof(v), cudaMemcpyDeviceToHost));
+  return v;
+}
+
+// Prints the elements the k_lb_push_hop launch just made pushed (debug only).
+void debug_push_hop(mf_ctx* c, const unsigned long long* counter, unsigned long long before) {
+  static long long launch = 0;
+  std::fprintf(stderr, "[misfit_gb] k_lb_push_hop launch %lld elements %llu\n", launch++,
+               debug_counter(c, counter) - before);
+}
+
 // Exact 2-hop list sizes of the seeds into c->rowlens[0..ns).
 // With bound_only, dense seeds get an upper bound (k_dense_bound) instead of
 // their exact size and nothing is cached.
@@ -2182,11 +2206,19 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_K(k_self_push<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, ep, c->bval.p, c->wval.p));
     MF_K(k_self_push<<<grid_for(nh), kTB, 0, s>>>(c->hlist.p, nh, ep, c->bval.p, c->wval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedPushers, ns, ep);
-    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, c->wval.p,
-                                                  wk_extra + 1));
+    const unsigned long long dbg0 = debug_launches() ? debug_counter(c, wk_extra + 1) : 0;
+    sc.emplace(c, kStPushHop);
+    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p,
+                                                                 c->wval.p, wk_extra + 1));
+    sc.emplace(c, kStPush);
+    if (debug_launches()) debug_push_hop(c, wk_extra + 1, dbg0);
     row_offsets(c, c->hlist.p, nh, kCntHopPushers, ns, ep);
-    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p, c->wval.p,
-                                                  wk_extra + 1));
+    const unsigned long long dbg1 = debug_launches() ? debug_counter(c, wk_extra + 1) : 0;
+    sc.emplace(c, kStPushHop);
+    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p,
+                                                                 c->wval.p, wk_extra + 1));
+    sc.emplace(c, kStPush);
+    if (debug_launches()) debug_push_hop(c, wk_extra + 1, dbg1);
     if (c->symmetric && c->rows_sorted) {
       c->pull_long.reserve(std::max<int32_t>(n, 1));
       const int64_t nwords = ((int64_t)n + 31) / 32;
