@@ -155,6 +155,8 @@ void release_all(mf_ctx* c) {
   for (auto* b : {&c->plan_cuts, &c->plan_ests, &c->plan_send, &c->plan_pos}) b->release();
   c->plan_flags.release();
   c->seeds_all.release();
+  for (auto* b : {&c->rq_idx, &c->rq_v, &c->mq_idx, &c->mq_v}) b->release();
+  c->mq_base.release();
   c->n2cache.release();
   c->n2stamp.release();
   for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();

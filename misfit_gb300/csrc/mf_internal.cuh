@@ -432,6 +432,9 @@ struct mf_ctx {
   mf::DBuf<int64_t> plan_cuts, plan_ests, plan_send, plan_pos;
   mf::DBuf<uint8_t> plan_flags;
   mf::DBuf<int32_t> seeds_all;
+  // first-hit chunk queue (rows) and the need seeds' chunk queue
+  mf::DBuf<int32_t> rq_idx, rq_v, mq_idx, mq_v;
+  mf::DBuf<int64_t> mq_base;
   mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
   mf::DBuf<uint32_t> n2stamp;          // batch stamp of each cached size
   uint32_t n2batch = 0;

@@ -610,50 +610,146 @@ struct HasCid {   // the element already carries a cluster id
   __device__ __forceinline__ bool operator()(int32_t y) const { return cid[y] != -1; }
 };
 
-template <class P>
-__global__ void k_first_bounded(GraphView g, const int32_t* list, int64_t cnt, P pred, unsigned long long* firstpos,
-                                int32_t* unres_idx, int32_t* unres_v, int64_t* unres_cnt,
-                                unsigned long long* ucount) {
-  const int64_t w = warp_id();
-  if (w >= cnt) return;
-  const int lane = threadIdx.x & 31;
-  const int32_t x = list[w];
-  const int64_t nb = g.nindex[x + 1] - g.nindex[x];
-  const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
-  const int64_t lim = np < kFirstBound ? np : kFirstBound;
-  for (int64_t k0 = 0; k0 < lim; k0 += 32) {
-    const int64_t k = k0 + lane;
-    bool ok = false;
-    if (k < lim) {
-      const int32_t y = row_elem(g, x, k, nb);
-      ok = y >= 0 && pred(y);
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, ok);
-    if (m) {
-      if (lane == 0) firstpos[w] = (unsigned long long)(k0 + __ffs(m) - 1);
-      return;
-    }
+// ---- first-hit searches with device-side counts ---------------------------------
+// Three levels, none of which needs the host to know a count:
+//   1. one thread per row probes the first kProbe positions;
+//   2. rows still open go to a queue; a fixed grid of warps scans positions
+//      kProbe .. kFirstBound of each;
+//   3. rows still open get chunks of kFirstChunk positions from one packed
+//      64-bit counter ((rows << 40) | chunks), so that the chunk bases grow
+//      with the row slots; a fixed grid of warps takes chunks, finds the row
+//      by binary search over the bases and keeps the minimum hit position.
+// The same chunk queue drives the marking of the need seeds' neighbours.
+constexpr int kProbe = 8;
+constexpr int64_t kFirstChunk = 256;
+constexpr int kChunkShift = 40;
+constexpr unsigned long long kChunkMask = (1ull << kChunkShift) - 1;
+
+struct ChunkQueue {
+  int32_t* idx;                    // caller's row index
+  int32_t* v;                      // row vertex
+  int64_t* base;                   // first chunk of the row
+  unsigned long long* packed;      // (rows << 40) | chunks
+};
+
+__device__ __forceinline__ void cq_push(const ChunkQueue& q, int32_t idx, int32_t v, int64_t chunks) {
+  const unsigned long long old = atomicAdd(q.packed, (1ull << kChunkShift) | (unsigned long long)chunks);
+  const int64_t slot = (int64_t)(old >> kChunkShift);
+  q.idx[slot] = idx;
+  q.v[slot] = v;
+  q.base[slot] = (int64_t)(old & kChunkMask);
+}
+
+// Slot of chunk c: the last slot whose base is <= c (bases grow with slots).
+__device__ __forceinline__ int64_t cq_slot(const ChunkQueue& q, int64_t rows, int64_t c) {
+  int64_t lo = 0, hi = rows;
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (q.base[mid] <= c) lo = mid; else hi = mid;
   }
-  if (lane == 0) {
-    firstpos[w] = kNoPos;
-    if (np > kFirstBound) {
-      const unsigned long long u = atomicAdd(ucount, 1ull);
-      unres_idx[u] = (int32_t)w;
-      unres_v[u] = x;
-      unres_cnt[u] = np - kFirstBound;
+  return lo;
+}
+
+struct FirstQueues {
+  int32_t* mid_idx;
+  int32_t* mid_v;
+  unsigned long long* mid_count;
+  ChunkQueue rest;
+};
+
+template <class P>
+__global__ void k_first_probe(GraphView g, const int32_t* list, const unsigned long long* dcnt, P pred,
+                              unsigned long long* firstpos, FirstQueues q) {
+  const int64_t cnt = (int64_t)*dcnt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t x = list[i];
+    const int64_t nb = g.nindex[x + 1] - g.nindex[x];
+    const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
+    const int64_t lim = np < kProbe ? np : kProbe;
+    unsigned long long fp = kNoPos;
+    for (int64_t k = 0; k < lim; ++k) {
+      const int32_t y = row_elem(g, x, k, nb);
+      if (y >= 0 && pred(y)) {
+        fp = (unsigned long long)k;
+        break;
+      }
+    }
+    firstpos[i] = fp;
+    if (fp == kNoPos && np > kProbe) {
+      const unsigned long long u = atomicAdd(q.mid_count, 1ull);
+      q.mid_idx[u] = (int32_t)i;
+      q.mid_v[u] = x;
     }
   }
 }
 
 template <class P>
-__global__ void k_first_rest(GraphView g, const int32_t* unres_idx, const int32_t* unres_v, const int64_t* offs,
-                             int64_t ucnt, P pred, unsigned long long* firstpos) {
-  lb_rows_pos(g, unres_v, offs, ucnt, kFirstBound, [&](int64_t i, int32_t, int32_t y, int64_t j) {
-    if (pred(y)) {
-      unsigned long long* fp = firstpos + unres_idx[i];
-      if ((unsigned long long)j < *fp) atomicMin(fp, (unsigned long long)j);
+__global__ void k_first_warp(GraphView g, P pred, unsigned long long* firstpos, FirstQueues q) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nmid = (int64_t)*q.mid_count;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp_id(); w < nmid; w += nw) {
+    const int32_t i = q.mid_idx[w];
+    const int32_t x = q.mid_v[w];
+    const int64_t nb = g.nindex[x + 1] - g.nindex[x];
+    const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
+    const int64_t lim = np < kFirstBound ? np : kFirstBound;
+    bool found = false;
+    for (int64_t k0 = kProbe; k0 < lim; k0 += 32) {
+      const int64_t k = k0 + lane;
+      bool ok = false;
+      if (k < lim) {
+        const int32_t y = row_elem(g, x, k, nb);
+        ok = y >= 0 && pred(y);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, ok);
+      if (m) {
+        if (lane == 0) firstpos[i] = (unsigned long long)(k0 + __ffs(m) - 1);
+        found = true;
+        break;
+      }
     }
-  });
+    if (!found && np > kFirstBound && lane == 0)
+      cq_push(q.rest, i, x, (np - kFirstBound + kFirstChunk - 1) / kFirstChunk);
+  }
+}
+
+template <class P>
+__global__ void k_first_chunks(GraphView g, P pred, unsigned long long* firstpos, FirstQueues q) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long pk = *q.rest.packed;
+  const int64_t rows = (int64_t)(pk >> kChunkShift), chunks = (int64_t)(pk & kChunkMask);
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp_id(); c < chunks; c += nw) {
+    int64_t slot = 0;
+    if (lane == 0) slot = cq_slot(q.rest, rows, c);
+    slot = __shfl_sync(0xffffffffu, slot, 0);
+    const int32_t i = q.rest.idx[slot];
+    const int32_t x = q.rest.v[slot];
+    const int64_t p0 = kFirstBound + (c - q.rest.base[slot]) * kFirstChunk;
+    // skip when an earlier position already hit; one lane reads, so that the
+    // whole warp takes the same branch while other warps lower the value
+    unsigned long long fp = 0;
+    if (lane == 0) fp = *(volatile const unsigned long long*)(firstpos + i);
+    fp = __shfl_sync(0xffffffffu, fp, 0);
+    if (fp <= (unsigned long long)p0) continue;
+    const int64_t nb = g.nindex[x + 1] - g.nindex[x];
+    const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
+    const int64_t end = min(p0 + kFirstChunk, np);
+    for (int64_t k0 = p0; k0 < end; k0 += 32) {
+      const int64_t k = k0 + lane;
+      bool ok = false;
+      if (k < end) {
+        const int32_t y = row_elem(g, x, k, nb);
+        ok = y >= 0 && pred(y);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, ok);
+      if (m) {
+        if (lane == 0) atomicMin(firstpos + i, (unsigned long long)(k0 + __ffs(m) - 1));
+        break;
+      }
+    }
+  }
 }
 
 // Per row: early return when the row's own vertex already has an id
@@ -677,42 +773,66 @@ __global__ void k_row_skip(const int32_t* seeds, int64_t ns, const int32_t* cand
 
 // The first existing id of row(x) in order, if any; seeds without one go on
 // to their hop-2 part (`need`), everything else without one creates a cluster.
-__global__ void k_live_decide(GraphView g, const int32_t* live_i, const int32_t* live_v, int64_t cnt, int64_t ns,
-                              const unsigned long long* firstpos, const int32_t* cid, int32_t* rowcid,
-                              uint8_t* creates, int32_t* need, unsigned long long* nneed) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= cnt) return;
-  const int32_t i = live_i[k];
-  const int32_t x = live_v[k];
-  const unsigned long long fp = firstpos[k];
-  if (fp != kNoPos) {
-    rowcid[i] = cid[row_elem(g, x, (int64_t)fp, g.nindex[x + 1] - g.nindex[x])];
-    creates[i] = 0;
-    return;
+__global__ void k_live_decide(GraphView g, const int32_t* live_i, const int32_t* live_v,
+                              const unsigned long long* dcnt, int64_t ns, const unsigned long long* firstpos,
+                              const int32_t* cid, int32_t* rowcid, uint8_t* creates, const int32_t* seeds,
+                              int32_t* need, int32_t* needv, unsigned long long* nneed, ChunkQueue mq) {
+  const int64_t cnt = (int64_t)*dcnt;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t i = live_i[k];
+    const int32_t x = live_v[k];
+    const unsigned long long fp = firstpos[k];
+    if (fp != kNoPos) {
+      rowcid[i] = cid[row_elem(g, x, (int64_t)fp, g.nindex[x + 1] - g.nindex[x])];
+      creates[i] = 0;
+      continue;
+    }
+    rowcid[i] = -1;
+    creates[i] = 1;
+    if (i < ns) {
+      const unsigned long long u = atomicAdd(nneed, 1ull);
+      need[u] = i;
+      const int32_t s = seeds[i];
+      needv[u] = s;
+      const int64_t np = row_positions(g, s);
+      if (np > 0) cq_push(mq, (int32_t)u, s, (np + kFirstChunk - 1) / kFirstChunk);
+    }
   }
-  rowcid[i] = -1;
-  creates[i] = 1;
-  if (i < ns) need[atomicAdd(nneed, 1ull)] = i;
 }
 
 // A seed row is [s] ++ row(s) ++ row(h1) ++ row(h2) ++ ... (h over row(s) in
 // order): after row(s), its first existing id is f1(h) of the first h of
 // row(s) that has one, f1(h) being the id of the first element of row(h)
 // with an id.  f1 is computed for the neighbours of the seeds that need it.
-__global__ void k_lb_mark_need(GraphView g, const int32_t* needv, const int64_t* offs, int64_t cnt, uint32_t epoch,
-                               uint32_t* nmark, int32_t* list, unsigned long long* count) {
-  lb_rows(g, needv, offs, cnt, [&](int64_t, int32_t, int32_t y) {
-    if (nmark[y] != epoch && atomicExch(nmark + y, epoch) != epoch) list[atomicAdd(count, 1ull)] = y;
-  });
+__global__ void k_mark_need(GraphView g, ChunkQueue mq, uint32_t epoch, uint32_t* nmark, int32_t* list,
+                            unsigned long long* count) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long pk = *mq.packed;
+  const int64_t rows = (int64_t)(pk >> kChunkShift), chunks = (int64_t)(pk & kChunkMask);
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp_id(); c < chunks; c += nw) {
+    int64_t slot = 0;
+    if (lane == 0) slot = cq_slot(mq, rows, c);
+    slot = __shfl_sync(0xffffffffu, slot, 0);
+    const int32_t x = mq.v[slot];
+    const int64_t p0 = (c - mq.base[slot]) * kFirstChunk;
+    const int64_t nb = g.nindex[x + 1] - g.nindex[x];
+    const int64_t end = min(p0 + kFirstChunk, nb + (g.aoff[x + 1] - g.aoff[x]));
+    for (int64_t k = p0 + lane; k < end; k += 32) {
+      const int32_t y = row_elem(g, x, k, nb);
+      if (y >= 0 && nmark[y] != epoch && atomicExch(nmark + y, epoch) != epoch) list[atomicAdd(count, 1ull)] = y;
+    }
+  }
 }
 
-__global__ void k_f1_finish(GraphView g, const int32_t* list, int64_t cnt, const unsigned long long* firstpos,
-                            const int32_t* cid, int32_t* f1) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cnt) return;
-  const int32_t x = list[i];
-  const unsigned long long fp = firstpos[i];
-  f1[x] = fp == kNoPos ? -1 : cid[row_elem(g, x, (int64_t)fp, g.nindex[x + 1] - g.nindex[x])];
+__global__ void k_f1_finish(GraphView g, const int32_t* list, const unsigned long long* dcnt,
+                            const unsigned long long* firstpos, const int32_t* cid, int32_t* f1) {
+  const int64_t cnt = (int64_t)*dcnt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t x = list[i];
+    const unsigned long long fp = firstpos[i];
+    f1[x] = fp == kNoPos ? -1 : cid[row_elem(g, x, (int64_t)fp, g.nindex[x + 1] - g.nindex[x])];
+  }
 }
 
 struct HasF1 {    // the element's own row holds an element with a cluster id
@@ -720,22 +840,18 @@ struct HasF1 {    // the element's own row holds an element with a cluster id
   __device__ __forceinline__ bool operator()(int32_t y) const { return f1[y] != -1; }
 };
 
-__global__ void k_need_vertices(const int32_t* need, int64_t cnt, const int32_t* seeds, int32_t* out) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < cnt) out[k] = seeds[need[k]];
-}
-
-__global__ void k_need_decide(GraphView g, const int32_t* need, const int32_t* needv, int64_t cnt,
+__global__ void k_need_decide(GraphView g, const int32_t* need, const int32_t* needv, const unsigned long long* dcnt,
                               const unsigned long long* firstpos, const int32_t* f1, int32_t* rowcid,
                               uint8_t* creates) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= cnt) return;
-  const unsigned long long fp = firstpos[k];
-  if (fp == kNoPos) return;
-  const int32_t s = needv[k];
-  const int32_t h = row_elem(g, s, (int64_t)fp, g.nindex[s + 1] - g.nindex[s]);
-  rowcid[need[k]] = f1[h];
-  creates[need[k]] = 0;
+  const int64_t cnt = (int64_t)*dcnt;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long fp = firstpos[k];
+    if (fp == kNoPos) continue;
+    const int32_t s = needv[k];
+    const int32_t h = row_elem(g, s, (int64_t)fp, g.nindex[s + 1] - g.nindex[s]);
+    rowcid[need[k]] = f1[h];
+    creates[need[k]] = 0;
+  }
 }
 
 __global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid) {
@@ -1832,28 +1948,26 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
 }
 
 
-// First-hit search of `pred` over the rows of list[0..cnt) into c->fpos.
+// First-hit search of `pred` over the rows of list[0 .. *dcnt) into c->fpos;
+// `upper` bounds *dcnt.  No host round trip: every level reads its count on
+// the device.
 template <class P>
-void first_hits(mf_ctx* c, const int32_t* list, int64_t cnt, P pred) {
+void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, int64_t upper, P pred) {
   cudaStream_t s = c->stream;
-  int64_t* h = c->h_counters;
-  c->fpos.reserve(std::max<int64_t>(cnt, 1));
-  c->un_idx.reserve(std::max<int64_t>(cnt, 1));
-  c->un_v.reserve(std::max<int64_t>(cnt, 1));
-  c->un_cnt.reserve(std::max<int64_t>(cnt, 1));
-  if (cnt == 0) return;
-  MF_CUDA(cudaMemsetAsync(c->counters.p + 32, 0, sizeof(int64_t), s));
-  MF_K(k_first_bounded<<<warps_grid(cnt), kTB, 0, s>>>(c->view(), list, cnt, pred, c->fpos.p, c->un_idx.p, c->un_v.p,
-                                                     c->un_cnt.p,
-                                                     reinterpret_cast<unsigned long long*>(c->counters.p) + 32));
-  MF_CUDA(cudaMemcpyAsync(h + 32, c->counters.p + 32, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-  MF_CUDA(cudaStreamSynchronize(s));
-  const int64_t un = h[32];
-  if (un == 0) return;
-  c->lb_offs.reserve(un + 1);
-  scan_exclusive_i64(c->un_cnt.p, c->lb_offs.p, un, c->ws, s);
-  MF_K(k_first_rest<<<lb_grid(c, k_first_rest<P>), kTB, 0, s>>>(c->view(), c->un_idx.p, c->un_v.p, c->lb_offs.p, un, pred,
-                                               c->fpos.p));
+  const int64_t cap = std::max<int64_t>(upper, 1);
+  c->fpos.reserve(cap);
+  c->un_idx.reserve(cap);
+  c->un_v.reserve(cap);
+  c->un_cnt.reserve(cap);
+  c->rq_idx.reserve(cap);
+  c->rq_v.reserve(cap);
+  unsigned long long* ucnt = reinterpret_cast<unsigned long long*>(c->counters.p);
+  MF_CUDA(cudaMemsetAsync(ucnt + 48, 0, sizeof(unsigned long long) * 2, s));
+  const FirstQueues q{c->un_idx.p, c->un_v.p, ucnt + 48, ChunkQueue{c->rq_idx.p, c->rq_v.p, c->un_cnt.p, ucnt + 49}};
+  const GraphView g = c->view();
+  MF_K(k_first_probe<<<lb_grid(c, k_first_probe<P>), kTB, 0, s>>>(g, list, dcnt, pred, c->fpos.p, q));
+  MF_K(k_first_warp<<<lb_grid(c, k_first_warp<P>), kTB, 0, s>>>(g, pred, c->fpos.p, q));
+  MF_K(k_first_chunks<<<lb_grid(c, k_first_chunks<P>), kTB, 0, s>>>(g, pred, c->fpos.p, q));
 }
 
 void next_epoch(mf_ctx* c) {
@@ -2158,43 +2272,31 @@ void process_batch(mf_ctx* c, int64_t m) {
     }
     MF_CUDA(cudaGetLastError());
 
-    // ---- clustering (bulk-synchronous)
+    // ---- clustering (bulk-synchronous); counts stay on the device
     sc.emplace(c, kStFirst);
     c->live_i.reserve(std::max<int64_t>(rows, 1));
     c->live_v.reserve(std::max<int64_t>(rows, 1));
     c->need.reserve(std::max<int64_t>(ns, 1));
-    MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t) * 2, s));
+    c->needv.reserve(std::max<int64_t>(ns, 1));
+    c->mq_idx.reserve(std::max<int64_t>(ns, 1));
+    c->mq_v.reserve(std::max<int64_t>(ns, 1));
+    c->mq_base.reserve(std::max<int64_t>(ns, 1));
+    MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t) * 3, s));   // live rows, need seeds, their neighbours
+    MF_CUDA(cudaMemsetAsync(cnt + 50, 0, sizeof(int64_t), s));       // chunk queue of the need seeds' rows
+    const ChunkQueue mq{c->mq_idx.p, c->mq_v.p, c->mq_base.p, ucnt + 50};
     MF_K(k_row_skip<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->rowcid.p,
                                                     c->creates.p, c->live_i.p, c->live_v.p, ucnt + 33));
-    MF_CUDA(cudaMemcpyAsync(h + 33, cnt + 33, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    MF_CUDA(cudaStreamSynchronize(s));
-    const int64_t nlive = h[33];
-    if (nlive > 0) {
-      first_hits(c, c->live_v.p, nlive, HasCid{c->cid.p});
-      MF_K(k_live_decide<<<grid_for(nlive), kTB, 0, s>>>(g, c->live_i.p, c->live_v.p, nlive, ns, c->fpos.p, c->cid.p,
-                                                          c->rowcid.p, c->creates.p, c->need.p, ucnt + 34));
-      MF_CUDA(cudaMemcpyAsync(h + 34, cnt + 34, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-      MF_CUDA(cudaStreamSynchronize(s));
-      const int64_t nneed = h[34];
-      if (nneed > 0) {
-        c->needv.reserve(nneed);
-        MF_K(k_need_vertices<<<grid_for(nneed), kTB, 0, s>>>(c->need.p, nneed, c->seeds.p, c->needv.p));
-        row_offsets(c, c->needv.p, nneed, kCntAll, ns, ep);
-        MF_CUDA(cudaMemsetAsync(cnt + 35, 0, sizeof(int64_t), s));
-        MF_K(k_lb_mark_need<<<lb_grid(c, k_lb_mark_need), kTB, 0, s>>>(g, c->needv.p, c->lb_offs.p, nneed, ep, c->nmark.p,
-                                                       c->nlist_need.p, ucnt + 35));
-        MF_CUDA(cudaMemcpyAsync(h + 35, cnt + 35, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        MF_CUDA(cudaStreamSynchronize(s));
-        const int64_t nn = h[35];
-        if (nn > 0) {
-          first_hits(c, c->nlist_need.p, nn, HasCid{c->cid.p});
-          MF_K(k_f1_finish<<<grid_for(nn), kTB, 0, s>>>(g, c->nlist_need.p, nn, c->fpos.p, c->cid.p, c->f1.p));
-          first_hits(c, c->needv.p, nneed, HasF1{c->f1.p});
-          MF_K(k_need_decide<<<grid_for(nneed), kTB, 0, s>>>(g, c->need.p, c->needv.p, nneed, c->fpos.p, c->f1.p,
-                                                              c->rowcid.p, c->creates.p));
-        }
-      }
-    }
+    first_hits(c, c->live_v.p, ucnt + 33, rows, HasCid{c->cid.p});
+    MF_K(k_live_decide<<<lb_grid(c, k_live_decide), kTB, 0, s>>>(g, c->live_i.p, c->live_v.p, ucnt + 33, ns,
+                                                                 c->fpos.p, c->cid.p, c->rowcid.p, c->creates.p,
+                                                                 c->seeds.p, c->need.p, c->needv.p, ucnt + 34, mq));
+    MF_K(k_mark_need<<<lb_grid(c, k_mark_need), kTB, 0, s>>>(g, mq, ep, c->nmark.p, c->nlist_need.p, ucnt + 35));
+    first_hits(c, c->nlist_need.p, ucnt + 35, n, HasCid{c->cid.p});
+    MF_K(k_f1_finish<<<lb_grid(c, k_f1_finish), kTB, 0, s>>>(g, c->nlist_need.p, ucnt + 35, c->fpos.p, c->cid.p,
+                                                             c->f1.p));
+    first_hits(c, c->needv.p, ucnt + 34, ns, HasF1{c->f1.p});
+    MF_K(k_need_decide<<<lb_grid(c, k_need_decide), kTB, 0, s>>>(g, c->need.p, c->needv.p, ucnt + 34, c->fpos.p,
+                                                                 c->f1.p, c->rowcid.p, c->creates.p));
     scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
     MF_K(k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p));
     MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
