@@ -1743,6 +1743,144 @@ __global__ void k_spec_compact(const uint64_t* keys, const uint32_t* vals, const
   ovals[pos[k]] = vals[k];
 }
 
+// One CTA finishes a round whose pending positions fit kRoundCap (the common
+// case: a sub-batch has tens of processed edges).  It does, in order, what
+// k_spec_first_change, k_spec_count + scan + k_spec_fill, the sort,
+// k_spec_clear_flags, k_spec_commit, k_spec_keep_flags and k_spec_compact
+// do for larger rounds, with the writes in shared memory.  out[0] = first
+// changed position (cnt when none), out[1] = entries of the new view.
+constexpr int kRoundThreads = 1024;
+constexpr int kRoundCap = kRoundThreads;          // pending positions
+constexpr int kRoundWrites = 2 * kRoundCap;       // at most two writes per position
+
+// Exclusive block scan of one int per thread (blockDim.x == kRoundThreads).
+__device__ __forceinline__ int round_scan(int x, int* s_warp, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = x;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int w = s_warp[threadIdx.x];
+    int wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (threadIdx.x >= o) wi += y;
+    }
+    s_warp[threadIdx.x] = wi - w;
+    if (threadIdx.x == 31) s_warp[32] = wi;
+  }
+  __syncthreads();
+  const int r = s_warp[wid] + inc - x;
+  *total = s_warp[32];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kRoundThreads) k_spec_round(const int32_t* n0, const int32_t* n1, const int32_t* r0,
+                                                              const int32_t* r1, int64_t p0, int64_t cnt,
+                                                              const uint8_t* ins, int64_t p, const uint32_t* order,
+                                                              uint64_t* view_keys, uint32_t* view_vals,
+                                                              int64_t nview_old, uint8_t* m,
+                                                              unsigned long long* out) {
+  __shared__ uint64_t s_keys[kRoundWrites];
+  __shared__ uint32_t s_vals[kRoundWrites];
+  __shared__ int s_warp[33];
+  __shared__ unsigned long long s_f;
+  const int tid = threadIdx.x;
+  const int64_t pending = cnt - p0;
+  if (tid == 0) s_f = (unsigned long long)cnt;
+  __syncthreads();
+  // first changed position; this round's writes into shared memory
+  int32_t a = -1, b = -1;
+  const int64_t pos = p0 + tid;
+  if (tid < pending) {
+    a = n0[pos];
+    b = n1[pos];
+    if (a != r0[pos] || b != r1[pos]) atomicMin(&s_f, (unsigned long long)pos);
+  }
+  int nk = 0;
+  const int off = round_scan((a >= 0) + (b >= 0), s_warp, &nk);
+  if (tid < pending) {
+    int k = off;
+    if (a >= 0) {
+      s_keys[k] = ((uint64_t)(uint32_t)a << 32) | (uint64_t)pos;
+      s_vals[k] = ins[p + order[pos]] ? 0u : 1u;
+      ++k;
+    }
+    if (b >= 0) {
+      s_keys[k] = ((uint64_t)(uint32_t)b << 32) | (uint64_t)pos;
+      s_vals[k] = 1u;
+    }
+  }
+  // bitonic sort of the keys (with their values) over the next power of two
+  int np2 = 1;
+  while (np2 < nk) np2 <<= 1;
+  for (int k = nk + tid; k < np2; k += kRoundThreads) {
+    s_keys[k] = ~0ull;
+    s_vals[k] = 0u;
+  }
+  __syncthreads();
+  for (int size = 2; size <= np2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = tid; t < (np2 >> 1); t += kRoundThreads) {
+        const int lo = 2 * t - (t & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const uint64_t x = s_keys[lo], y = s_keys[hi];
+        if ((x > y) == up) {
+          s_keys[lo] = y;
+          s_keys[hi] = x;
+          const uint32_t vx = s_vals[lo];
+          s_vals[lo] = s_vals[hi];
+          s_vals[hi] = vx;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // the previous view's pending flags go
+  for (int64_t k = tid; k < nview_old; k += kRoundThreads) m[view_keys[k] >> 32] &= 1;
+  __syncthreads();
+  const unsigned long long f = s_f;
+  const uint64_t last = (uint64_t)min((int64_t)f, cnt - 1);
+  // commit every write at a position <= last that is the last such write to its vertex
+  for (int k = tid; k < nk; k += kRoundThreads) {
+    const uint64_t key = s_keys[k];
+    if ((key & 0xffffffffull) > last) continue;
+    if (k + 1 < nk) {
+      const uint64_t nx = s_keys[k + 1];
+      if ((nx >> 32) == (key >> 32) && (nx & 0xffffffffull) <= last) continue;
+    }
+    m[key >> 32] = (uint8_t)s_vals[k];
+  }
+  __syncthreads();
+  // writes after `last` become the next view (in key order) and flag their vertex
+  const int k0 = 2 * tid, k1 = 2 * tid + 1;
+  const bool keep0 = k0 < nk && (s_keys[k0] & 0xffffffffull) > last;
+  const bool keep1 = k1 < nk && (s_keys[k1] & 0xffffffffull) > last;
+  if (keep0) m[s_keys[k0] >> 32] |= 2;
+  if (keep1) m[s_keys[k1] >> 32] |= 2;
+  int nview = 0;
+  int w = round_scan((int)keep0 + (int)keep1, s_warp, &nview);
+  if (keep0) {
+    view_keys[w] = s_keys[k0];
+    view_vals[w] = s_vals[k0];
+    ++w;
+  }
+  if (keep1) {
+    view_keys[w] = s_keys[k1];
+    view_vals[w] = s_vals[k1];
+  }
+  if (tid == 0) {
+    out[0] = f;
+    out[1] = (unsigned long long)nview;
+  }
+}
+
 __global__ void k_clear(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, int32_t* cid,
                         int32_t* v2i) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2063,6 +2201,29 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     MF_K(k_big_scan<<<(unsigned)c->big_grid, kBigChunk, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
     MF_K(k_big_finalize<<<grid_for(pending), kTB, 0, s>>>(a, c->big_best.p));
     rsc.emplace(c, kStRepair);
+    if (pending <= kRoundCap) {
+      // small round: one CTA finishes it, one host round trip
+      MF_K(k_spec_round<<<1, kRoundThreads, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0, nproc, c->bins.p,
+                                                    p, order, c->rp_keys.p, c->rp_vals.p, nview, c->mis.p, ucnt + 20));
+      MF_CUDA(cudaMemcpyAsync(h + 20, c->counters.p + 20, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaStreamSynchronize(s));
+      const int64_t f = h[20];
+      if (debug_counters()) {
+        unsigned long long q[4];
+        MF_CUDA(cudaMemcpy(q, c->counters.p + 24, sizeof(q), cudaMemcpyDeviceToHost));
+        int64_t tot = 0;
+        if (q[0] > 0) MF_CUDA(cudaMemcpy(&tot, c->big_chunks.p + q[0], sizeof(tot), cudaMemcpyDeviceToHost));
+        dbg_big += (int64_t)q[0];
+        dbg_chunks += tot;
+        dbg_scanned += (int64_t)q[3];
+      }
+      if (f >= nproc) break;
+      nview = h[21];
+      std::swap(c->rp_w0, c->rp_n0);
+      std::swap(c->rp_w1, c->rp_n1);
+      p0 = f + 1;
+      continue;
+    }
     h[20] = (int64_t)nproc;
     MF_CUDA(cudaMemcpyAsync(c->counters.p + 20, h + 20, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     MF_K(k_spec_first_change<<<grid_for(pending), kTB, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0,
