@@ -122,7 +122,6 @@ void release_all(mf_ctx* c) {
                               &c->acnt_new, &c->seeds, &c->cands, &c->hlist, &c->touched, &c->rowcid};
   for (auto* b : b32) b->release();
   c->live.release();
-  c->hmark.release();
   c->bval.release();
   c->wval.release();
   c->bitmaps.release();
@@ -157,6 +156,8 @@ void release_all(mf_ctx* c) {
   c->seeds_all.release();
   for (auto* b : {&c->rq_idx, &c->rq_v, &c->mq_idx, &c->mq_v}) b->release();
   c->mq_base.release();
+  c->hbits.release();
+  c->bits_sums.release();
   c->n2cache.release();
   c->n2stamp.release();
   for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();
@@ -247,12 +248,12 @@ void run_batch(mf_ctx* c, int64_t m) {
   }
   if (c->profile) {
     // algorithmic bytes per stage from the device work counters:
-    //   hop1: 4 B row entry + 8 B mark read-modify-write per element
+    //   hop1: 4 B row entry + 4 B bitmap OR per element
     //   push: 4 B row entry + 8 B max read-modify-write per element, plus
     //         the cluster-id resolve pass: 4 B tag + 4 B id per vertex
     unsigned long long w[2 * mf::kStCount];
     MF_CUDA(cudaMemcpy(w, c->work.p, sizeof(w), cudaMemcpyDeviceToHost));
-    c->stage_bytes[mf::kStHop1] += 12.0 * (double)w[2 * mf::kStHop1];
+    c->stage_bytes[mf::kStHop1] += 8.0 * (double)w[2 * mf::kStHop1];
     c->stage_bytes[mf::kStPush] += 8.0 * (double)c->touched_total;
   }
 }

@@ -329,8 +329,7 @@ void scan_exclusive_i32(const int32_t* in, int64_t* out, int64_t n, Scratch& ws,
 void scan_exclusive_u8(const uint8_t* in, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s);
 // Packed scan of the hop-1 marks: high 32 bits count marked vertices, low 32
 // bits marked vertices that are not seed rows (v2i < 0).
-void scan_exclusive_marks(const uint32_t* hmark, const int32_t* v2i, uint32_t epoch, int64_t* out, int64_t n,
-                          Scratch& ws, cudaStream_t s);
+
 // Stable LSD radix sort of (key, value) on key bits [0, bits); result in keys/vals.
 void radix_sort_pairs(uint64_t* keys, uint32_t* vals, int64_t n, int bits, Scratch& ws, cudaStream_t s);
 
@@ -384,7 +383,7 @@ struct mf_ctx {
 
   mf::DBuf<uint8_t> mis;
   mf::DBuf<int32_t> cid, v2i;
-  mf::DBuf<uint32_t> hmark, bval, wval;
+  mf::DBuf<uint32_t> bval, wval;
   mf::DBuf<int32_t> f1;
   uint32_t epoch = 0;
 
@@ -435,6 +434,8 @@ struct mf_ctx {
   // first-hit chunk queue (rows) and the need seeds' chunk queue
   mf::DBuf<int32_t> rq_idx, rq_v, mq_idx, mq_v;
   mf::DBuf<int64_t> mq_base;
+  mf::DBuf<uint32_t> hbits;           // hop-1 and seed bitmaps of the current sub-batch
+  mf::DBuf<int64_t> bits_sums;        // their per-block counts
   mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
   mf::DBuf<uint32_t> n2stamp;          // batch stamp of each cached size
   uint32_t n2batch = 0;

@@ -390,7 +390,6 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   c->mis.reserve(n);
   c->cid.reserve(n);
   c->v2i.reserve(n);
-  c->hmark.reserve(n);
   c->bval.reserve(n);
   c->wval.reserve(n);
   c->f1.reserve(n);
@@ -405,7 +404,6 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   MF_CUDA(cudaMemsetAsync(c->mis.p, 0, (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->cid.p, 0xFF, sizeof(int32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->v2i.p, 0xFF, sizeof(int32_t) * (size_t)n, s));
-  MF_CUDA(cudaMemsetAsync(c->hmark.p, 0, sizeof(uint32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->bval.p, 0, sizeof(uint32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->wval.p, 0, sizeof(uint32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->nmark.p, 0, sizeof(uint32_t) * (size_t)n, s));

@@ -328,25 +328,6 @@ void scan_exclusive_u8(const uint8_t* in, int64_t* out, int64_t n, Scratch& ws, 
   scan_exclusive(Loader<uint8_t>{in}, out, n, ws, s);
 }
 
-namespace {
-// (hop-1 mark) << 32 | (hop-1 mark and not a seed row): both compactions of
-// the hop-1 set and of the candidates come out of one scan.
-struct MarkLoader {
-  const uint32_t* hmark;
-  const int32_t* v2i;
-  uint32_t epoch;
-  __device__ __forceinline__ int64_t operator()(int64_t i) const {
-    if (hmark[i] != epoch) return 0;
-    return ((int64_t)1 << 32) | (v2i[i] < 0 ? 1 : 0);
-  }
-};
-}  // namespace
-
-void scan_exclusive_marks(const uint32_t* hmark, const int32_t* v2i, uint32_t epoch, int64_t* out, int64_t n,
-                          Scratch& ws, cudaStream_t s) {
-  scan_exclusive(MarkLoader{hmark, v2i, epoch}, out, n, ws, s);
-}
-
 void radix_sort_pairs(uint64_t* keys, uint32_t* vals, int64_t n, int bits, Scratch& ws, cudaStream_t s) {
   if (n <= 1) return;
   if (n <= kSmallSort) {

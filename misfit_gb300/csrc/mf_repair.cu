@@ -216,39 +216,24 @@ __device__ __forceinline__ void add_work(unsigned long long* work, int64_t visit
   if ((threadIdx.x & 31) == 0 && visited) atomicAdd(work, (unsigned long long)visited);
 }
 
-__global__ void k_lb_mark_hop1(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t epoch,
-                               uint32_t* hmark, unsigned long long* work) {
-  const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t, int32_t, int32_t y) { hmark[y] = epoch; });
-  add_work(work, vis);
-}
+// ---- hop-1 set as a bitmap ----------------------------------------------------------
+// The hop-1 marks of a sub-batch go into a bitmap (hbits) and the seeds into
+// another (sbits); a two-level popcount scan over the words gives, per word,
+// the offsets of its marked vertices in hlist and of its marked non-seeds in
+// the candidate list, so both lists come out in ascending vertex id without
+// touching n-sized arrays.  Counts are packed as (hop-1 << 32) | candidates.
+constexpr int kBitsThreads = 256;
+constexpr int kBitsPerThread = 4;                               // words per thread
+constexpr int kBitsWords = kBitsThreads * kBitsPerThread;       // words per block
 
-// Both lists from the packed scan: hlist = marked vertices, cands = marked
-// vertices that are not seeds (ascending id, capped).
-__global__ void k_mark_compact(const uint32_t* hmark, const int64_t* pos, int32_t n, uint32_t epoch, int64_t cap,
-                               int64_t ns, int32_t* hlist, int32_t* cands, int32_t* v2i) {
-  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= n || hmark[x] != epoch) return;
-  const int64_t pk = pos[x];
-  hlist[pk >> 32] = (int32_t)x;
-  if (v2i[x] < 0) {
-    const int64_t k = pk & 0xffffffffll;
-    if (k < cap) {
-      cands[k] = (int32_t)x;
-      v2i[x] = (int32_t)(ns + k);
-    }
-  }
-}
-
-// ---- packed sizes ---------------------------------------------------------------
-
-// Upper bound of the packed element count: per seed 1 + len(s) + sum of
-// len(h) over row(s), capped by n; plus the candidate row lengths.  The sums
-// over row(s) use the load-balanced traversal (hub seeds have long rows).
-__global__ void k_lb_bound(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns,
-                           unsigned long long* uacc) {
+// One pass over the seed rows: the hop-1 bit of every element, and per seed
+// the sum of len(h) over row(s) for the packed-size upper bound (uacc).
+__global__ void k_lb_hop1_bound(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t* hbits,
+                                unsigned long long* uacc, unsigned long long* work) {
   int64_t cur = -1;
   unsigned long long acc = 0;
-  lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
+  const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
+    atomicOr(hbits + (y >> 5), 1u << (y & 31));
     if (i != cur) {
       if (cur >= 0 && acc) atomicAdd(uacc + cur, acc);
       cur = i;
@@ -257,8 +242,111 @@ __global__ void k_lb_bound(GraphView g, const int32_t* seeds, const int64_t* off
     acc += (unsigned long long)row_len(g, y);
   });
   if (cur >= 0 && acc) atomicAdd(uacc + cur, acc);
+  add_work(work, vis);
 }
 
+__global__ void k_seed_bits(const int32_t* seeds, int64_t ns, uint32_t* sbits) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ns) atomicOr(sbits + (seeds[i] >> 5), 1u << (seeds[i] & 31));
+}
+
+__device__ __forceinline__ int64_t bits_count4(const uint32_t* hbits, const uint32_t* sbits, int64_t w0,
+                                               int64_t words) {
+  int64_t h = 0, c = 0;
+  for (int j = 0; j < kBitsPerThread; ++j) {
+    const int64_t w = w0 + j;
+    if (w < words) {
+      const uint32_t m = hbits[w];
+      h += __popc(m);
+      c += __popc(m & ~sbits[w]);
+    }
+  }
+  return (h << 32) | c;
+}
+
+// Block-wide exclusive scan of one int64 per thread (kBitsThreads threads).
+__device__ __forceinline__ int64_t bits_block_scan(int64_t x, int64_t* s_warp, int64_t* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int64_t inc = x;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run = 0;
+    for (int w = 0; w < kBitsThreads / 32; ++w) { const int64_t y = s_warp[w]; s_warp[w] = run; run += y; }
+    s_warp[kBitsThreads / 32] = run;
+  }
+  __syncthreads();
+  const int64_t r = s_warp[wid] + inc - x;
+  *total = s_warp[kBitsThreads / 32];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kBitsThreads) k_bits_reduce(const uint32_t* hbits, const uint32_t* sbits,
+                                                              int64_t words, int64_t* block_sums) {
+  __shared__ int64_t s_warp[kBitsThreads / 32 + 1];
+  const int64_t w0 = (int64_t)blockIdx.x * kBitsWords + (int64_t)threadIdx.x * kBitsPerThread;
+  int64_t total = 0;
+  bits_block_scan(bits_count4(hbits, sbits, w0, words), s_warp, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of the block sums in place (one block; loops for any count);
+// the grand total goes to *total.
+__global__ void __launch_bounds__(kBitsThreads) k_bits_scan_sums(int64_t* block_sums, int64_t nblocks,
+                                                                 int64_t* total) {
+  __shared__ int64_t s_warp[kBitsThreads / 32 + 1];
+  int64_t carry = 0;
+  for (int64_t b0 = 0; b0 < nblocks; b0 += kBitsThreads) {
+    const int64_t b = b0 + threadIdx.x;
+    const int64_t x = b < nblocks ? block_sums[b] : 0;
+    int64_t t = 0;
+    const int64_t e = bits_block_scan(x, s_warp, &t);
+    if (b < nblocks) block_sums[b] = carry + e;
+    carry += t;
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kBitsThreads) k_bits_compact(const uint32_t* hbits, const uint32_t* sbits,
+                                                               int64_t words, const int64_t* block_offs, int64_t cap,
+                                                               int64_t ns, int32_t* hlist, int32_t* cands,
+                                                               int32_t* v2i) {
+  __shared__ int64_t s_warp[kBitsThreads / 32 + 1];
+  const int64_t w0 = (int64_t)blockIdx.x * kBitsWords + (int64_t)threadIdx.x * kBitsPerThread;
+  int64_t total = 0;
+  const int64_t off = block_offs[blockIdx.x] + bits_block_scan(bits_count4(hbits, sbits, w0, words), s_warp, &total);
+  int64_t ph = off >> 32, pc = off & 0xffffffffll;
+  for (int j = 0; j < kBitsPerThread; ++j) {
+    const int64_t w = w0 + j;
+    if (w >= words) break;
+    uint32_t m = hbits[w];
+    const uint32_t sm = sbits[w];
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const int32_t x = (int32_t)(w * 32 + b);
+      hlist[ph++] = x;
+      if (!((sm >> b) & 1u)) {
+        if (pc < cap) {
+          cands[pc] = x;
+          v2i[x] = (int32_t)(ns + pc);
+        }
+        ++pc;
+      }
+    }
+  }
+}
+
+// ---- packed sizes ---------------------------------------------------------------
+
+// Upper bound of the packed element count: per seed 1 + len(s) + sum of
+// len(h) over row(s), capped by n (the sums come from k_lb_hop1_bound); plus
+// the candidate row lengths.
 // The candidate count comes from the hop-1 compaction on the device (low 32
 // bits of *hop_counts, capped at capc), so the bound needs no host round trip
 // after the hop-1 stage.  Grid-stride over the ns + nct rows.
@@ -2111,7 +2199,6 @@ void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, 
 void next_epoch(mf_ctx* c) {
   if (c->epoch >= kMaxEpoch) {
     cudaStream_t s = c->stream;
-    MF_CUDA(cudaMemsetAsync(c->hmark.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
     MF_CUDA(cudaMemsetAsync(c->bval.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
     MF_CUDA(cudaMemsetAsync(c->wval.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
     MF_CUDA(cudaMemsetAsync(c->nmark.p, 0, sizeof(uint32_t) * (size_t)c->n, s));
@@ -2380,21 +2467,29 @@ void process_batch(mf_ctx* c, int64_t m) {
     next_epoch(c);
     const uint32_t ep = c->epoch;
     row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
-    MF_K(k_lb_mark_hop1<<<lb_grid(c, k_lb_mark_hop1), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->hmark.p,
-                                                   c->work.p + 2 * kStHop1));
-    scan_exclusive_marks(c->hmark.p, c->v2i.p, ep, c->i64a.p, n, c->ws, s);
+    const int64_t words = ((int64_t)n + 31) / 32;
+    const int64_t bblocks = (words + kBitsWords - 1) / kBitsWords;
+    c->hbits.reserve(std::max<int64_t>(2 * words, 1));
+    c->bits_sums.reserve(bblocks + 1);
+    uint32_t* hbits = c->hbits.p;
+    uint32_t* sbits = c->hbits.p + words;
+    MF_CUDA(cudaMemsetAsync(hbits, 0, sizeof(uint32_t) * (size_t)(2 * words), s));
+    c->uacc.reserve(std::max<int64_t>(ns, 1));
+    MF_CUDA(cudaMemsetAsync(c->uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), s));
+    MF_K(k_lb_hop1_bound<<<lb_grid(c, k_lb_hop1_bound), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, hbits, c->uacc.p,
+                                                                     c->work.p + 2 * kStHop1));
+    if (ns > 0) MF_K(k_seed_bits<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, sbits));
     const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
-    MF_K(k_mark_compact<<<grid_for(n), kTB, 0, s>>>(c->hmark.p, c->i64a.p, n, ep, capc, ns, c->hlist.p, c->cands.p,
-                                                    c->v2i.p));
+    MF_K(k_bits_reduce<<<(unsigned)bblocks, kBitsThreads, 0, s>>>(hbits, sbits, words, c->bits_sums.p));
+    // packed counts (hop-1 << 32 | candidates) at i64a[n], where the size bound reads them
+    MF_K(k_bits_scan_sums<<<1, kBitsThreads, 0, s>>>(c->bits_sums.p, bblocks, c->i64a.p + n));
+    MF_K(k_bits_compact<<<(unsigned)bblocks, kBitsThreads, 0, s>>>(hbits, sbits, words, c->bits_sums.p, capc, ns,
+                                                                   c->hlist.p, c->cands.p, c->v2i.p));
 
     // ---- packed sizes (upper bound) and MAX_CSR_ELEMENTS growth; one host
     // round trip for the hop-1 counts and the bound
     sc.emplace(c, kStSizes);
     MF_CUDA(cudaMemsetAsync(cnt + 4, 0, sizeof(int64_t), s));
-    c->uacc.reserve(std::max<int64_t>(ns, 1));
-    MF_CUDA(cudaMemsetAsync(c->uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), s));
-    row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
-    MF_K(k_lb_bound<<<lb_grid(c, k_lb_bound), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, c->uacc.p));
     MF_K(k_bound_finish<<<lb_grid(c, k_bound_finish), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, c->i64a.p + n,
                                                                    capc, c->uacc.p, c->n2cache.p, c->n2stamp.p,
                                                                    c->n2batch, ucnt + 4));
