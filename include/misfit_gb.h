@@ -205,8 +205,10 @@ void mf_free(void* p);
 #define MF_NUM_STAGES 13
 /* Name of stage i (0 <= i < MF_NUM_STAGES), NULL otherwise. */
 const char* mf_stage_name(int stage);
-/* When on, every later batch records CUDA events around each stage on the
- * context's stream; times accumulate until mf_profile_reset. */
+/* on = 1: every later batch records CUDA events around each stage on the
+ * context's stream; times accumulate until mf_profile_reset.  on = 2: only
+ * the k_lb_push_hop launches are timed (the "push_hop" stage), which costs
+ * four event records per sub-batch instead of about fifty.  on = 0: off. */
 int mf_profile_enable(mf_ctx* ctx, int on);
 int mf_profile_reset(mf_ctx* ctx);
 /* Accumulated device milliseconds, occurrences and algorithmic bytes per

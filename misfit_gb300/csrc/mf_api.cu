@@ -160,6 +160,8 @@ void release_all(mf_ctx* c) {
   c->bits_sums.release();
   c->n2cache.release();
   c->n2stamp.release();
+  c->n2bound.release();
+  c->n2bstamp.release();
   for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();
   for (auto* b : {&c->un_idx, &c->un_v, &c->need, &c->needv, &c->live_i, &c->live_v, &c->nlist_need}) b->release();
   c->nmark.release();
@@ -827,8 +829,8 @@ const char* mf_stage_name(int stage) {
 
 int mf_profile_enable(mf_ctx* c, int on) {
   return guarded([&] {
-    need(c != nullptr, MF_EINVAL, "null context");
-    c->profile = on != 0;
+    need(c != nullptr && on >= 0 && on <= 2, MF_EINVAL, "bad arguments");
+    c->profile = on;
   });
 }
 

@@ -438,6 +438,8 @@ struct mf_ctx {
   mf::DBuf<int64_t> bits_sums;        // their per-block counts
   mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
   mf::DBuf<uint32_t> n2stamp;          // batch stamp of each cached size
+  mf::DBuf<int64_t> n2bound;           // tighter upper bounds of this batch's 2-hop sizes
+  mf::DBuf<uint32_t> n2bstamp;         // batch stamp of each cached bound
   uint32_t n2batch = 0;
   mf::DBuf<int32_t> dense_idx, dense_hl, pair_d, pair_h, todo;
   mf::DBuf<unsigned long long> fpos;   // first-hit positions
@@ -454,7 +456,7 @@ struct mf_ctx {
   std::vector<SubBatchTrace> traces;
 
   // optional per-stage CUDA-event profiling
-  bool profile = false;
+  int profile = 0;                     // 0 off, 1 all stages, 2 the push_hop stage only
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<std::pair<int, size_t>> ev_marks;
@@ -483,7 +485,8 @@ struct StageScope {
   int stage;
   size_t first = 0;
   bool on;
-  StageScope(mf_ctx* ctx, int st) : c(ctx), stage(st), on(ctx->profile) {
+  StageScope(mf_ctx* ctx, int st)
+      : c(ctx), stage(st), on(ctx->profile == 1 || (ctx->profile == 2 && st == kStPushHop)) {
     if (!on) return;
     if (c->ev_used + 2 > c->ev_pool.size()) {
       for (int k = 0; k < 64; ++k) {

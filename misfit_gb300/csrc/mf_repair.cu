@@ -223,7 +223,7 @@ __device__ __forceinline__ void add_work(unsigned long long* work, int64_t visit
 // the candidate list, so both lists come out in ascending vertex id without
 // touching n-sized arrays.  Counts are packed as (hop-1 << 32) | candidates.
 constexpr int kBitsThreads = 256;
-constexpr int kBitsPerThread = 4;                               // words per thread
+constexpr int kBitsPerThread = 1;                               // words per thread
 constexpr int kBitsWords = kBitsThreads * kBitsPerThread;       // words per block
 
 // One pass over the seed rows: the hop-1 bit of every element, and per seed
@@ -352,8 +352,8 @@ __global__ void __launch_bounds__(kBitsThreads) k_bits_compact(const uint32_t* h
 // after the hop-1 stage.  Grid-stride over the ns + nct rows.
 __global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, const int32_t* cands,
                                const int64_t* hop_counts, int64_t capc, const unsigned long long* uacc,
-                               const int64_t* n2cache, const uint32_t* n2stamp, uint32_t stamp,
-                               unsigned long long* out) {
+                               const int64_t* n2cache, const uint32_t* n2stamp, const int64_t* n2bound,
+                               const uint32_t* n2bstamp, uint32_t stamp, unsigned long long* out) {
   const int64_t nct = min((int64_t)(*hop_counts & 0xffffffffll), capc);
   const int64_t rows = ns + nct;
   unsigned long long b = 0;
@@ -362,6 +362,8 @@ __global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, co
       const int32_t s = seeds[i];
       if (n2stamp[s] == stamp) {
         b += (unsigned long long)n2cache[s];   // exact size known from an earlier sub-batch
+      } else if (n2bstamp[s] == stamp) {
+        b += (unsigned long long)n2bound[s];   // tighter bound known from an earlier sub-batch
       } else {
         unsigned long long e = 1ull + (unsigned long long)row_len(g, s) + uacc[i];
         if (e > (unsigned long long)g.n) e = (unsigned long long)g.n;
@@ -377,12 +379,15 @@ __global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, co
 
 // Seeds whose exact size is cached for this batch take it; the others are
 // listed for computation.
+// With bounds (the tighter-bound pass), a cached bound also counts as known.
 __global__ void k_exact_todo(const int32_t* seeds, int64_t ns, const int64_t* n2cache, const uint32_t* n2stamp,
-                             uint32_t stamp, int64_t* lens, int32_t* todo, unsigned long long* cnt) {
+                             const int64_t* n2bound, const uint32_t* n2bstamp, bool bounds, uint32_t stamp,
+                             int64_t* lens, int32_t* todo, unsigned long long* cnt) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ns) return;
   const int32_t s = seeds[i];
   if (n2stamp[s] == stamp) lens[i] = n2cache[s];
+  else if (bounds && n2bstamp[s] == stamp) lens[i] = n2bound[s];
   else todo[atomicAdd(cnt, 1ull)] = (int32_t)i;
 }
 
@@ -2050,7 +2055,7 @@ void debug_push_hop(mf_ctx* c, const unsigned long long* counter, unsigned long 
 
 // Exact 2-hop list sizes of the seeds into c->rowlens[0..ns).
 // With bound_only, dense seeds get an upper bound (k_dense_bound) instead of
-// their exact size and nothing is cached.
+// their exact size, and the results go to the bound cache.
 void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
   cudaStream_t s = c->stream;
   const int32_t n = c->n;
@@ -2113,8 +2118,8 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
   c->pair_h.reserve(pcap);
   c->todo.reserve(3 * ns);
   MF_CUDA(cudaMemsetAsync(c->counters.p + 44, 0, sizeof(int64_t), s));
-  MF_K(k_exact_todo<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, c->n2cache.p, c->n2stamp.p, c->n2batch,
-                                                 c->rowlens.p, c->todo.p,
+  MF_K(k_exact_todo<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, c->n2cache.p, c->n2stamp.p, c->n2bound.p,
+                                                 c->n2bstamp.p, bound_only, c->n2batch, c->rowlens.p, c->todo.p,
                                                  reinterpret_cast<unsigned long long*>(c->counters.p) + 44));
   MF_CUDA(cudaMemcpyAsync(h + 44, c->counters.p + 44, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   MF_CUDA(cudaStreamSynchronize(s));
@@ -2167,9 +2172,10 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
     std::swap(todo, todo_next);
     ntodo = left;
   }
-  if (nnew > 0 && !bound_only)
-    MF_K(k_exact_store<<<grid_for(nnew), kTB, 0, s>>>(c->seeds.p, computed, nnew, c->rowlens.p, c->n2cache.p,
-                                                      c->n2stamp.p, c->n2batch));
+  if (nnew > 0)
+    MF_K(k_exact_store<<<grid_for(nnew), kTB, 0, s>>>(c->seeds.p, computed, nnew, c->rowlens.p,
+                                                      bound_only ? c->n2bound.p : c->n2cache.p,
+                                                      bound_only ? c->n2bstamp.p : c->n2stamp.p, c->n2batch));
   MF_CUDA(cudaGetLastError());
 }
 
@@ -2393,8 +2399,11 @@ void process_batch(mf_ctx* c, int64_t m) {
   // exact 2-hop sizes stay valid for the rows of this batch only
   c->n2cache.reserve(std::max<int32_t>(n, 1));
   c->n2stamp.reserve(std::max<int32_t>(n, 1));
+  c->n2bound.reserve(std::max<int32_t>(n, 1));
+  c->n2bstamp.reserve(std::max<int32_t>(n, 1));
   if (c->n2batch == 0 || c->n2batch == 0xffffffffu) {
     MF_CUDA(cudaMemsetAsync(c->n2stamp.p, 0, sizeof(uint32_t) * (size_t)std::max<int32_t>(n, 1), s));
+    MF_CUDA(cudaMemsetAsync(c->n2bstamp.p, 0, sizeof(uint32_t) * (size_t)std::max<int32_t>(n, 1), s));
     c->n2batch = 0;
   }
   ++c->n2batch;
@@ -2492,7 +2501,8 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_CUDA(cudaMemsetAsync(cnt + 4, 0, sizeof(int64_t), s));
     MF_K(k_bound_finish<<<lb_grid(c, k_bound_finish), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, c->i64a.p + n,
                                                                    capc, c->uacc.p, c->n2cache.p, c->n2stamp.p,
-                                                                   c->n2batch, ucnt + 4));
+                                                                   c->n2bound.p, c->n2bstamp.p, c->n2batch,
+                                                                   ucnt + 4));
     MF_CUDA(cudaMemcpyAsync(h + 2, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));

@@ -263,7 +263,9 @@ class Graph:
         _check(_lib().mf_compact(self._h, os.fsencode(path), 1 if rebase else 0), "mf_compact")
 
     def profile(self, on=True):
-        _check(_lib().mf_profile_enable(self._h, 1 if on else 0), "mf_profile_enable")
+        """True/1: all stages; 2: the k_lb_push_hop launches only; False/0: off."""
+        level = 1 if on is True else (0 if on is False else int(on))
+        _check(_lib().mf_profile_enable(self._h, level), "mf_profile_enable")
 
     def profile_reset(self):
         _check(_lib().mf_profile_reset(self._h), "mf_profile_reset")
