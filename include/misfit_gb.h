@@ -231,6 +231,57 @@ int mf_trace_enable(mf_ctx* ctx, int on);
 int mf_trace_count(mf_ctx* ctx, int64_t* count);
 int mf_trace_get(mf_ctx* ctx, int64_t index, int field, void* out, int64_t cap, int64_t* len);
 
+/* ---- serving pool (no counterpart in the reference) -------------------------
+ *
+ * The reference runs one graph per process.  A pool keeps many graphs on one
+ * GPU and serves update batches as they arrive:
+ *   - batches for one graph run in submission order, one at a time; batches
+ *     of different graphs run concurrently, each graph on its own stream,
+ *     driven by one of the pool's host worker threads;
+ *   - admission is by HBM budget: before a graph runs, idle resident graphs
+ *     are evicted, least recently used first, to pinned host memory until it
+ *     fits (a graph whose batch is running is never evicted; when every
+ *     resident graph is running the new one is admitted over budget and
+ *     counted in over_budget);
+ *   - eviction saves the graph's state exactly (base CSR, overlay with its
+ *     tombstone positions and insertion order, membership, cluster ids), so
+ *     every batch result equals the one a dedicated context gives. */
+typedef struct mf_pool mf_pool;
+
+typedef struct mf_pool_stats {
+  int64_t graphs;               /* graphs added */
+  int64_t completed;            /* batches completed */
+  int64_t updates;              /* update lines in the completed batches */
+  int64_t errors;               /* batches or moves that failed */
+  int64_t evictions;            /* graphs moved to pinned host memory */
+  int64_t restores;             /* graphs moved back to the device */
+  int64_t over_budget;          /* admissions made while over the budget */
+  int64_t resident_bytes;       /* device bytes of the resident graphs now */
+  int64_t peak_resident_bytes;  /* the largest value seen */
+} mf_pool_stats;
+
+/* A pool on device `gpu` that keeps at most `hbm_budget` bytes of graph state
+ * and scratch resident, with `workers` host threads (1..64). */
+int mf_pool_create(int gpu, int64_t hbm_budget, int workers, mf_pool** out);
+/* Waits for the running batches, then frees everything. */
+int mf_pool_destroy(mf_pool* pool);
+/* Adds a graph from an in-memory CSR (nindex n+1 entries; copied) with its
+ * initial membership (n bytes, 0/1); *gid receives its id. */
+int mf_pool_add_graph(mf_pool* pool, int32_t n, const int64_t* nindex, const int32_t* nlist, const uint8_t* mis,
+                      int32_t* gid);
+/* Queues one batch (arrays copied; same meaning as mf_apply_batch) and
+ * returns at once; *rid identifies the request. */
+int mf_pool_submit(mf_pool* pool, int32_t gid, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m,
+                   int64_t* rid);
+/* Waits for request rid; returns its status and, in *latency_ms, the time
+ * from submission to completion.  Each request is waited for once. */
+int mf_pool_wait(mf_pool* pool, int64_t rid, double* latency_ms);
+/* Waits until no batch is queued or running. */
+int mf_pool_drain(mf_pool* pool);
+/* Membership of graph gid after its queued batches (n bytes). */
+int mf_pool_get_mis(mf_pool* pool, int32_t gid, uint8_t* out, int64_t n);
+int mf_pool_stats_get(mf_pool* pool, mf_pool_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,12 @@ const char* const kStageNames[kStCount] = {"overlay", "split",  "seeds", "hop1",
                                            "push_hop"};
 
 void set_error(const std::string& msg) { g_error = msg; }
+
+void bind_device(const mf_ctx* c) { MF_CUDA(cudaSetDevice(c->device)); }
+
+double now_ms_host() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 const char* get_error() { return g_error.c_str(); }
 
 }  // namespace mf
@@ -115,62 +121,7 @@ void need(bool cond, int status, const char* msg) {
 }
 
 void release_all(mf_ctx* c) {
-  mf::DBuf<int64_t>* b64[] = {&c->nindex, &c->aoff, &c->aoff_alt, &c->i64a, &c->i64b, &c->rowlens, &c->counters};
-  for (auto* b : b64) b->release();
-  mf::DBuf<int32_t>* b32[] = {&c->nlist, &c->dead, &c->rcnt, &c->deg, &c->aadj, &c->aown, &c->aadj_alt, &c->aown_alt,
-                              &c->cid, &c->v2i, &c->f1, &c->bu, &c->bv, &c->prev, &c->i32a, &c->i32b, &c->i32c,
-                              &c->acnt_new, &c->seeds, &c->cands, &c->hlist, &c->touched, &c->rowcid};
-  for (auto* b : b32) b->release();
-  c->live.release();
-  c->bval.release();
-  c->wval.release();
-  c->bitmaps.release();
-  c->mis.release();
-  c->bins.release();
-  c->u8a.release();
-  c->akill.release();
-  c->creates.release();
-  c->keys.release();
-  c->vals.release();
-  c->app_keys.release();
-  c->app_vals.release();
-  for (auto* b : {&c->rp_w0, &c->rp_w1, &c->rp_n0, &c->rp_n1}) b->release();
-  c->rp_keys.release();
-  c->rp_keys2.release();
-  c->rp_vals.release();
-  c->rp_vals2.release();
-  c->rp_u8.release();
-  c->rp_pos.release();
-  c->work.release();
-  c->uacc.release();
-  c->heavy_slot.release();
-  c->heavy_list.release();
-  c->heavy_bits.release();
-  c->fpos.release();
-  c->dense_bits.release();
-  c->dense_light.release();
-  c->pull_long.release();
-  c->ncbits.release();
-  for (auto* b : {&c->plan_cuts, &c->plan_ests, &c->plan_send, &c->plan_pos}) b->release();
-  c->plan_flags.release();
-  c->seeds_all.release();
-  for (auto* b : {&c->rq_idx, &c->rq_v, &c->mq_idx, &c->mq_v}) b->release();
-  c->mq_base.release();
-  c->hbits.release();
-  c->bits_sums.release();
-  c->n2cache.release();
-  c->n2stamp.release();
-  c->n2bound.release();
-  c->n2bstamp.release();
-  for (auto* b : {&c->dense_idx, &c->dense_hl, &c->pair_d, &c->pair_h, &c->todo}) b->release();
-  for (auto* b : {&c->un_idx, &c->un_v, &c->need, &c->needv, &c->live_i, &c->live_v, &c->nlist_need}) b->release();
-  c->nmark.release();
-  c->un_cnt.release();
-  c->lb_offs.release();
-  for (auto* b : {&c->big_pos, &c->big_off, &c->big_nr, &c->big_chunks, &c->big_pre}) b->release();
-  c->big_r.release();
-  c->big_best.release();
-  c->ws.release();
+  mf::release_device_state(c);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   c->h_counters = nullptr;
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);

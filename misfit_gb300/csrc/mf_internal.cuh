@@ -480,6 +480,64 @@ struct mf_ctx {
 
 namespace mf {
 // Records a start/end event pair around a stage when profiling is on.
+// Calls f(buf) for every device buffer a context owns (graph state,
+// per-batch and per-sub-batch scratch, primitive workspace).
+template <class F>
+void for_each_buffer(mf_ctx* c, F&& f) {
+  f(c->nindex); f(c->aoff); f(c->aoff_alt); f(c->i64a); f(c->i64b); f(c->rowlens); f(c->rp_pos);
+  f(c->big_pos); f(c->big_off); f(c->big_nr); f(c->big_chunks); f(c->big_pre); f(c->dense_light);
+  f(c->plan_cuts); f(c->plan_ests); f(c->plan_send); f(c->plan_pos); f(c->mq_base); f(c->bits_sums);
+  f(c->n2cache); f(c->n2bound); f(c->un_cnt); f(c->counters); f(c->lb_offs);
+  f(c->nlist); f(c->dead); f(c->rcnt); f(c->deg); f(c->aadj); f(c->aown); f(c->aadj_alt); f(c->aown_alt);
+  f(c->cid); f(c->v2i); f(c->f1); f(c->bu); f(c->bv); f(c->prev); f(c->i32a); f(c->i32b); f(c->i32c);
+  f(c->acnt_new); f(c->seeds); f(c->cands); f(c->hlist); f(c->touched); f(c->rowcid);
+  f(c->rp_w0); f(c->rp_w1); f(c->rp_n0); f(c->rp_n1); f(c->big_r); f(c->heavy_slot); f(c->heavy_list);
+  f(c->pull_long); f(c->seeds_all); f(c->rq_idx); f(c->rq_v); f(c->mq_idx); f(c->mq_v);
+  f(c->dense_idx); f(c->dense_hl); f(c->pair_d); f(c->pair_h); f(c->todo);
+  f(c->un_idx); f(c->un_v); f(c->need); f(c->needv); f(c->live_i); f(c->live_v); f(c->nlist_need);
+  f(c->live); f(c->bval); f(c->wval); f(c->vals); f(c->app_vals); f(c->rp_vals); f(c->rp_vals2);
+  f(c->bitmaps); f(c->heavy_bits); f(c->dense_bits); f(c->ncbits); f(c->hbits); f(c->n2stamp);
+  f(c->n2bstamp); f(c->nmark);
+  f(c->mis); f(c->bins); f(c->u8a); f(c->akill); f(c->creates); f(c->rp_u8); f(c->plan_flags);
+  f(c->keys); f(c->app_keys); f(c->rp_keys); f(c->rp_keys2);
+  f(c->big_best); f(c->fpos); f(c->work); f(c->uacc);
+  f(c->ws.block_sums); f(c->ws.block_sums2); f(c->ws.hist); f(c->ws.hist_scan); f(c->ws.keys_alt);
+  f(c->ws.vals_alt);
+}
+
+// Device bytes a context holds now.
+inline int64_t ctx_device_bytes(mf_ctx* c) {
+  int64_t total = 0;
+  for_each_buffer(c, [&](auto& b) { total += b.cap * (int64_t)sizeof(*b.p); });
+  return total;
+}
+
+// Frees every device buffer (the stream, events and pinned counters stay) and
+// resets the state that lives in them, so that the next use re-creates it.
+inline void release_device_state(mf_ctx* c) {
+  for_each_buffer(c, [](auto& b) { b.release(); });
+  c->bitmap_ctas = 0;
+  c->bitmap_words = 0;
+  c->heavy_cap = 0;
+  c->heavy_used = 0;
+  c->epoch = 0;
+  c->n2batch = 0;
+}
+
+// Pinned host copy of a graph's state (see mf_pool.cu).
+struct PinnedSnapshot {
+  uint8_t* host = nullptr;
+  size_t cap = 0, used = 0;
+  std::vector<std::pair<size_t, size_t>> parts;  // (offset, bytes) per saved buffer
+};
+
+int64_t snapshot_bytes(const mf_ctx* c);
+void evict(mf_ctx* c, PinnedSnapshot& snap);        // device -> pinned host, then frees the device buffers
+void restore(mf_ctx* c, const PinnedSnapshot& snap);
+void alloc_vertex_scratch(mf_ctx* c);              // n-sized scratch with its initial values (mf_overlay.cu)
+void bind_device(const mf_ctx* c);                 // cudaSetDevice(c->device)
+double now_ms_host();
+
 struct StageScope {
   mf_ctx* c;
   int stage;

@@ -386,30 +386,15 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   c->rcnt.reserve(n);
   c->deg.reserve(n);
   c->aoff.reserve((int64_t)n + 1);
-  c->aoff_alt.reserve((int64_t)n + 1);
   c->mis.reserve(n);
   c->cid.reserve(n);
-  c->v2i.reserve(n);
-  c->bval.reserve(n);
-  c->wval.reserve(n);
-  c->f1.reserve(n);
-  c->nmark.reserve(n);
-  c->nlist_need.reserve(n);
-  c->touched.reserve(n);
-  c->hlist.reserve(n);
-  c->acnt_new.reserve(n);
   MF_CUDA(cudaMemsetAsync(c->dead.p, 0, sizeof(int32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->rcnt.p, 0, sizeof(int32_t) * (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->aoff.p, 0, sizeof(int64_t) * ((size_t)n + 1), s));
   MF_CUDA(cudaMemsetAsync(c->mis.p, 0, (size_t)n, s));
   MF_CUDA(cudaMemsetAsync(c->cid.p, 0xFF, sizeof(int32_t) * (size_t)n, s));
-  MF_CUDA(cudaMemsetAsync(c->v2i.p, 0xFF, sizeof(int32_t) * (size_t)n, s));
-  MF_CUDA(cudaMemsetAsync(c->bval.p, 0, sizeof(uint32_t) * (size_t)n, s));
-  MF_CUDA(cudaMemsetAsync(c->wval.p, 0, sizeof(uint32_t) * (size_t)n, s));
-  MF_CUDA(cudaMemsetAsync(c->nmark.p, 0, sizeof(uint32_t) * (size_t)n, s));
   c->a_total = 0;
-  c->epoch = 0;
-  c->counters.reserve(64);
+  alloc_vertex_scratch(c);
   if (n > 0) {
     MF_K(k_base_degree<<<grid_for(n), kTB, 0, s>>>(c->nindex.p, n, c->deg.p));
   }
@@ -452,6 +437,31 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
     c->symmetric = true;
   }
   c->max_csr = initial_max_csr(n, c->header_edges);
+}
+
+// The n-sized scratch with its initial values: no row mapped (v2i = -1),
+// epoch-tagged arrays at epoch 0, plus the device counters.
+void alloc_vertex_scratch(mf_ctx* c) {
+  cudaStream_t s = c->stream;
+  const int32_t n = c->n;
+  c->aoff_alt.reserve((int64_t)n + 1);
+  c->v2i.reserve(n);
+  c->bval.reserve(n);
+  c->wval.reserve(n);
+  c->f1.reserve(n);
+  c->nmark.reserve(n);
+  c->nlist_need.reserve(n);
+  c->touched.reserve(n);
+  c->hlist.reserve(n);
+  c->acnt_new.reserve(n);
+  if (n > 0) {
+    MF_CUDA(cudaMemsetAsync(c->v2i.p, 0xFF, sizeof(int32_t) * (size_t)n, s));
+    MF_CUDA(cudaMemsetAsync(c->bval.p, 0, sizeof(uint32_t) * (size_t)n, s));
+    MF_CUDA(cudaMemsetAsync(c->wval.p, 0, sizeof(uint32_t) * (size_t)n, s));
+    MF_CUDA(cudaMemsetAsync(c->nmark.p, 0, sizeof(uint32_t) * (size_t)n, s));
+  }
+  c->epoch = 0;
+  c->counters.reserve(64);
 }
 
 void flag_updates(mf_ctx* c, int64_t m) {

@@ -1,0 +1,444 @@
+// mf_pool.cu -- the serving form: many resident graphs, continuous admission.
+//
+// No counterpart in the reference, which processes one graph per process.
+// A pool owns graph contexts on one GPU and a set of host worker threads:
+//   * every graph keeps its base CSR, delta overlay, membership and cluster
+//     ids; batches submitted for a graph run in submission order, one at a
+//     time, while batches of different graphs run concurrently on their own
+//     CUDA streams (one worker thread drives one graph's batch);
+//   * admission is by HBM budget: before a graph runs, idle resident graphs
+//     are evicted least-recently-used first until its footprint fits;
+//   * eviction copies the graph's state to pinned host memory and frees all
+//     of its device buffers; restore copies it back.  The state is restored
+//     bit for bit (tombstone positions and added-entry order decide later
+//     rows), so a graph's results do not depend on how often it moved.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "mf_internal.cuh"
+
+namespace mf {
+
+namespace {
+
+template <class T>
+void save(PinnedSnapshot& snap, const DBuf<T>& b, int64_t count, cudaStream_t s) {
+  const size_t bytes = sizeof(T) * (size_t)count;
+  snap.parts.push_back({snap.used, bytes});
+  if (bytes > 0) MF_CUDA(cudaMemcpyAsync(snap.host + snap.used, b.p, bytes, cudaMemcpyDeviceToHost, s));
+  snap.used += (bytes + 255) & ~(size_t)255;
+}
+
+template <class T>
+void load(const PinnedSnapshot& snap, size_t& part, DBuf<T>& b, int64_t count, cudaStream_t s) {
+  b.reserve(std::max<int64_t>(count, 1));
+  const auto& pr = snap.parts[part++];
+  if (pr.second > 0) MF_CUDA(cudaMemcpyAsync(b.p, snap.host + pr.first, pr.second, cudaMemcpyHostToDevice, s));
+}
+
+}  // namespace
+
+int64_t snapshot_bytes(const mf_ctx* c) {
+  const int64_t n = c->n, words = (c->nnz + 31) / 32;
+  auto r = [](int64_t b) { return (b + 255) & ~(int64_t)255; };
+  return r(8 * (n + 1)) + r(4 * c->nnz) + r(4 * words) + 3 * r(4 * n) + r(8 * (n + 1)) + 2 * r(4 * c->a_total) +
+         r(n) + r(4 * n);
+}
+
+void evict(mf_ctx* c, PinnedSnapshot& snap) {
+  cudaStream_t s = c->stream;
+  MF_CUDA(cudaStreamSynchronize(s));
+  const size_t need = (size_t)snapshot_bytes(c);
+  if (snap.cap < need) {
+    if (snap.host) cudaFreeHost(snap.host);
+    snap.host = nullptr;
+    snap.cap = 0;
+    MF_CUDA(cudaMallocHost(&snap.host, need));
+    snap.cap = need;
+  }
+  snap.used = 0;
+  snap.parts.clear();
+  const int64_t n = c->n, words = (c->nnz + 31) / 32;
+  save(snap, c->nindex, n + 1, s);
+  save(snap, c->nlist, c->nnz, s);
+  save(snap, c->live, words, s);
+  save(snap, c->dead, n, s);
+  save(snap, c->rcnt, n, s);
+  save(snap, c->deg, n, s);
+  save(snap, c->aoff, n + 1, s);
+  save(snap, c->aadj, c->a_total, s);
+  save(snap, c->aown, c->a_total, s);
+  save(snap, c->mis, n, s);
+  save(snap, c->cid, n, s);
+  MF_CUDA(cudaStreamSynchronize(s));
+  release_device_state(c);
+}
+
+void restore(mf_ctx* c, const PinnedSnapshot& snap) {
+  cudaStream_t s = c->stream;
+  const int64_t n = c->n, words = (c->nnz + 31) / 32;
+  size_t part = 0;
+  load(snap, part, c->nindex, n + 1, s);
+  load(snap, part, c->nlist, c->nnz, s);
+  load(snap, part, c->live, words, s);
+  load(snap, part, c->dead, n, s);
+  load(snap, part, c->rcnt, n, s);
+  load(snap, part, c->deg, n, s);
+  load(snap, part, c->aoff, n + 1, s);
+  load(snap, part, c->aadj, c->a_total, s);
+  load(snap, part, c->aown, c->a_total, s);
+  load(snap, part, c->mis, n, s);
+  load(snap, part, c->cid, n, s);
+  alloc_vertex_scratch(c);
+  MF_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace mf
+
+// ---- the pool -------------------------------------------------------------------
+
+namespace {
+
+struct Request {
+  int64_t rid = 0;
+  int32_t gid = 0;
+  std::vector<int32_t> u, v;
+  std::vector<uint8_t> ins;
+  double t_submit = 0, t_start = 0, t_done = 0;
+  int status = MF_OK;
+  std::string error;
+  bool done = false;
+};
+
+struct Graph {
+  mf_ctx* ctx = nullptr;
+  bool resident = false;
+  bool busy = false;           // a worker runs its batch, or it is being moved
+  mf::PinnedSnapshot snap;
+  int64_t bytes = 0;           // device bytes when last resident
+  uint64_t last_use = 0;
+  std::deque<Request*> queue;  // in submission order
+};
+
+}  // namespace
+
+struct mf_pool {
+  int device = 0;
+  int64_t budget = 0;
+  std::deque<Graph> graphs;    // a deque: references stay valid while graphs are added
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<int32_t> ready;   // graphs with queued batches and no running one
+  std::unordered_map<int64_t, Request*> reqs;
+  std::vector<std::thread> workers;
+  bool stop = false;
+  int64_t next_rid = 1;
+  uint64_t tick = 0;
+  int64_t resident_bytes = 0;
+  mf_pool_stats st{};
+
+  // Makes room for `need` bytes by evicting idle resident graphs, least
+  // recently used first.  Called with the lock held; evictions run with the
+  // lock released (the victims are marked busy meanwhile).
+  void make_room(std::unique_lock<std::mutex>& lk, int64_t need, int32_t self) {
+    while (resident_bytes + need > budget) {
+      int32_t victim = -1;
+      for (int32_t g = 0; g < (int32_t)graphs.size(); ++g) {
+        const Graph& gr = graphs[(size_t)g];
+        if (g == self || !gr.resident || gr.busy) continue;
+        if (victim < 0 || (gr.queue.empty() && !graphs[(size_t)victim].queue.empty()) ||
+            (gr.queue.empty() == graphs[(size_t)victim].queue.empty() && gr.last_use < graphs[(size_t)victim].last_use))
+          victim = g;
+      }
+      if (victim < 0) {
+        st.over_budget += 1;  // every resident graph is running: admit anyway
+        return;
+      }
+      Graph& v = graphs[(size_t)victim];
+      v.busy = true;
+      lk.unlock();
+      int status = MF_OK;
+      try {
+        mf::bind_device(v.ctx);
+        v.bytes = mf::ctx_device_bytes(v.ctx);
+        mf::evict(v.ctx, v.snap);
+      } catch (const mf::Failure& f) {
+        status = f.status;
+      }
+      lk.lock();
+      v.busy = false;
+      if (status == MF_OK) {
+        v.resident = false;
+        resident_bytes -= v.bytes;
+        st.evictions += 1;
+      } else {
+        st.errors += 1;
+      }
+      if (!v.queue.empty()) {
+        ready.push_back(victim);
+        cv_work.notify_one();
+      }
+    }
+  }
+
+  void worker() {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    while (true) {
+      cv_work.wait(lk, [&] { return stop || !ready.empty(); });
+      if (stop && ready.empty()) return;
+      const int32_t gid = ready.front();
+      ready.pop_front();
+      Graph& gr = graphs[(size_t)gid];
+      if (gr.busy || gr.queue.empty()) continue;
+      gr.busy = true;
+      Request* rq = gr.queue.front();
+      int status = MF_OK;
+      std::string err;
+      if (!gr.resident) {
+        make_room(lk, gr.bytes, gid);
+        lk.unlock();
+        try {
+          mf::bind_device(gr.ctx);
+          mf::restore(gr.ctx, gr.snap);
+        } catch (const mf::Failure& f) {
+          status = f.status;
+          err = mf_last_error();
+        }
+        lk.lock();
+        if (status == MF_OK) {
+          gr.resident = true;
+          resident_bytes += gr.bytes;
+          st.restores += 1;
+        }
+      }
+      rq->t_start = mf::now_ms_host();
+      lk.unlock();
+      if (status == MF_OK) {
+        status = mf_apply_batch(gr.ctx, rq->u.data(), rq->v.data(), rq->ins.data(), (int64_t)rq->u.size());
+        if (status != MF_OK) err = mf_last_error();
+      }
+      const int64_t bytes = status == MF_OK ? mf::ctx_device_bytes(gr.ctx) : gr.bytes;
+      lk.lock();
+      rq->t_done = mf::now_ms_host();
+      rq->status = status;
+      rq->error = err;
+      rq->done = true;
+      resident_bytes += bytes - gr.bytes;
+      gr.bytes = bytes;
+      gr.queue.pop_front();
+      gr.busy = false;
+      gr.last_use = ++tick;
+      st.completed += 1;
+      st.updates += (int64_t)rq->u.size();
+      if (status != MF_OK) st.errors += 1;
+      st.resident_bytes = resident_bytes;
+      st.peak_resident_bytes = std::max(st.peak_resident_bytes, resident_bytes);
+      if (!gr.queue.empty()) {
+        ready.push_back(gid);
+        cv_work.notify_one();
+      }
+      cv_done.notify_all();
+    }
+  }
+};
+
+namespace {
+
+template <class F>
+int pool_guarded(F&& f) {
+  try {
+    mf::set_error("");
+    f();
+    return MF_OK;
+  } catch (const mf::Failure& e) {
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    mf::set_error("host allocation failed");
+    return MF_ENOMEM;
+  } catch (const std::exception& e) {
+    mf::set_error(e.what());
+    return MF_EINVAL;
+  }
+}
+
+void need_arg(bool cond, const char* msg) {
+  if (!cond) MF_FAIL(MF_EINVAL, msg);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mf_pool_create(int gpu, int64_t hbm_budget, int workers, mf_pool** out) {
+  return pool_guarded([&] {
+    need_arg(out != nullptr && hbm_budget > 0 && workers >= 1 && workers <= 64, "bad arguments");
+    int count = 0;
+    MF_CUDA(cudaGetDeviceCount(&count));
+    need_arg(gpu >= 0 && gpu < count, "gpu id out of range");
+    mf_pool* p = new mf_pool();
+    p->device = gpu;
+    p->budget = hbm_budget;
+    for (int i = 0; i < workers; ++i) p->workers.emplace_back([p] { p->worker(); });
+    *out = p;
+  });
+}
+
+int mf_pool_destroy(mf_pool* p) {
+  return pool_guarded([&] {
+    need_arg(p != nullptr, "null pool");
+    {
+      std::lock_guard<std::mutex> lk(p->mu);
+      p->stop = true;
+    }
+    p->cv_work.notify_all();
+    for (auto& t : p->workers) t.join();
+    for (auto& gr : p->graphs) {
+      if (gr.ctx) mf_close(gr.ctx);
+      if (gr.snap.host) cudaFreeHost(gr.snap.host);
+    }
+    for (auto& kv : p->reqs) delete kv.second;  // every request not yet waited for, queued ones included
+    delete p;
+  });
+}
+
+int mf_pool_add_graph(mf_pool* p, int32_t n, const int64_t* nindex, const int32_t* nlist, const uint8_t* mis,
+                      int32_t* gid) {
+  return pool_guarded([&] {
+    need_arg(p && gid && n > 0 && nindex && mis, "bad arguments");
+    mf_ctx* c = nullptr;
+    int st = mf_open_csr(n, nindex, nlist, p->device, &c);
+    if (st != MF_OK) throw mf::Failure{st};
+    st = mf_set_mis(c, mis, n);
+    if (st != MF_OK) {
+      mf_close(c);
+      throw mf::Failure{st};
+    }
+    std::unique_lock<std::mutex> lk(p->mu);
+    Graph gr;
+    gr.ctx = c;
+    gr.resident = true;
+    gr.bytes = mf::ctx_device_bytes(c);
+    gr.last_use = ++p->tick;
+    p->graphs.push_back(std::move(gr));
+    const int32_t id = (int32_t)p->graphs.size() - 1;
+    p->resident_bytes += p->graphs.back().bytes;
+    // over budget: the new graph waits on the host until its first batch
+    if (p->resident_bytes > p->budget) {
+      Graph& me = p->graphs.back();
+      me.busy = true;
+      p->resident_bytes -= me.bytes;
+      lk.unlock();
+      mf::bind_device(c);
+      mf::evict(c, me.snap);
+      lk.lock();
+      me.resident = false;
+      me.busy = false;
+      p->st.evictions += 1;
+      if (!me.queue.empty()) {
+        p->ready.push_back(id);
+        p->cv_work.notify_one();
+      }
+    }
+    p->st.graphs = (int64_t)p->graphs.size();
+    p->st.resident_bytes = p->resident_bytes;
+    p->st.peak_resident_bytes = std::max(p->st.peak_resident_bytes, p->resident_bytes);
+    *gid = id;
+  });
+}
+
+int mf_pool_submit(mf_pool* p, int32_t gid, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m,
+                   int64_t* rid) {
+  return pool_guarded([&] {
+    need_arg(p && rid && m >= 0 && (m == 0 || (u && v && ins)), "bad arguments");
+    Request* r = new Request();
+    r->u.assign(u, u + m);
+    r->v.assign(v, v + m);
+    r->ins.assign(ins, ins + m);
+    r->t_submit = mf::now_ms_host();
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (gid < 0 || gid >= (int32_t)p->graphs.size()) {
+      delete r;
+      MF_FAIL(MF_EINVAL, "unknown graph id");
+    }
+    r->gid = gid;
+    r->rid = p->next_rid++;
+    Graph& gr = p->graphs[(size_t)gid];
+    gr.queue.push_back(r);
+    p->reqs[r->rid] = r;
+    if (gr.queue.size() == 1 && !gr.busy) {
+      p->ready.push_back(gid);
+      p->cv_work.notify_one();
+    }
+    *rid = r->rid;
+  });
+}
+
+int mf_pool_wait(mf_pool* p, int64_t rid, double* latency_ms) {
+  int status = MF_OK;
+  std::string err;
+  const int st = pool_guarded([&] {
+    need_arg(p != nullptr, "null pool");
+    std::unique_lock<std::mutex> lk(p->mu);
+    auto it = p->reqs.find(rid);
+    if (it == p->reqs.end()) MF_FAIL(MF_EINVAL, "unknown request id");
+    Request* r = it->second;
+    p->cv_done.wait(lk, [&] { return r->done; });
+    if (latency_ms) *latency_ms = r->t_done - r->t_submit;
+    status = r->status;
+    err = r->error;
+    p->reqs.erase(it);
+    delete r;
+  });
+  if (st != MF_OK) return st;
+  if (status != MF_OK) mf::set_error(err);
+  return status;
+}
+
+int mf_pool_drain(mf_pool* p) {
+  return pool_guarded([&] {
+    need_arg(p != nullptr, "null pool");
+    std::unique_lock<std::mutex> lk(p->mu);
+    p->cv_done.wait(lk, [&] {
+      for (const auto& gr : p->graphs)
+        if (!gr.queue.empty() || gr.busy) return false;
+      return true;
+    });
+  });
+}
+
+int mf_pool_get_mis(mf_pool* p, int32_t gid, uint8_t* out, int64_t n) {
+  return pool_guarded([&] {
+    need_arg(p && out, "bad arguments");
+    std::unique_lock<std::mutex> lk(p->mu);
+    need_arg(gid >= 0 && gid < (int32_t)p->graphs.size(), "unknown graph id");
+    Graph& gr = p->graphs[(size_t)gid];
+    p->cv_done.wait(lk, [&] { return gr.queue.empty() && !gr.busy; });
+    need_arg(n == gr.ctx->n, "output must have n entries");
+    if (gr.resident) {
+      const int st = mf_get_mis(gr.ctx, out, n);
+      if (st != MF_OK) throw mf::Failure{st};
+    } else {
+      // membership is the tenth saved part (see mf::evict)
+      const auto& pr = gr.snap.parts[9];
+      std::copy(gr.snap.host + pr.first, gr.snap.host + pr.first + pr.second, out);
+    }
+  });
+}
+
+int mf_pool_stats_get(mf_pool* p, mf_pool_stats* out) {
+  return pool_guarded([&] {
+    need_arg(p && out, "bad arguments");
+    std::lock_guard<std::mutex> lk(p->mu);
+    *out = p->st;
+    out->resident_bytes = p->resident_bytes;
+  });
+}
+
+}  // extern "C"

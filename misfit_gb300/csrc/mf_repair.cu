@@ -1677,18 +1677,29 @@ __global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_
     const int64_t nr = a.big_nr[i];
     const int64_t vol = pre[nr];
     const int32_t r = a.big_r[i];
-    if (threadIdx.x == 0) {
-      s_best = ~0ull;
-      s_nu = 0;
-      s_live = (unsigned long long)p0 < best[i] ? 1 : 0;  // an earlier chunk may have answered already
-      if (s_live) {
-        atomicAdd(queue + 1, 1ull);                       // chunks scanned (the rest were skipped)
-        int64_t klo = 0, khi = nr;                        // last k with pre[k] <= p0
-        while (khi - klo > 1) {
-          const int64_t mid = (klo + khi) >> 1;
-          if (pre[mid] <= p0) klo = mid; else khi = mid;
-        }
-        s_k0 = klo;
+    if (wid == 0) {
+      // warp 0: skip test, then the last k with pre[k] <= p0 by a 32-way
+      // search (each step samples 32 prefix entries and keeps the interval
+      // around the boundary, so a hub row of 10^6 entries takes 4 steps)
+      int live = 0;
+      if (lane == 0) live = (unsigned long long)p0 < best[i] ? 1 : 0;  // an earlier chunk may have answered
+      live = __shfl_sync(0xffffffffu, live, 0);
+      int64_t lo = 0, hi = nr;  // pre[lo] <= p0 < pre[hi]
+      while (live && hi - lo > 1) {
+        const int64_t step = (hi - lo + 31) / 32;
+        const int64_t idx = lo + (int64_t)lane * step;
+        const unsigned m = __ballot_sync(0xffffffffu, idx < hi && pre[idx] <= p0);
+        const int top = 31 - __clz(m);
+        const int64_t nlo = lo + (int64_t)top * step;
+        hi = min(nlo + step, hi);
+        lo = nlo;
+      }
+      if (lane == 0) {
+        s_best = ~0ull;
+        s_nu = 0;
+        s_live = live;
+        s_k0 = lo;
+        if (live) atomicAdd(queue + 1, 1ull);  // chunks scanned (the rest were skipped)
       }
     }
     __syncthreads();

@@ -23,6 +23,8 @@ EXPORTS = [
     "mf_write_mis_file", "mf_read_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
     "mf_trace_count", "mf_trace_get", "mf_stage_name", "mf_profile_enable", "mf_profile_reset",
     "mf_profile_read", "mf_kernel_launches",
+    "mf_pool_create", "mf_pool_destroy", "mf_pool_add_graph", "mf_pool_submit", "mf_pool_wait", "mf_pool_drain",
+    "mf_pool_get_mis", "mf_pool_stats_get",
 ]
 
 
@@ -32,6 +34,17 @@ class BatchStats(C.Structure):
         ("candidates", C.c_int64), ("clusters", C.c_int64), ("processed_edges", C.c_int64),
         ("exact_sizes", C.c_int64), ("max_csr", C.c_int64), ("repair_rounds", C.c_int64),
         ("device_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PoolStats(C.Structure):
+    _fields_ = [
+        ("graphs", C.c_int64), ("completed", C.c_int64), ("updates", C.c_int64), ("errors", C.c_int64),
+        ("evictions", C.c_int64), ("restores", C.c_int64), ("over_budget", C.c_int64),
+        ("resident_bytes", C.c_int64), ("peak_resident_bytes", C.c_int64),
     ]
 
     def as_dict(self):
@@ -102,6 +115,14 @@ def _lib():
         "mf_trace_enable": (C.c_int, [_P, C.c_int]),
         "mf_trace_count": (C.c_int, [_P, _I64P]),
         "mf_trace_get": (C.c_int, [_P, C.c_int64, C.c_int, C.c_void_p, C.c_int64, _I64P]),
+        "mf_pool_create": (C.c_int, [C.c_int, C.c_int64, C.c_int, C.POINTER(_P)]),
+        "mf_pool_destroy": (C.c_int, [_P]),
+        "mf_pool_add_graph": (C.c_int, [_P, C.c_int32, _I64P, _I32P, _U8P, _I32P]),
+        "mf_pool_submit": (C.c_int, [_P, C.c_int32, _I32P, _I32P, _U8P, C.c_int64, _I64P]),
+        "mf_pool_wait": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_double)]),
+        "mf_pool_drain": (C.c_int, [_P]),
+        "mf_pool_get_mis": (C.c_int, [_P, C.c_int32, _U8P, C.c_int64]),
+        "mf_pool_stats_get": (C.c_int, [_P, C.POINTER(PoolStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -347,3 +368,62 @@ def list_batch_files(folder):
     finally:
         _lib().mf_free(names)
     return [x for x in s.split("\n") if x]
+
+
+class Pool:
+    """A serving pool (mf_pool): many graphs on one GPU, batches served by
+    host worker threads under an HBM budget, idle graphs evicted to pinned
+    host memory."""
+
+    def __init__(self, hbm_budget, workers=4, gpu=0):
+        h = C.c_void_p()
+        _check(_lib().mf_pool_create(gpu, int(hbm_budget), int(workers), C.byref(h)), "mf_pool_create")
+        self._h = h
+        self._n = {}
+
+    def add_graph(self, nindex, nlist, mis):
+        nindex = np.ascontiguousarray(nindex, dtype=np.int64)
+        nlist = np.ascontiguousarray(nlist, dtype=np.int32)
+        mis = _u8(mis)
+        gid = C.c_int32()
+        n = nindex.size - 1
+        _check(_lib().mf_pool_add_graph(self._h, n, _ptr(nindex, C.c_int64), _ptr(nlist, C.c_int32),
+                                        _ptr(mis, C.c_uint8), C.byref(gid)), "mf_pool_add_graph")
+        self._n[gid.value] = n
+        return gid.value
+
+    def submit(self, gid, u, v, ins):
+        u, v, ins = _i32(u), _i32(v), _u8(ins)
+        rid = C.c_int64()
+        _check(_lib().mf_pool_submit(self._h, gid, _ptr(u, C.c_int32), _ptr(v, C.c_int32), _ptr(ins, C.c_uint8),
+                                     u.size, C.byref(rid)), "mf_pool_submit")
+        return rid.value
+
+    def wait(self, rid):
+        lat = C.c_double()
+        _check(_lib().mf_pool_wait(self._h, rid, C.byref(lat)), "mf_pool_wait")
+        return lat.value
+
+    def drain(self):
+        _check(_lib().mf_pool_drain(self._h), "mf_pool_drain")
+
+    def get_mis(self, gid):
+        out = np.zeros(self._n[gid], dtype=np.uint8)
+        _check(_lib().mf_pool_get_mis(self._h, gid, _ptr(out, C.c_uint8), out.size), "mf_pool_get_mis")
+        return out
+
+    def stats(self):
+        st = PoolStats()
+        _check(_lib().mf_pool_stats_get(self._h, C.byref(st)), "mf_pool_stats_get")
+        return st.as_dict()
+
+    def close(self):
+        if self._h:
+            _check(_lib().mf_pool_destroy(self._h), "mf_pool_destroy")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

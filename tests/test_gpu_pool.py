@@ -1,0 +1,101 @@
+"""Serving pool (mf_pool_*) through the C-ABI: every graph's membership after
+its batches must equal the one a dedicated context gives ("alone"), while the
+pool runs the graphs' batches concurrently under an HBM budget that forces
+evictions to pinned host memory and restores ("in the mix").  Membership is
+bytes: comparisons are exact."""
+import numpy as np
+import pytest
+
+from misfit_gb300 import native
+from misfit_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _graphs(count, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(rng.integers(2000, 20000))
+        if k % 2 == 0:
+            nindex, nlist = W.er_graph(n, float(rng.uniform(4, 12)), seed + k)
+        else:
+            nindex, nlist = W.rgg_graph(n, float(rng.uniform(4, 16)), seed + k)
+        out.append((nindex, nlist))
+    return out
+
+
+def _streams(graphs, nbatches, seed):
+    """Per graph: initial MIS, its batches with flags, the membership a
+    dedicated context has after each batch."""
+    plans = []
+    for k, (nindex, nlist) in enumerate(graphs):
+        n = nindex.size - 1
+        g = native.Graph.from_csr(nindex, nlist)
+        try:
+            mis0 = g.greedy_mis()
+            g.set_mis(mis0)
+            ts = W.ToggleStream(n, nindex, nlist, seed + 17 * k)
+            batches, after = [], []
+            for b in range(nbatches):
+                u, v = ts.next_batch(int(np.random.default_rng(seed + k + b).integers(10, 3000)))
+                ins = g.flag_updates(u, v)
+                g.apply_batch(u, v, ins)
+                batches.append((u, v, ins))
+                after.append(g.get_mis())
+        finally:
+            g.close()
+        plans.append((mis0, batches, after))
+    return plans
+
+
+def test_pool_matches_dedicated_contexts_under_eviction(gpu_lib):
+    graphs = _graphs(12, 5)
+    plans = _streams(graphs, 3, 100)
+    # a budget that holds only a few of the graphs at once (a graph's device
+    # footprint is ~100-200 B per vertex plus ~8 B per entry)
+    budget = int(3 * max((ni.size - 1) * 200 + nl.size * 8 for ni, nl in graphs))
+    with native.Pool(budget, workers=4) as pool:
+        gids = [pool.add_graph(ni, nl, plans[k][0]) for k, (ni, nl) in enumerate(graphs)]
+        rids = []
+        for b in range(3):                       # interleaved: batch b of every graph
+            for k, gid in enumerate(gids):
+                u, v, ins = plans[k][1][b]
+                rids.append(pool.submit(gid, u, v, ins))
+        lat = [pool.wait(r) for r in rids]
+        assert all(x >= 0 for x in lat)
+        for k, gid in enumerate(gids):
+            assert np.array_equal(pool.get_mis(gid), plans[k][2][-1]), k
+        st = pool.stats()
+    assert st["completed"] == 3 * len(graphs)
+    assert st["errors"] == 0
+    assert st["evictions"] > 0 and st["restores"] > 0
+
+
+def test_pool_one_graph_batch_by_batch(gpu_lib):
+    """Waiting for each batch before the next: the membership after every
+    batch equals the dedicated context's."""
+    graphs = _graphs(3, 9)
+    plans = _streams(graphs, 4, 300)
+    with native.Pool(1 << 34, workers=2) as pool:
+        gids = [pool.add_graph(ni, nl, plans[k][0]) for k, (ni, nl) in enumerate(graphs)]
+        for b in range(4):
+            for k, gid in enumerate(gids):
+                u, v, ins = plans[k][1][b]
+                pool.wait(pool.submit(gid, u, v, ins))
+                assert np.array_equal(pool.get_mis(gid), plans[k][2][b]), (k, b)
+
+
+def test_pool_errors(gpu_lib):
+    with native.Pool(1 << 30, workers=1) as pool:
+        ni, nl = W.er_graph(500, 4, 3)
+        gid = pool.add_graph(ni, nl, np.zeros(500, np.uint8))
+        with pytest.raises(native.MisfitError):
+            pool.submit(gid + 5, np.array([0], np.int32), np.array([1], np.int32), np.array([1], np.uint8))
+        # a bad batch fails on its own request; the pool keeps serving
+        bad = pool.submit(gid, np.array([0, 3], np.int32), np.array([0, 4], np.int32), np.array([1, 1], np.uint8))
+        with pytest.raises(native.MisfitError):
+            pool.wait(bad)
+        ok = pool.submit(gid, np.array([0], np.int32), np.array([1], np.int32), np.array([1], np.uint8))
+        pool.wait(ok)
+        assert pool.stats()["errors"] == 1
