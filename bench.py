@@ -61,6 +61,12 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-served", action="store_true", help="skip the served and batched legs")
+    ap.add_argument("--served-graphs", type=int, default=64)
+    ap.add_argument("--served-requests", type=int, default=300)
+    ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrivals per second")
+    ap.add_argument("--served-workers", type=int, default=8)
+    ap.add_argument("--served-budget", type=float, default=0.6, help="HBM budget as a fraction of the footprint")
     return ap.parse_args()
 
 
@@ -202,6 +208,146 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+# ---- served and batched forms (many graphs on one GPU) ------------------------------
+
+def graph_set(count, nmin, nmax, seed):
+    """2-D random geometric graphs with log-uniform vertex counts in [nmin,
+    nmax] and mean degree uniform in 4..32, one seed per graph."""
+    from misfit_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        nindex, nlist = W.rgg_graph(n, float(rng.uniform(4, 32)), seed * 1000 + k)
+        out.append((n, nindex, nlist))
+    return out
+
+
+def initial_mis(graphs):
+    from misfit_gb300 import native
+    mis = []
+    for n, nindex, nlist in graphs:
+        g = native.Graph.from_csr(nindex, nlist)
+        mis.append(g.greedy_mis())
+        g.close()
+    return mis
+
+
+def plain_loop(graphs, mis0, reqs):
+    """One dedicated context per graph, requests applied one after another in
+    arrival order (waiting for each arrival).  Returns (updates/s, latencies
+    ms, final memberships)."""
+    from misfit_gb300 import native
+    ctxs = []
+    for (n, nindex, nlist), m in zip(graphs, mis0):
+        g = native.Graph.from_csr(nindex, nlist)
+        g.set_mis(m)
+        ctxs.append(g)
+    lat = []
+    t0 = time.perf_counter()
+    for t, gid, u, v, ins in reqs:
+        wait = t - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        ctxs[gid].apply_batch(u, v, ins)
+        lat.append((time.perf_counter() - t0 - t) * 1e3)
+    span = time.perf_counter() - t0
+    out = [c.get_mis() for c in ctxs]
+    for c in ctxs:
+        c.close()
+    updates = sum(int(r[2].size) for r in reqs)
+    return updates / span, lat, out
+
+
+def pooled(graphs, mis0, reqs, workers, budget_frac):
+    """The same requests through a serving pool: submitted at their arrival
+    times, served by `workers` threads under budget_frac of the graphs' HBM
+    footprint.  Returns (updates/s, latencies ms, memberships, pool stats)."""
+    from misfit_gb300 import native
+    pool = native.Pool(1 << 40, workers=workers)
+    gids = [pool.add_graph(nindex, nlist, m) for (n, nindex, nlist), m in zip(graphs, mis0)]
+    footprint = pool.stats()["resident_bytes"]
+    pool.set_budget(max(1, int(footprint * budget_frac)))
+    rids = []
+    t0 = time.perf_counter()
+    for t, gid, u, v, ins in reqs:
+        wait = t - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        rids.append(pool.submit(gids[gid], u, v, ins))
+    lat = [pool.wait(r) for r in rids]
+    span = time.perf_counter() - t0
+    out = [pool.get_mis(g) for g in gids]
+    st = pool.stats()
+    st["footprint_bytes"] = footprint
+    pool.close()
+    updates = sum(int(r[2].size) for r in reqs)
+    return updates / span, lat, out, st
+
+
+def run_served(args, graphs, mis0):
+    """Serving form at reduced scale: graphs drawn as in the batched form,
+    requests arriving as a Poisson stream, each one batch of log-uniform
+    10..20,000 toggles to a graph chosen Zipf(1.1), endpoints uniform,
+    preferential or low-degree (1/3 each).  Compared with the plain
+    sequential loop on the same requests."""
+    from misfit_gb300 import workloads as W
+    rng = np.random.default_rng(11)
+    streams = [W.ToggleStream(n, ni, nl, 500 + k) for k, (n, ni, nl) in enumerate(graphs)]
+    zipf = np.arange(1, len(graphs) + 1, dtype=np.float64) ** -1.1
+    zipf /= zipf.sum()
+    modes = ["uniform", "preferential", "low_degree"]
+    reqs, t = [], 0.0
+    for _ in range(args.served_requests):
+        t += float(rng.exponential(1.0 / args.served_rate))
+        gid = int(rng.choice(len(graphs), p=zipf))
+        size = int(round(np.exp(rng.uniform(np.log(10), np.log(20000)))))
+        u, v, ins = streams[gid].next_batch(size, endpoints=modes[int(rng.integers(3))], with_flags=True)
+        reqs.append((t, gid, u, v, ins))
+    p_rate, p_lat, p_mis = plain_loop(graphs, mis0, reqs)
+    s_rate, s_lat, s_mis, st = pooled(graphs, mis0, reqs, args.served_workers, args.served_budget)
+    same = all(np.array_equal(a, b) for a, b in zip(p_mis, s_mis))
+    return {
+        "workload": "%d RGGs (n log-uniform 1e3..2e5, mean degree 4..32); %d requests, Poisson %.0f/s, "
+                    "batches log-uniform 10..20000 toggles, graph Zipf(1.1), endpoints uniform/preferential/"
+                    "low-degree" % (len(graphs), len(reqs), args.served_rate),
+        "value": s_rate, "unit": UNIT, "p50_ms": float(np.percentile(s_lat, 50)),
+        "p99_ms": float(np.percentile(s_lat, 99)), "workers": args.served_workers,
+        "hbm_budget_fraction": args.served_budget, "evictions": st["evictions"], "restores": st["restores"],
+        "scratch_trims": st["trims"], "over_budget_admissions": st["over_budget"],
+        "footprint_bytes": st["footprint_bytes"], "peak_resident_bytes": st["peak_resident_bytes"],
+        "plain_loop": {"value": p_rate, "unit": UNIT, "p50_ms": float(np.percentile(p_lat, 50)),
+                       "p99_ms": float(np.percentile(p_lat, 99))},
+        "identical_to_plain_loop": bool(same), "timing": "host wall clock, host buffers in and out",
+    }
+
+
+def run_batched(args, graphs, mis0):
+    """Batched form at reduced scale: independent graphs, one batch each
+    (log-uniform 10..50,000 toggles, low-degree and uniform endpoints 50/50),
+    all submitted at once to a pool with room for every graph, against the
+    plain per-graph loop.  Same graphs as the served form, from their initial
+    state."""
+    from misfit_gb300 import workloads as W
+    rng = np.random.default_rng(12)
+    reqs = []
+    for k, (n, ni, nl) in enumerate(graphs):
+        ts = W.ToggleStream(n, ni, nl, 900 + k)
+        size = int(round(np.exp(rng.uniform(np.log(10), np.log(50000)))))
+        mode = "low_degree" if k % 2 == 0 else "uniform"
+        u, v, ins = ts.next_batch(size, endpoints=mode, with_flags=True)
+        reqs.append((0.0, k, u, v, ins))
+    p_rate, _, p_mis = plain_loop(graphs, mis0, reqs)
+    s_rate, _, s_mis, st = pooled(graphs, mis0, reqs, args.served_workers, 1.0)
+    same = all(np.array_equal(a, b) for a, b in zip(p_mis, s_mis))
+    return {
+        "workload": "%d RGGs (n log-uniform 1e3..2e5), one batch each of log-uniform 10..50000 toggles" % len(graphs),
+        "value": s_rate, "unit": UNIT, "workers": args.served_workers,
+        "plain_loop": {"value": p_rate, "unit": UNIT},
+        "identical_to_plain_loop": bool(same), "timing": "host wall clock, host buffers in and out",
+    }
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -336,9 +482,14 @@ def main():
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": "oracle on the first %d lines of batch 1 from the initial state "
                                           "(%.1f s)" % (lines, spent)}
+    g.close()
+    if rank == 0 and not args.no_served:
+        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        mis0 = initial_mis(graphs)
+        line["served"] = run_served(args, graphs, mis0)
+        line["batched"] = run_batched(args, graphs, mis0)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    g.close()
     dist_barrier()
 
 

@@ -238,11 +238,12 @@ int mf_trace_get(mf_ctx* ctx, int64_t index, int field, void* out, int64_t cap, 
  *   - batches for one graph run in submission order, one at a time; batches
  *     of different graphs run concurrently, each graph on its own stream,
  *     driven by one of the pool's host worker threads;
- *   - admission is by HBM budget: before a graph runs, idle resident graphs
- *     are evicted, least recently used first, to pinned host memory until it
- *     fits (a graph whose batch is running is never evicted; when every
- *     resident graph is running the new one is admitted over budget and
- *     counted in over_budget);
+ *   - admission is by HBM budget, checked before a graph runs and after each
+ *     batch: idle resident graphs, least recently used first, first give up
+ *     their per-batch scratch and are then evicted to pinned host memory
+ *     until the resident graphs fit (a graph whose batch is running is never
+ *     touched; when every resident graph is running the new one is admitted
+ *     over budget and counted in over_budget);
  *   - eviction saves the graph's state exactly (base CSR, overlay with its
  *     tombstone positions and insertion order, membership, cluster ids), so
  *     every batch result equals the one a dedicated context gives. */
@@ -255,6 +256,7 @@ typedef struct mf_pool_stats {
   int64_t errors;               /* batches or moves that failed */
   int64_t evictions;            /* graphs moved to pinned host memory */
   int64_t restores;             /* graphs moved back to the device */
+  int64_t trims;                /* idle graphs that gave up their per-batch scratch */
   int64_t over_budget;          /* admissions made while over the budget */
   int64_t resident_bytes;       /* device bytes of the resident graphs now */
   int64_t peak_resident_bytes;  /* the largest value seen */
@@ -281,6 +283,8 @@ int mf_pool_drain(mf_pool* pool);
 /* Membership of graph gid after its queued batches (n bytes). */
 int mf_pool_get_mis(mf_pool* pool, int32_t gid, uint8_t* out, int64_t n);
 int mf_pool_stats_get(mf_pool* pool, mf_pool_stats* out);
+/* Changes the budget; it applies from the next admission on. */
+int mf_pool_set_budget(mf_pool* pool, int64_t hbm_budget);
 
 #ifdef __cplusplus
 }

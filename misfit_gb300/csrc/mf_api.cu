@@ -27,6 +27,7 @@ thread_local std::string g_error;
 }
 
 std::atomic<long long> g_launches{0};
+thread_local cudaStream_t g_alloc_stream = nullptr;
 
 namespace {
 struct KTimes {
@@ -86,7 +87,10 @@ const char* const kStageNames[kStCount] = {"overlay", "split",  "seeds", "hop1",
 
 void set_error(const std::string& msg) { g_error = msg; }
 
-void bind_device(const mf_ctx* c) { MF_CUDA(cudaSetDevice(c->device)); }
+void bind_device(const mf_ctx* c) {
+  MF_CUDA(cudaSetDevice(c->device));
+  g_alloc_stream = c->stream;
+}
 
 double now_ms_host() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -99,8 +103,13 @@ namespace {
 
 using mf::Failure;
 
+// Runs an entry point: exceptions become status codes, and the thread's
+// allocation stream (set by bind) does not outlive the call.
 template <class F>
 int guarded(F&& f) {
+  struct ClearStream {
+    ~ClearStream() { mf::g_alloc_stream = nullptr; }
+  } clear;
   try {
     mf::set_error("");
     f();
@@ -141,6 +150,13 @@ mf_ctx* new_ctx(int gpu) {
   c->device = gpu;
   try {
     MF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    mf::g_alloc_stream = c->stream;
+    // keep freed stream-ordered memory in this process's pool for reuse
+    cudaMemPool_t mp;
+    if (cudaDeviceGetDefaultMemPool(&mp, gpu) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     MF_CUDA(cudaEventCreate(&c->ev0));
     MF_CUDA(cudaEventCreate(&c->ev1));
     MF_CUDA(cudaMallocHost(&c->h_counters, sizeof(int64_t) * 64));
@@ -153,7 +169,10 @@ mf_ctx* new_ctx(int gpu) {
   return c;
 }
 
-void bind(const mf_ctx* c) { MF_CUDA(cudaSetDevice(c->device)); }
+void bind(const mf_ctx* c) {
+  MF_CUDA(cudaSetDevice(c->device));
+  mf::g_alloc_stream = c->stream;
+}
 
 // Inputs of a batch are already in c->bu / c->bv / c->bins.
 void run_batch(mf_ctx* c, int64_t m) {
@@ -422,6 +441,7 @@ int mf_close(mf_ctx* c) {
   if (!c) return MF_OK;
   return guarded([&] {
     cudaSetDevice(c->device);
+    mf::g_alloc_stream = c->stream;
     if (c->stream) cudaStreamSynchronize(c->stream);
     release_all(c);
     delete c;

@@ -98,23 +98,38 @@ extern const char* const kStageNames[kStCount];
 
 // ---- device buffers ------------------------------------------------------
 
+// Stream the calling thread's context works on (set by the entry points,
+// cleared when they return).  Device buffers are allocated and freed in that
+// stream's order, so growing a buffer does not synchronise the whole device
+// (which would stall the other contexts' streams); with no stream set they
+// use cudaMalloc / cudaFree.
+extern thread_local cudaStream_t g_alloc_stream;
+
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   int64_t cap = 0;
+  cudaStream_t s = nullptr;   // stream p was allocated on (stream-ordered), or null
   void reserve(int64_t count) {
     if (count <= cap) return;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
+    release();
     int64_t c = count < 16 ? 16 : count;
-    MF_CUDA(cudaMalloc(&p, sizeof(T) * (size_t)c));
+    if (g_alloc_stream) {
+      MF_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), sizeof(T) * (size_t)c, g_alloc_stream));
+      s = g_alloc_stream;
+    } else {
+      MF_CUDA(cudaMalloc(&p, sizeof(T) * (size_t)c));
+    }
     cap = c;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (s) cudaFreeAsync(p, s);
+      else cudaFree(p);
+    }
     p = nullptr;
     cap = 0;
+    s = nullptr;
   }
 };
 
@@ -521,6 +536,24 @@ inline void release_device_state(mf_ctx* c) {
   c->heavy_cap = 0;
   c->heavy_used = 0;
   c->epoch = 0;
+  c->n2batch = 0;
+}
+
+// Frees the per-batch and per-sub-batch scratch but keeps the graph state
+// and the n-sized vertex scratch (what a context needs between batches).
+inline void release_batch_scratch(mf_ctx* c) {
+  const void* keep[] = {&c->nindex, &c->nlist, &c->live, &c->dead, &c->rcnt, &c->deg, &c->aoff, &c->aadj,
+                        &c->aown, &c->mis, &c->cid, &c->v2i, &c->bval, &c->wval, &c->f1, &c->nmark,
+                        &c->nlist_need, &c->touched, &c->hlist, &c->acnt_new, &c->aoff_alt, &c->counters};
+  for_each_buffer(c, [&](auto& b) {
+    for (const void* k : keep)
+      if (k == static_cast<const void*>(&b)) return;
+    b.release();
+  });
+  c->bitmap_ctas = 0;
+  c->bitmap_words = 0;
+  c->heavy_cap = 0;
+  c->heavy_used = 0;
   c->n2batch = 0;
 }
 

@@ -122,6 +122,7 @@ struct Graph {
   bool busy = false;           // a worker runs its batch, or it is being moved
   mf::PinnedSnapshot snap;
   int64_t bytes = 0;           // device bytes when last resident
+  bool trimmed = false;        // per-batch scratch freed since its last batch
   uint64_t last_use = 0;
   std::deque<Request*> queue;  // in submission order
 };
@@ -143,40 +144,58 @@ struct mf_pool {
   int64_t resident_bytes = 0;
   mf_pool_stats st{};
 
-  // Makes room for `need` bytes by evicting idle resident graphs, least
-  // recently used first.  Called with the lock held; evictions run with the
-  // lock released (the victims are marked busy meanwhile).
+  // Makes room for `need` bytes, least recently used idle graphs first: a
+  // graph that still holds per-batch scratch gives that up (no copy), one
+  // that does not is evicted to pinned host memory.  Called with the lock
+  // held; the moves run with it released (the victim is marked busy).
   void make_room(std::unique_lock<std::mutex>& lk, int64_t need, int32_t self) {
     while (resident_bytes + need > budget) {
       int32_t victim = -1;
       for (int32_t g = 0; g < (int32_t)graphs.size(); ++g) {
         const Graph& gr = graphs[(size_t)g];
         if (g == self || !gr.resident || gr.busy) continue;
-        if (victim < 0 || (gr.queue.empty() && !graphs[(size_t)victim].queue.empty()) ||
-            (gr.queue.empty() == graphs[(size_t)victim].queue.empty() && gr.last_use < graphs[(size_t)victim].last_use))
-          victim = g;
+        if (victim < 0) { victim = g; continue; }
+        const Graph& vb = graphs[(size_t)victim];
+        // idle graphs with nothing queued first, then untrimmed ones, then LRU
+        const auto rank = [](const Graph& x) { return (x.queue.empty() ? 0 : 2) + (x.trimmed ? 1 : 0); };
+        if (rank(gr) < rank(vb) || (rank(gr) == rank(vb) && gr.last_use < vb.last_use)) victim = g;
       }
       if (victim < 0) {
         st.over_budget += 1;  // every resident graph is running: admit anyway
         return;
       }
       Graph& v = graphs[(size_t)victim];
+      const bool full = v.trimmed;
       v.busy = true;
       lk.unlock();
       int status = MF_OK;
+      int64_t after = 0;
       try {
         mf::bind_device(v.ctx);
-        v.bytes = mf::ctx_device_bytes(v.ctx);
-        mf::evict(v.ctx, v.snap);
+        MF_CUDA(cudaStreamSynchronize(v.ctx->stream));
+        if (full) {
+          mf::evict(v.ctx, v.snap);
+        } else {
+          mf::release_batch_scratch(v.ctx);
+          after = mf::ctx_device_bytes(v.ctx);
+        }
       } catch (const mf::Failure& f) {
         status = f.status;
       }
+      mf::g_alloc_stream = nullptr;
       lk.lock();
       v.busy = false;
       if (status == MF_OK) {
-        v.resident = false;
-        resident_bytes -= v.bytes;
-        st.evictions += 1;
+        if (full) {
+          v.resident = false;
+          resident_bytes -= v.bytes;
+          st.evictions += 1;
+        } else {
+          resident_bytes -= v.bytes - after;
+          v.bytes = after;
+          v.trimmed = true;
+          st.trims += 1;
+        }
       } else {
         st.errors += 1;
       }
@@ -211,6 +230,7 @@ struct mf_pool {
           status = f.status;
           err = mf_last_error();
         }
+        mf::g_alloc_stream = nullptr;
         lk.lock();
         if (status == MF_OK) {
           gr.resident = true;
@@ -232,6 +252,7 @@ struct mf_pool {
       rq->done = true;
       resident_bytes += bytes - gr.bytes;
       gr.bytes = bytes;
+      gr.trimmed = false;
       gr.queue.pop_front();
       gr.busy = false;
       gr.last_use = ++tick;
@@ -245,6 +266,9 @@ struct mf_pool {
         cv_work.notify_one();
       }
       cv_done.notify_all();
+      // the batch may have grown its scratch: back under the budget
+      if (resident_bytes > budget) make_room(lk, 0, -1);
+      st.resident_bytes = resident_bytes;
     }
   }
 };
@@ -337,6 +361,7 @@ int mf_pool_add_graph(mf_pool* p, int32_t n, const int64_t* nindex, const int32_
       lk.unlock();
       mf::bind_device(c);
       mf::evict(c, me.snap);
+      mf::g_alloc_stream = nullptr;
       lk.lock();
       me.resident = false;
       me.busy = false;
@@ -429,6 +454,14 @@ int mf_pool_get_mis(mf_pool* p, int32_t gid, uint8_t* out, int64_t n) {
       const auto& pr = gr.snap.parts[9];
       std::copy(gr.snap.host + pr.first, gr.snap.host + pr.first + pr.second, out);
     }
+  });
+}
+
+int mf_pool_set_budget(mf_pool* p, int64_t hbm_budget) {
+  return pool_guarded([&] {
+    need_arg(p != nullptr && hbm_budget > 0, "bad arguments");
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->budget = hbm_budget;
   });
 }
 

@@ -2270,7 +2270,7 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
   c->big_nr.reserve(nproc);
   c->big_chunks.reserve(nproc + 1);
   c->big_best.reserve(nproc);
-  c->big_pre.reserve((int64_t)1 << 22);
+  c->big_pre.reserve(std::max<int64_t>(4096, std::min<int64_t>((int64_t)1 << 22, 4 * (int64_t)c->n)));
   if (c->big_grid == 0) {
     int sms = 0;
     MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));

@@ -24,7 +24,7 @@ EXPORTS = [
     "mf_trace_count", "mf_trace_get", "mf_stage_name", "mf_profile_enable", "mf_profile_reset",
     "mf_profile_read", "mf_kernel_launches",
     "mf_pool_create", "mf_pool_destroy", "mf_pool_add_graph", "mf_pool_submit", "mf_pool_wait", "mf_pool_drain",
-    "mf_pool_get_mis", "mf_pool_stats_get",
+    "mf_pool_get_mis", "mf_pool_stats_get", "mf_pool_set_budget",
 ]
 
 
@@ -43,7 +43,7 @@ class BatchStats(C.Structure):
 class PoolStats(C.Structure):
     _fields_ = [
         ("graphs", C.c_int64), ("completed", C.c_int64), ("updates", C.c_int64), ("errors", C.c_int64),
-        ("evictions", C.c_int64), ("restores", C.c_int64), ("over_budget", C.c_int64),
+        ("evictions", C.c_int64), ("restores", C.c_int64), ("trims", C.c_int64), ("over_budget", C.c_int64),
         ("resident_bytes", C.c_int64), ("peak_resident_bytes", C.c_int64),
     ]
 
@@ -123,6 +123,7 @@ def _lib():
         "mf_pool_drain": (C.c_int, [_P]),
         "mf_pool_get_mis": (C.c_int, [_P, C.c_int32, _U8P, C.c_int64]),
         "mf_pool_stats_get": (C.c_int, [_P, C.POINTER(PoolStats)]),
+        "mf_pool_set_budget": (C.c_int, [_P, C.c_int64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -411,6 +412,9 @@ class Pool:
         out = np.zeros(self._n[gid], dtype=np.uint8)
         _check(_lib().mf_pool_get_mis(self._h, gid, _ptr(out, C.c_uint8), out.size), "mf_pool_get_mis")
         return out
+
+    def set_budget(self, hbm_budget):
+        _check(_lib().mf_pool_set_budget(self._h, int(hbm_budget)), "mf_pool_set_budget")
 
     def stats(self):
         st = PoolStats()

@@ -258,7 +258,10 @@ class ToggleStream:
                 got = self.rng.permutation(got)[:count]
         return got
 
-    def next_batch(self, batch_size, delete_frac=0.5, endpoints="uniform"):
+    def next_batch(self, batch_size, delete_frac=0.5, endpoints="uniform", with_flags=False):
+        """(u, v), or (u, v, ins) with ins = 1 for inserts and 0 for deletes
+        when with_flags (the flags against the nominal graph, which is what a
+        serving client sends)."""
         n = self.n
         nd = min(int(round(batch_size * delete_frac)), self.num_edges)
         ni = batch_size - nd
@@ -277,7 +280,10 @@ class ToggleStream:
             if ikeys.size > ni:
                 ikeys = self.rng.permutation(ikeys)[:ni]
         keys = np.concatenate([dkeys, ikeys])
-        keys = keys[self.rng.permutation(keys.size)]
+        is_ins = np.concatenate([np.zeros(dkeys.size, np.uint8), np.ones(ikeys.size, np.uint8)])
+        perm = self.rng.permutation(keys.size)
+        keys = keys[perm]
+        is_ins = is_ins[perm]
         lo = keys // n
         hi = keys % n
         flip = self.rng.random(keys.size) < 0.5
@@ -295,6 +301,8 @@ class ToggleStream:
         for keyset, sign in ((dkeys, -1.0), (ikeys, 1.0)):
             np.add.at(self.deg, keyset // n, sign)
             np.add.at(self.deg, keyset % n, sign)
+        if with_flags:
+            return u, v, is_ins
         return u, v
 
 
