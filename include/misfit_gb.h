@@ -172,6 +172,13 @@ int mf_get_cluster_ids(mf_ctx* ctx, int32_t* out, int64_t n);
  * vertices (neither in the set nor adjacent to it) on the current graph. */
 int mf_check_mis(mf_ctx* ctx, int64_t* violations, int64_t* uncovered);
 
+/* Exact-MIS mode (on != 0).  No counterpart in the reference, whose repair
+ * rules are conservative and can leave violations and uncovered vertices.
+ * After each batch's repair: every member with a smaller-id member neighbour
+ * leaves, then the vertices with no member neighbour join greedily in
+ * ascending id, so the set is independent and maximal afterwards. */
+int mf_set_exact(mf_ctx* ctx, int on);
+
 /* ---- compaction -------------------------------------------------------- */
 
 /* Merge base + overlay on the device and write an int64-sentinel .egr via a

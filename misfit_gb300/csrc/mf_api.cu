@@ -190,6 +190,7 @@ void run_batch(mf_ctx* c, int64_t m) {
       mf::apply_overlay(c, m);
     }
     mf::process_batch(c, m);
+    if (c->exact) mf::exact_fixup(c);
   }
   MF_CUDA(cudaEventRecord(c->ev1, s));
   MF_CUDA(cudaEventSynchronize(c->ev1));
@@ -652,6 +653,13 @@ int mf_set_max_csr(mf_ctx* c, int64_t value) {
   return guarded([&] {
     need(c && value > 0, MF_EINVAL, "bad arguments");
     c->max_csr = value;
+  });
+}
+
+int mf_set_exact(mf_ctx* c, int on) {
+  return guarded([&] {
+    need(c != nullptr, MF_EINVAL, "null context");
+    c->exact = on != 0;
   });
 }
 

@@ -449,6 +449,8 @@ struct mf_ctx {
   // first-hit chunk queue (rows) and the need seeds' chunk queue
   mf::DBuf<int32_t> rq_idx, rq_v, mq_idx, mq_v;
   mf::DBuf<int64_t> mq_base;
+  mf::DBuf<uint8_t> xst, xleave;      // exact-MIS mode: completion states, leave flags
+  bool exact = false;                  // exact-MIS mode on
   mf::DBuf<uint32_t> hbits;           // hop-1 and seed bitmaps of the current sub-batch
   mf::DBuf<int64_t> bits_sums;        // their per-block counts
   mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
@@ -514,6 +516,7 @@ void for_each_buffer(mf_ctx* c, F&& f) {
   f(c->bitmaps); f(c->heavy_bits); f(c->dense_bits); f(c->ncbits); f(c->hbits); f(c->n2stamp);
   f(c->n2bstamp); f(c->nmark);
   f(c->mis); f(c->bins); f(c->u8a); f(c->akill); f(c->creates); f(c->rp_u8); f(c->plan_flags);
+  f(c->xst); f(c->xleave);
   f(c->keys); f(c->app_keys); f(c->rp_keys); f(c->rp_keys2);
   f(c->big_best); f(c->fpos); f(c->work); f(c->uacc);
   f(c->ws.block_sums); f(c->ws.block_sums2); f(c->ws.hist); f(c->ws.hist_scan); f(c->ws.keys_alt);
@@ -607,6 +610,7 @@ void compact_graph(mf_ctx* c, std::vector<int64_t>& nindex_out, std::vector<int3
 void rebase(mf_ctx* c);
 void greedy_mis(mf_ctx* c, uint8_t* d_out);
 void check_mis(mf_ctx* c, int64_t* viol, int64_t* uncovered);
+void exact_fixup(mf_ctx* c);                       // exact-MIS mode after a batch
 // mf_repair.cu
 void process_batch(mf_ctx* c, int64_t m);          // everything after the overlay apply
 int64_t initial_max_csr(int32_t n, uint64_t edges);

@@ -346,6 +346,52 @@ __global__ void k_greedy_round(GraphView g, bool sorted, uint8_t* st, int64_t* c
   else atomicAdd((unsigned long long*)counters, 1ull);
 }
 
+// ---- exact-MIS mode (no reference counterpart) -----------------------------------
+// After a batch's repair: a member with a smaller-id member neighbour leaves
+// (decided on the set the repair left), then the vertices with no member
+// neighbour are completed in ascending id by the greedy rounds (state 1 in,
+// 2 out, 0 undecided; non-members next to a member start out).
+
+__global__ void k_exact_leave(GraphView g, bool sorted, const uint8_t* mis, uint8_t* leave) {
+  const int64_t xi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (xi >= g.n) return;
+  const int32_t x = (int32_t)xi;
+  bool found = false;
+  if (mis[x] & 1) {
+    const int64_t b = g.nindex[x], e = g.nindex[x + 1];
+    const bool filt = g.dead[x] != 0;
+    for (int64_t k = b; k < e && !found; ++k) {
+      const int32_t y = g.nlist[k];
+      if (sorted && y >= x) break;
+      if (y >= x || (filt && !live_at(g.live, k))) continue;
+      found = (mis[y] & 1) != 0;
+    }
+    for (int64_t k = g.aoff[x]; k < g.aoff[x + 1] && !found; ++k) {
+      const int32_t y = g.aadj[k];
+      found = y < x && (mis[y] & 1) != 0;
+    }
+  }
+  leave[x] = found ? 1 : 0;
+}
+
+__global__ void k_exact_init(GraphView g, const uint8_t* mis, const uint8_t* leave, uint8_t* st) {
+  const int64_t xi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (xi >= g.n) return;
+  const int32_t x = (int32_t)xi;
+  auto member = [&](int32_t y) { return (mis[y] & 1) != 0 && leave[y] == 0; };
+  if (member(x)) {
+    st[x] = 1;
+    return;
+  }
+  const bool covered = thread_row_until(g, x, [&](int32_t y) { return member(y); });
+  st[x] = covered ? 2 : 0;
+}
+
+__global__ void k_exact_out(const uint8_t* st, int32_t n, uint8_t* mis) {
+  const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x < n) mis[x] = st[x] == 1 ? 1 : 0;
+}
+
 __global__ void k_greedy_out(const uint8_t* st, int32_t n, uint8_t* out) {
   int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x < n) out[x] = st[x] == 1 ? 1 : 0;
@@ -569,6 +615,26 @@ void greedy_mis(mf_ctx* c, uint8_t* d_out) {
   MF_K(k_greedy_out<<<grid_for(n), kTB, 0, s>>>(st.p, n, d_out));
   MF_CUDA(cudaStreamSynchronize(s));
   st.release();
+}
+
+void exact_fixup(mf_ctx* c) {
+  cudaStream_t s = c->stream;
+  const int32_t n = c->n;
+  if (n <= 0) return;
+  c->xst.reserve(n);
+  c->xleave.reserve(n);
+  MF_K(k_exact_leave<<<grid_for(n), kTB, 0, s>>>(c->view(), c->rows_sorted, c->mis.p, c->xleave.p));
+  MF_K(k_exact_init<<<grid_for(n), kTB, 0, s>>>(c->view(), c->mis.p, c->xleave.p, c->xst.p));
+  for (int round = 0;; ++round) {
+    MF_CUDA(cudaMemsetAsync(c->counters.p, 0, sizeof(int64_t), s));
+    MF_K(k_greedy_round<<<grid_for(n), kTB, 0, s>>>(c->view(), c->rows_sorted, c->xst.p, c->counters.p));
+    MF_CUDA(cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    if (c->h_counters[0] == 0) break;
+    if (round > n + 2) MF_FAIL(MF_ESTATE, "exact-MIS completion did not settle");
+  }
+  MF_K(k_exact_out<<<grid_for(n), kTB, 0, s>>>(c->xst.p, n, c->mis.p));
+  MF_CUDA(cudaGetLastError());
 }
 
 void check_mis(mf_ctx* c, int64_t* viol, int64_t* uncovered) {

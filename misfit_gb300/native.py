@@ -19,7 +19,7 @@ EXPORTS = [
     "mf_num_nodes", "mf_num_base_entries", "mf_set_mis", "mf_get_mis", "mf_mis_size", "mf_greedy_mis",
     "mf_flag_updates", "mf_flag_updates_noalloc", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_sync",
     "mf_last_batch_stats", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
-    "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_compact", "mf_read_mis_file",
+    "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_set_exact", "mf_compact", "mf_read_mis_file",
     "mf_write_mis_file", "mf_read_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
     "mf_trace_count", "mf_trace_get", "mf_stage_name", "mf_profile_enable", "mf_profile_reset",
     "mf_profile_read", "mf_kernel_launches",
@@ -101,6 +101,7 @@ def _lib():
         "mf_set_max_csr": (C.c_int, [_P, C.c_int64]),
         "mf_get_cluster_ids": (C.c_int, [_P, _I32P, C.c_int64]),
         "mf_check_mis": (C.c_int, [_P, _I64P, _I64P]),
+        "mf_set_exact": (C.c_int, [_P, C.c_int]),
         "mf_compact": (C.c_int, [_P, C.c_char_p, C.c_int]),
         "mf_read_mis_file": (C.c_int, [C.c_char_p, C.c_int32, _U8P, _I64P]),
         "mf_write_mis_file": (C.c_int, [C.c_char_p, _U8P, C.c_int32]),
@@ -275,6 +276,10 @@ class Graph:
     @max_csr.setter
     def max_csr(self, value):
         _check(_lib().mf_set_max_csr(self._h, int(value)), "mf_set_max_csr")
+
+    def set_exact(self, on=True):
+        """Exact-MIS mode: independent, maximal membership after every batch."""
+        _check(_lib().mf_set_exact(self._h, 1 if on else 0), "mf_set_exact")
 
     def check_mis(self):
         a, b = C.c_int64(), C.c_int64()

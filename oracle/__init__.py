@@ -42,6 +42,7 @@ def lib():
             "or_base_entries": (C.c_int64, [_P]),
             "or_max_csr": (C.c_int64, [_P]),
             "or_set_max_csr": (None, [_P, C.c_int64]),
+            "or_set_exact": (None, [_P, C.c_int]),
             "or_set_mis": (None, [_P, _U8P]),
             "or_get_mis": (None, [_P, _U8P]),
             "or_get_cluster_ids": (None, [_P, _I32P]),
@@ -106,6 +107,10 @@ class Oracle:
     @max_csr.setter
     def max_csr(self, v):
         lib().or_set_max_csr(self._h, int(v))
+
+    def set_exact(self, on=True):
+        """Exact-MIS mode: independent, maximal membership after every batch."""
+        lib().or_set_exact(self._h, 1 if on else 0)
 
     def set_mis(self, mis):
         mis = np.ascontiguousarray(mis, dtype=np.uint8)

@@ -58,6 +58,7 @@ struct or_graph {
   std::vector<int32_t> cid;
   int64_t max_csr = 0;
   bool trace = false;
+  bool exact = false;   // exact-MIS mode: fix-up after every batch (no reference counterpart)
   std::vector<SubBatchTrace> traces;
 };
 
@@ -331,6 +332,7 @@ int32_t or_num_nodes(const or_graph* g) { return g->n; }
 int64_t or_base_entries(const or_graph* g) { return (int64_t)g->edges; }
 int64_t or_max_csr(const or_graph* g) { return g->max_csr; }
 void or_set_max_csr(or_graph* g, int64_t v) { g->max_csr = v; }
+void or_set_exact(or_graph* g, int on) { g->exact = on != 0; }
 
 // setMISFromHost / getMISToHost (src/misfit/misfit.cu:448-462).
 void or_set_mis(or_graph* g, const uint8_t* mis) {
@@ -345,6 +347,32 @@ void or_flag_updates(const or_graph* g, const int32_t* u, const int32_t* v, int6
   for (int64_t i = 0; i < m; ++i) ins_out[i] = adjacent(g, u[i], v[i]) ? 0 : 1;
 }
 int or_is_adjacent(const or_graph* g, int32_t u, int32_t v) { return adjacent(g, u, v) ? 1 : 0; }
+
+// Exact-MIS mode (no reference counterpart): after the reference's repair,
+// (1) every member with a smaller-id member neighbour leaves (decided on the
+// set as the repair left it), then (2) the non-members with no member
+// neighbour are completed greedily in ascending id.  The result is an
+// independent, maximal set.
+static void exact_fixup(or_graph* g) {
+  std::vector<int32_t> r;
+  std::vector<uint8_t> leave((size_t)g->n, 0);
+  for (int32_t x = 0; x < g->n; ++x) {
+    if (!g->mis[(size_t)x]) continue;
+    row_into(g, x, r);
+    for (int32_t y : r)
+      if (y < x && g->mis[(size_t)y]) { leave[(size_t)x] = 1; break; }
+  }
+  for (int32_t x = 0; x < g->n; ++x)
+    if (leave[(size_t)x]) g->mis[(size_t)x] = 0;
+  for (int32_t x = 0; x < g->n; ++x) {
+    if (g->mis[(size_t)x]) continue;
+    row_into(g, x, r);
+    bool covered = false;
+    for (int32_t y : r)
+      if (g->mis[(size_t)y]) { covered = true; break; }
+    if (!covered) g->mis[(size_t)x] = 1;
+  }
+}
 
 int64_t or_apply_batch(or_graph* g, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
   g->traces.clear();
@@ -442,6 +470,7 @@ int64_t or_apply_batch(or_graph* g, const int32_t* u, const int32_t* v, const ui
     p = q;
     ++nsub;
   }
+  if (g->exact) exact_fixup(g);
   return nsub;
 }
 

@@ -49,6 +49,10 @@ int32_t or_num_nodes(const or_graph* g);
 int64_t or_base_entries(const or_graph* g);
 int64_t or_max_csr(const or_graph* g);
 void or_set_max_csr(or_graph* g, int64_t v);
+/* Exact-MIS mode (no reference counterpart): after each batch's repair, a
+ * member with a smaller-id member neighbour leaves, then the uncovered
+ * vertices are completed greedily in ascending id. */
+void or_set_exact(or_graph* g, int on);
 
 void or_set_mis(or_graph* g, const uint8_t* mis);
 void or_get_mis(const or_graph* g, uint8_t* out);

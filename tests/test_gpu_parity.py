@@ -289,3 +289,32 @@ def test_general_graphs_use_push_form(layout, gpu_lib):
         gr.apply_batch(u[sl], v[sl], ins)
         _assert_same_trace(gr.trace_records(), orc.trace_records(), n)
         assert np.array_equal(gr.get_mis(), orc.get_mis())
+
+
+@pytest.mark.parametrize("kind", ["er", "rmat"])
+def test_exact_mode_matches_oracle(gpu_lib, kind):
+    """Exact-MIS mode: the membership after every batch equals the oracle's
+    exact mode bit for bit, and it is independent and maximal."""
+    if kind == "er":
+        nindex, nlist = W.er_graph(4000, 8, 31)
+    else:
+        _, (nindex, nlist) = W.rmat_graph(12, 8, 31)
+    n = nindex.size - 1
+    gr = native.Graph.from_csr(nindex, nlist)
+    orc = O.Oracle.from_csr(nindex, nlist)
+    try:
+        mis0 = O.greedy_mis(nindex, nlist)
+        gr.set_mis(mis0)
+        orc.set_mis(mis0)
+        gr.set_exact(True)
+        orc.set_exact(True)
+        ts = W.ToggleStream(n, nindex, nlist, 32)
+        for b in range(4):
+            u, v, ins = ts.next_batch(1500, with_flags=True)
+            gr.apply_batch(u, v, ins)
+            orc.apply_batch(u, v, ins)
+            assert np.array_equal(gr.get_mis(), orc.get_mis()), b
+            assert gr.check_mis() == (0, 0), b
+    finally:
+        gr.close()
+        orc.close()

@@ -77,3 +77,20 @@ def test_oracle_property_counts_sample():
     viol, uncovered = orc.check_mis()
     assert viol == 0
     assert uncovered == 19
+
+
+def test_oracle_exact_mode_is_a_mis():
+    """Exact-MIS mode of the oracle: independent and maximal after every batch."""
+    from misfit_gb300 import workloads as W
+    nindex, nlist = W.er_graph(2000, 6, 41)
+    orc = O.Oracle.from_csr(nindex, nlist)
+    try:
+        orc.set_mis(O.greedy_mis(nindex, nlist))
+        orc.set_exact(True)
+        ts = W.ToggleStream(2000, nindex, nlist, 42)
+        for _ in range(3):
+            u, v, ins = ts.next_batch(600, with_flags=True)
+            orc.apply_batch(u, v, ins)
+            assert orc.check_mis() == (0, 0)
+    finally:
+        orc.close()
