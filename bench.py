@@ -62,6 +62,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="skip the served and batched legs")
+    ap.add_argument("--no-exact", action="store_true", help="skip the exact-MIS leg")
     ap.add_argument("--served-graphs", type=int, default=64)
     ap.add_argument("--served-requests", type=int, default=300)
     ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrivals per second")
@@ -370,8 +371,10 @@ def main():
     n, nindex, nlist, stream = make_workload(args, "cuda:%d" % local)
     g = native.Graph.from_csr(nindex, nlist, gpu=local)
     g.set_mis(g.greedy_mis())
-    # warm-up, timed, e2e, and one untimed batch with every stage timed
-    total = args.warmup + args.steps + (0 if args.no_e2e else args.steps) + 1
+    # warm-up, timed, e2e, one untimed batch with every stage timed, then the
+    # exact-MIS leg (one warm-up and `steps` timed batches)
+    exact_steps = 0 if args.no_exact else 1 + args.steps
+    total = args.warmup + args.steps + (0 if args.no_e2e else args.steps) + 1 + exact_steps
     batches = [stream.next_batch(args.batch) for _ in range(total)]
     flags = [g.flag_updates(u, v) for u, v in batches]  # against the base graph, before any batch
 
@@ -438,12 +441,31 @@ def main():
                "h2d_bytes_per_step": int(args.batch * 9), "d2h_bytes_per_step": int(n)}
 
     # ---- per-stage breakdown: one more batch, untimed, with every stage timed
+    nxt = args.warmup + args.steps + (0 if args.no_e2e else args.steps)
     g.profile(True)
     g.profile_reset()
-    u, v = batches[-1]
-    g.apply_batch(u, v, flags[-1])
+    u, v = batches[nxt]
+    g.apply_batch(u, v, flags[nxt])
     stage_prof = g.profile_read()
     g.profile(False)
+    nxt += 1
+
+    # ---- exact-MIS mode on the same context: the fix-up after every batch
+    exact = None
+    if exact_steps:
+        g.set_exact(True)
+        ex_ms = []
+        for k in range(exact_steps):
+            u, v = batches[nxt + k]
+            g.apply_batch(u, v, flags[nxt + k])
+            if k >= 1:
+                ex_ms.append(g.stats()["device_ms"])
+        viol, unc = g.check_mis()
+        g.set_exact(False)
+        exact = {"value": len(ex_ms) * args.batch / (float(np.sum(ex_ms)) / 1e3), "unit": UNIT,
+                 "ms_per_step": float(np.mean(ex_ms)), "steps": len(ex_ms), "warmup": 1,
+                 "violations_after": int(viol), "uncovered_after": int(unc),
+                 "timing": "library CUDA events per batch, host-buffer batches"}
 
     # ---- roofline of the dominant kernel, k_lb_push_hop (the hop-2 reach of
     # the clustering write): algorithmic bytes = 12 B per pushed element
@@ -476,6 +498,8 @@ def main():
     }
     if e2e:
         line["e2e"] = e2e
+    if exact:
+        line["exact_mode"] = exact
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         u, v = batches[0]
         rate, lines, spent = cpu_sample(n, nindex, nlist, (u, v), flags[0], args.cpu_seconds)
