@@ -62,7 +62,7 @@ def write_egr(path, n, nindex, nlist, wide=None):
                 raise ValueError("int32 layout cannot hold %d entries" % e)
             f.write(struct.pack("<ii", n, e))
             f.write(nindex.astype("<i4").tobytes())
-        nlist.astype("<i4").tofile(f)
+        (nlist if nlist.dtype == np.dtype("<i4") else nlist.astype("<i4")).tofile(f)
     os.replace(tmp, path)
 
 
