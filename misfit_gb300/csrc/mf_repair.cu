@@ -1572,40 +1572,14 @@ __device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_
   return -1;
 }
 
-__global__ void k_spec_eval(SpecArgs a) {
-  const int64_t wi = warp_id();
-  if (wi >= a.cnt - a.p0) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t pos = a.p0 + wi;
-  const int64_t j = a.p + a.order[pos];
-  const int32_t x = a.u[j], y = a.v[j];
-  const bool ins = a.ins[j] != 0;
-  Member mem{&a.view, (uint32_t)pos, -1};
-  const int mx = mem(x), my = mem(y);
-  int32_t o0 = -1, o1 = -1;
-  if (ins) {
-    if (mx && my) {
-      const int32_t r = x > y ? x : y;
-      o0 = r;
-      mem.self0 = r;
-      if (a.v2i[r] >= 0) o1 = w_first_eligible(a, mem, r);
-    }
-  } else if (mx != my) {
-    const int32_t yy = mx ? y : x, keep = mx ? x : y;
-    if (a.v2i[yy] < 0 || !w_any(a, mem, yy, keep)) o0 = yy;
-  }
-  if (lane == 0) {
-    a.out0[pos] = o0;
-    a.out1[pos] = o1;
-  }
-}
-
 constexpr int kBigChunk = 256;  // positions per chunk = threads per block of k_big_scan
 
-// Chunk prefix over the deferred edges (one block): chunk_pre[i] = first chunk
-// of deferred edge i, chunk_pre[nbig] = total; best[i] = none.
-__global__ void k_big_prep(SpecArgs a, int64_t* chunk_pre, unsigned long long* best, unsigned long long* queue) {
-  const int64_t nbig = (int64_t)*a.big_count;
+// Chunk prefix over the deferred edges (one block, any size up to 1024
+// threads): chunk_pre[i] = first chunk of deferred edge i, chunk_pre[nbig] =
+// total; best[i] = none; the chunk queue restarts.
+__device__ void big_prep_block(const SpecArgs& a, int64_t* chunk_pre, unsigned long long* best,
+                               unsigned long long* queue) {
+  const int64_t nbig = (int64_t)*(volatile unsigned long long*)a.big_count;
   __shared__ int64_t s_carry;
   if (threadIdx.x == 0) { s_carry = 0; queue[0] = 0; queue[1] = 0; }
   __syncthreads();
@@ -1637,6 +1611,50 @@ __global__ void k_big_prep(SpecArgs a, int64_t* chunk_pre, unsigned long long* b
     __syncthreads();
   }
   if (threadIdx.x == 0) chunk_pre[nbig] = s_carry;
+}
+
+// One warp per pending edge.  The last block to finish also prepares the
+// grid-wide hop-2 search (big_prep_block): every block fences its deferral
+// records before it counts itself done.
+__global__ void k_spec_eval(SpecArgs a, int64_t* chunk_pre, unsigned long long* best, unsigned long long* queue,
+                            unsigned int* done) {
+  const int64_t wi = warp_id();
+  if (wi < a.cnt - a.p0) {
+    const int lane = threadIdx.x & 31;
+    const int64_t pos = a.p0 + wi;
+    const int64_t j = a.p + a.order[pos];
+    const int32_t x = a.u[j], y = a.v[j];
+    const bool ins = a.ins[j] != 0;
+    Member mem{&a.view, (uint32_t)pos, -1};
+    const int mx = mem(x), my = mem(y);
+    int32_t o0 = -1, o1 = -1;
+    if (ins) {
+      if (mx && my) {
+        const int32_t r = x > y ? x : y;
+        o0 = r;
+        mem.self0 = r;
+        if (a.v2i[r] >= 0) o1 = w_first_eligible(a, mem, r);
+      }
+    } else if (mx != my) {
+      const int32_t yy = mx ? y : x, keep = mx ? x : y;
+      if (a.v2i[yy] < 0 || !w_any(a, mem, yy, keep)) o0 = yy;
+    }
+    if (lane == 0) {
+      a.out0[pos] = o0;
+      a.out1[pos] = o1;
+    }
+  }
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    big_prep_block(a, chunk_pre, best, queue);
+  }
 }
 
 // Grid-wide first-eligible search over the flattened hop-2 sequences of the
@@ -1762,9 +1780,9 @@ __global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_
   }
 }
 
-__global__ void k_big_finalize(SpecArgs a, const unsigned long long* best) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)*a.big_count) return;
+// The answer of deferred edge i: the vertex at its smallest eligible
+// position, or -1.
+__device__ void big_finalize_one(const SpecArgs& a, const unsigned long long* best, int64_t i) {
   const GraphView& g = a.g;
   int32_t w = -1;
   if (best[i] != ~0ull) {
@@ -1781,6 +1799,11 @@ __global__ void k_big_finalize(SpecArgs a, const unsigned long long* best) {
     w = row_elem(g, h, q - pre[klo], g.nindex[h + 1] - g.nindex[h]);
   }
   a.out1[a.big_pos[i]] = w;
+}
+
+__global__ void k_big_finalize(SpecArgs a, const unsigned long long* best) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < (int64_t)*a.big_count) big_finalize_one(a, best, i);
 }
 
 __global__ void k_spec_first_change(const int32_t* n0, const int32_t* n1, const int32_t* r0, const int32_t* r1,
@@ -1889,12 +1912,17 @@ __global__ void __launch_bounds__(kRoundThreads) k_spec_round(const int32_t* n0,
                                                               const uint8_t* ins, int64_t p, const uint32_t* order,
                                                               uint64_t* view_keys, uint32_t* view_vals,
                                                               int64_t nview_old, uint8_t* m,
-                                                              unsigned long long* out) {
+                                                              unsigned long long* out, SpecArgs sa,
+                                                              const unsigned long long* best) {
   __shared__ uint64_t s_keys[kRoundWrites];
   __shared__ uint32_t s_vals[kRoundWrites];
   __shared__ int s_warp[33];
   __shared__ unsigned long long s_f;
   const int tid = threadIdx.x;
+  // answers of the edges whose hop-2 search ran grid-wide (k_big_scan)
+  const int64_t nbig = (int64_t)*sa.big_count;
+  for (int64_t i = tid; i < nbig; i += kRoundThreads) big_finalize_one(sa, best, i);
+  __syncthreads();
   const int64_t pending = cnt - p0;
   if (tid == 0) s_f = (unsigned long long)cnt;
   __syncthreads();
@@ -2293,22 +2321,23 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     }
     ++rounds;
     const int64_t pending = nproc - p0;
-    MF_CUDA(cudaMemsetAsync(c->counters.p + 24, 0, sizeof(int64_t) * 2, s));
+    MF_CUDA(cudaMemsetAsync(c->counters.p + 24, 0, sizeof(int64_t) * 6, s));  // deferrals, prefix use, queue, done
     SpecArgs a{g, c->bu.p, c->bv.p, c->bins.p, p, order, p0, nproc, ns, c->v2i.p,
                View{c->mis.p, c->rp_keys.p, c->rp_vals.p, nview}, c->rp_n0.p, c->rp_n1.p,
                big_threshold(), ucnt + 24, c->big_pos.p, c->big_r.p, c->big_off.p, c->big_nr.p,
                c->big_pre.p, ucnt + 25, c->big_pre.cap};
     rsc.emplace(c, kStRepair);
-    MF_K(k_spec_eval<<<warps_grid(pending), kTB, 0, s>>>(a));
+    MF_K(k_spec_eval<<<warps_grid(pending), kTB, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26,
+                                                          reinterpret_cast<unsigned int*>(ucnt + 29)));
     rsc.emplace(c, kStRepairBig);
-    MF_K(k_big_prep<<<1, 1024, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
     MF_K(k_big_scan<<<(unsigned)c->big_grid, kBigChunk, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
-    MF_K(k_big_finalize<<<grid_for(pending), kTB, 0, s>>>(a, c->big_best.p));
     rsc.emplace(c, kStRepair);
     if (pending <= kRoundCap) {
-      // small round: one CTA finishes it, one host round trip
+      // small round: one CTA finalizes the grid-wide searches and finishes
+      // the round, one host round trip
       MF_K(k_spec_round<<<1, kRoundThreads, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0, nproc, c->bins.p,
-                                                    p, order, c->rp_keys.p, c->rp_vals.p, nview, c->mis.p, ucnt + 20));
+                                                    p, order, c->rp_keys.p, c->rp_vals.p, nview, c->mis.p, ucnt + 20,
+                                                    a, c->big_best.p));
       MF_CUDA(cudaMemcpyAsync(h + 20, c->counters.p + 20, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
       MF_CUDA(cudaStreamSynchronize(s));
       const int64_t f = h[20];
@@ -2328,6 +2357,7 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
       p0 = f + 1;
       continue;
     }
+    MF_K(k_big_finalize<<<grid_for(pending), kTB, 0, s>>>(a, c->big_best.p));
     h[20] = (int64_t)nproc;
     MF_CUDA(cudaMemcpyAsync(c->counters.p + 20, h + 20, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     MF_K(k_spec_first_change<<<grid_for(pending), kTB, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0,
