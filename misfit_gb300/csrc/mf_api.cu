@@ -137,6 +137,13 @@ void release_all(mf_ctx* c) {
   c->ev_pool.clear();
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream_b) {
+    cudaStreamSynchronize(c->stream_b);
+    cudaStreamDestroy(c->stream_b);
+  }
+  c->stream_b = nullptr;
+  if (c->ev_a) cudaEventDestroy(c->ev_a);
+  if (c->ev_b) cudaEventDestroy(c->ev_b);
   if (c->stream) cudaStreamDestroy(c->stream);
   c->stream = nullptr;
 }
@@ -159,6 +166,9 @@ mf_ctx* new_ctx(int gpu) {
     }
     MF_CUDA(cudaEventCreate(&c->ev0));
     MF_CUDA(cudaEventCreate(&c->ev1));
+    MF_CUDA(cudaStreamCreateWithFlags(&c->stream_b, cudaStreamNonBlocking));
+    MF_CUDA(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
+    MF_CUDA(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
     MF_CUDA(cudaMallocHost(&c->h_counters, sizeof(int64_t) * 64));
     c->counters.reserve(64);
   } catch (...) {

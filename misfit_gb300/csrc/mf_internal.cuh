@@ -378,6 +378,22 @@ struct SubBatchTrace {
   std::vector<int64_t> row_len;
 };
 
+// Buffers of one sub-batch's "front": its hop-1 set, candidate list and
+// packed-size bound.  They depend only on the batch's graph and the planned
+// seed list, so the front of the next sub-batch is computed on a second
+// stream while the current one clusters and repairs (two sets, alternating).
+namespace mf {
+struct Front {
+  mf::DBuf<uint32_t> bits;                  // hop-1 bitmap, then the seed bitmap
+  mf::DBuf<int64_t> bits_sums;              // per-block counts of the bitmap scan
+  mf::DBuf<unsigned long long> uacc;        // per-seed sums of the size bound
+  mf::DBuf<int32_t> hlist, cands;           // swapped into the context when its sub-batch runs
+  mf::DBuf<int64_t> lb_offs;                // row offsets of the seeds
+  mf::DBuf<int64_t> cnt;                    // [0] (hop-1 << 32 | candidates), [1] size bound
+  mf::Scratch ws;
+};
+}  // namespace mf
+
 struct mf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -434,7 +450,6 @@ struct mf_ctx {
   mf::DBuf<uint32_t> bitmaps;   // per-CTA vertex bitmaps for exact 2-hop sizes
   int64_t bitmap_words = 0;
   int bitmap_ctas = 0;
-  mf::DBuf<unsigned long long> uacc;   // per-seed sums of the size bound
   mf::DBuf<int32_t> heavy_slot, heavy_list;
   mf::DBuf<uint32_t> heavy_bits;
   int64_t heavy_cap = 0, heavy_used = 0;
@@ -451,8 +466,9 @@ struct mf_ctx {
   mf::DBuf<int64_t> mq_base;
   mf::DBuf<uint8_t> xst, xleave;      // exact-MIS mode: completion states, leave flags
   bool exact = false;                  // exact-MIS mode on
-  mf::DBuf<uint32_t> hbits;           // hop-1 and seed bitmaps of the current sub-batch
-  mf::DBuf<int64_t> bits_sums;        // their per-block counts
+  mf::Front front[2];                 // current and next sub-batch fronts
+  cudaStream_t stream_b = nullptr;    // the fronts of later sub-batches run here
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr;
   mf::DBuf<int64_t> n2cache;           // exact 2-hop sizes of this batch's rows
   mf::DBuf<uint32_t> n2stamp;          // batch stamp of each cached size
   mf::DBuf<int64_t> n2bound;           // tighter upper bounds of this batch's 2-hop sizes
@@ -503,7 +519,7 @@ template <class F>
 void for_each_buffer(mf_ctx* c, F&& f) {
   f(c->nindex); f(c->aoff); f(c->aoff_alt); f(c->i64a); f(c->i64b); f(c->rowlens); f(c->rp_pos);
   f(c->big_pos); f(c->big_off); f(c->big_nr); f(c->big_chunks); f(c->big_pre); f(c->dense_light);
-  f(c->plan_cuts); f(c->plan_ests); f(c->plan_send); f(c->plan_pos); f(c->mq_base); f(c->bits_sums);
+  f(c->plan_cuts); f(c->plan_ests); f(c->plan_send); f(c->plan_pos); f(c->mq_base);
   f(c->n2cache); f(c->n2bound); f(c->un_cnt); f(c->counters); f(c->lb_offs);
   f(c->nlist); f(c->dead); f(c->rcnt); f(c->deg); f(c->aadj); f(c->aown); f(c->aadj_alt); f(c->aown_alt);
   f(c->cid); f(c->v2i); f(c->f1); f(c->bu); f(c->bv); f(c->prev); f(c->i32a); f(c->i32b); f(c->i32c);
@@ -513,14 +529,19 @@ void for_each_buffer(mf_ctx* c, F&& f) {
   f(c->dense_idx); f(c->dense_hl); f(c->pair_d); f(c->pair_h); f(c->todo);
   f(c->un_idx); f(c->un_v); f(c->need); f(c->needv); f(c->live_i); f(c->live_v); f(c->nlist_need);
   f(c->live); f(c->bval); f(c->wval); f(c->vals); f(c->app_vals); f(c->rp_vals); f(c->rp_vals2);
-  f(c->bitmaps); f(c->heavy_bits); f(c->dense_bits); f(c->ncbits); f(c->hbits); f(c->n2stamp);
+  f(c->bitmaps); f(c->heavy_bits); f(c->dense_bits); f(c->ncbits); f(c->n2stamp);
   f(c->n2bstamp); f(c->nmark);
   f(c->mis); f(c->bins); f(c->u8a); f(c->akill); f(c->creates); f(c->rp_u8); f(c->plan_flags);
   f(c->xst); f(c->xleave);
   f(c->keys); f(c->app_keys); f(c->rp_keys); f(c->rp_keys2);
-  f(c->big_best); f(c->fpos); f(c->work); f(c->uacc);
+  f(c->big_best); f(c->fpos); f(c->work);
   f(c->ws.block_sums); f(c->ws.block_sums2); f(c->ws.hist); f(c->ws.hist_scan); f(c->ws.keys_alt);
   f(c->ws.vals_alt);
+  for (auto& fr : c->front) {
+    f(fr.bits); f(fr.bits_sums); f(fr.uacc); f(fr.hlist); f(fr.cands); f(fr.lb_offs); f(fr.cnt);
+    f(fr.ws.block_sums); f(fr.ws.block_sums2); f(fr.ws.hist); f(fr.ws.hist_scan); f(fr.ws.keys_alt);
+    f(fr.ws.vals_alt);
+  }
 }
 
 // Device bytes a context holds now.

@@ -334,12 +334,19 @@ __global__ void __launch_bounds__(kBitsThreads) k_bits_compact(const uint32_t* h
       if (!((sm >> b) & 1u)) {
         if (pc < cap) {
           cands[pc] = x;
-          v2i[x] = (int32_t)(ns + pc);
+          if (v2i) v2i[x] = (int32_t)(ns + pc);
         }
         ++pc;
       }
     }
   }
+}
+
+// Row map of the candidates (rows ns .. ns + nct - 1), once the previous
+// sub-batch has cleared its rows.
+__global__ void k_cand_v2i(const int32_t* cands, int64_t nct, int64_t ns, int32_t* v2i) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nct) v2i[cands[i]] = (int32_t)(ns + i);
 }
 
 // ---- packed sizes ---------------------------------------------------------------
@@ -2059,6 +2066,63 @@ void row_offsets(mf_ctx* c, const int32_t* list, int64_t cnt, int kind, int64_t 
   scan_exclusive_i64(counts, c->lb_offs.p, cnt, c->ws, s);
 }
 
+// row_offsets into caller-given buffers on a given stream (the fronts).
+void row_offsets_into(mf_ctx* c, const int32_t* list, int64_t cnt, DBuf<int64_t>& offs, Scratch& ws,
+                      cudaStream_t s) {
+  offs.reserve(2 * cnt + 2);
+  int64_t* counts = offs.p + cnt + 1;
+  if (cnt > 0)
+    MF_K(k_row_counts<<<grid_for(cnt), kTB, 0, s>>>(c->view(), list, cnt, kCntAll, c->rowcid.p, 0, c->bval.p, 0,
+                                                   c->v2i.p, counts));
+  scan_exclusive_i64(counts, offs.p, cnt, ws, s);
+}
+
+// Buffers of both fronts at their largest sizes for a batch of m updates, so
+// that no front allocates while another stream may use its memory.
+void front_reserve(mf_ctx* c, int64_t m) {
+  const int64_t words = ((int64_t)c->n + 31) / 32;
+  const int64_t bblocks = (words + kBitsWords - 1) / kBitsWords;
+  const int64_t max_ns = 2 * std::min<int64_t>(m, kMaxBatchEdges);
+  for (auto& f : c->front) {
+    f.bits.reserve(std::max<int64_t>(2 * words, 1));
+    f.bits_sums.reserve(bblocks + 1);
+    f.uacc.reserve(std::max<int64_t>(max_ns, 1));
+    f.hlist.reserve(std::max<int32_t>(c->n, 1));
+    f.cands.reserve(kMaxRows);
+    f.lb_offs.reserve(2 * max_ns + 2);
+    f.cnt.reserve(2);
+  }
+}
+
+// Front of a sub-batch with `ns` seeds: hop-1 and seed bitmaps, the hop-1
+// list and the candidate list in ascending id (no row map yet), and the
+// packed-size upper bound; cnt[0] = (hop-1 << 32 | candidates), cnt[1] =
+// bound.  Everything on stream `st`; it reads only the graph, the seeds and
+// the per-batch size caches.
+void front_compute(mf_ctx* c, Front& f, const int32_t* seeds, int64_t ns, cudaStream_t st) {
+  const GraphView g = c->view();
+  const int32_t n = c->n;
+  const int64_t words = ((int64_t)n + 31) / 32;
+  const int64_t bblocks = (words + kBitsWords - 1) / kBitsWords;
+  uint32_t* hbits = f.bits.p;
+  uint32_t* sbits = f.bits.p + words;
+  MF_CUDA(cudaMemsetAsync(hbits, 0, sizeof(uint32_t) * (size_t)(2 * words), st));
+  MF_CUDA(cudaMemsetAsync(f.uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), st));
+  MF_CUDA(cudaMemsetAsync(f.cnt.p + 1, 0, sizeof(int64_t), st));
+  row_offsets_into(c, seeds, ns, f.lb_offs, f.ws, st);
+  MF_K(k_lb_hop1_bound<<<lb_grid(c, k_lb_hop1_bound), kTB, 0, st>>>(g, seeds, f.lb_offs.p, ns, hbits, f.uacc.p,
+                                                                    c->work.p + 2 * kStHop1));
+  if (ns > 0) MF_K(k_seed_bits<<<grid_for(ns), kTB, 0, st>>>(seeds, ns, sbits));
+  const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
+  MF_K(k_bits_reduce<<<(unsigned)bblocks, kBitsThreads, 0, st>>>(hbits, sbits, words, f.bits_sums.p));
+  MF_K(k_bits_scan_sums<<<1, kBitsThreads, 0, st>>>(f.bits_sums.p, bblocks, f.cnt.p));
+  MF_K(k_bits_compact<<<(unsigned)bblocks, kBitsThreads, 0, st>>>(hbits, sbits, words, f.bits_sums.p, capc, ns,
+                                                                  f.hlist.p, f.cands.p, nullptr));
+  MF_K(k_bound_finish<<<lb_grid(c, k_bound_finish), kTB, 0, st>>>(
+      g, seeds, ns, f.cands.p, f.cnt.p, capc, f.uacc.p, c->n2cache.p, c->n2stamp.p, c->n2bound.p, c->n2bstamp.p,
+      c->n2batch, reinterpret_cast<unsigned long long*>(f.cnt.p + 1)));
+}
+
 double host_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -2499,6 +2563,12 @@ void process_batch(mf_ctx* c, int64_t m) {
   };
   plan(0);
 
+  // the first sub-batch's front, on this stream
+  front_reserve(c, m);
+  int cur = 0;
+  bool front_on_b = false;
+  front_compute(c, c->front[0], c->seeds_all.p, seed_end.empty() ? 0 : seed_end[0], s);
+
   int64_t p = 0;
   while (p < m) {
     if (kidx >= cuts.size()) MF_FAIL(MF_ESTATE, "sub-batch plan ended before the batch");
@@ -2512,46 +2582,30 @@ void process_batch(mf_ctx* c, int64_t m) {
       MF_K(k_seed_rows<<<grid_for(ns), kTB, 0, s>>>(c->seeds_all.p + seed_base, ns, c->seeds.p, c->v2i.p));
     const int64_t max_before = c->max_csr;
 
-    // ---- hop-1 set, candidates in ascending id
+    // ---- hop-1 set and size bound: this sub-batch's front (computed on the
+    // second stream while the previous sub-batch ran, or just now for the
+    // first one); its lists become the context's
     sc.emplace(c, kStHop1);
     next_epoch(c);
     const uint32_t ep = c->epoch;
-    row_offsets(c, c->seeds.p, ns, kCntAll, ns, ep);
-    const int64_t words = ((int64_t)n + 31) / 32;
-    const int64_t bblocks = (words + kBitsWords - 1) / kBitsWords;
-    c->hbits.reserve(std::max<int64_t>(2 * words, 1));
-    c->bits_sums.reserve(bblocks + 1);
-    uint32_t* hbits = c->hbits.p;
-    uint32_t* sbits = c->hbits.p + words;
-    MF_CUDA(cudaMemsetAsync(hbits, 0, sizeof(uint32_t) * (size_t)(2 * words), s));
-    c->uacc.reserve(std::max<int64_t>(ns, 1));
-    MF_CUDA(cudaMemsetAsync(c->uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), s));
-    MF_K(k_lb_hop1_bound<<<lb_grid(c, k_lb_hop1_bound), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, hbits, c->uacc.p,
-                                                                     c->work.p + 2 * kStHop1));
-    if (ns > 0) MF_K(k_seed_bits<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, sbits));
-    const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
-    MF_K(k_bits_reduce<<<(unsigned)bblocks, kBitsThreads, 0, s>>>(hbits, sbits, words, c->bits_sums.p));
-    // packed counts (hop-1 << 32 | candidates) at i64a[n], where the size bound reads them
-    MF_K(k_bits_scan_sums<<<1, kBitsThreads, 0, s>>>(c->bits_sums.p, bblocks, c->i64a.p + n));
-    MF_K(k_bits_compact<<<(unsigned)bblocks, kBitsThreads, 0, s>>>(hbits, sbits, words, c->bits_sums.p, capc, ns,
-                                                                   c->hlist.p, c->cands.p, c->v2i.p));
+    Front& fr = c->front[cur];
+    if (front_on_b) MF_CUDA(cudaStreamWaitEvent(s, c->ev_b, 0));
+    std::swap(c->hlist, fr.hlist);
+    std::swap(c->cands, fr.cands);
 
     // ---- packed sizes (upper bound) and MAX_CSR_ELEMENTS growth; one host
     // round trip for the hop-1 counts and the bound
     sc.emplace(c, kStSizes);
-    MF_CUDA(cudaMemsetAsync(cnt + 4, 0, sizeof(int64_t), s));
-    MF_K(k_bound_finish<<<lb_grid(c, k_bound_finish), kTB, 0, s>>>(g, c->seeds.p, ns, c->cands.p, c->i64a.p + n,
-                                                                   capc, c->uacc.p, c->n2cache.p, c->n2stamp.p,
-                                                                   c->n2bound.p, c->n2bstamp.p, c->n2batch,
-                                                                   ucnt + 4));
-    MF_CUDA(cudaMemcpyAsync(h + 2, c->i64a.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    MF_CUDA(cudaMemcpyAsync(h + 4, cnt + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaMemcpyAsync(h + 2, fr.cnt.p, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
+    h[4] = h[3];
     h[3] = h[2] & 0xffffffffll;
     h[2] = h[2] >> 32;
     const int64_t nh = h[2];
+    const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
     const int64_t nct = std::min<int64_t>(h[3], capc);
     const int64_t rows = ns + nct;
+    if (nct > 0) MF_K(k_cand_v2i<<<grid_for(nct), kTB, 0, s>>>(c->cands.p, nct, ns, c->v2i.p));
     int64_t packed = -1;
     const bool exact = h[4] >= c->max_csr;
     if (exact) {
@@ -2578,6 +2632,28 @@ void process_batch(mf_ctx* c, int64_t m) {
       }
     }
     MF_CUDA(cudaGetLastError());
+
+    // ---- the next sub-batch: re-plan after a growth of the limit, then its
+    // front on the second stream, after everything issued so far on this one
+    size_t kidx_next = kidx + 1;
+    int64_t seed_base_next = seed_end[kidx];
+    if (c->max_csr != max_before && q < m) {
+      plan(q);  // the cuts after a growth follow the new limit
+      kidx_next = 0;
+      seed_base_next = 0;
+    }
+    front_on_b = false;
+    if (q < m) {
+      if (kidx_next >= cuts.size()) MF_FAIL(MF_ESTATE, "sub-batch plan ended before the batch");
+      const int64_t ns_next = seed_end[kidx_next] - seed_base_next;
+      MF_CUDA(cudaEventRecord(c->ev_a, s));
+      MF_CUDA(cudaStreamWaitEvent(c->stream_b, c->ev_a, 0));
+      g_alloc_stream = c->stream_b;   // any scratch the front's scans grow belongs to its stream
+      front_compute(c, c->front[cur ^ 1], c->seeds_all.p + seed_base_next, ns_next, c->stream_b);
+      g_alloc_stream = s;
+      MF_CUDA(cudaEventRecord(c->ev_b, c->stream_b));
+      front_on_b = true;
+    }
 
     // ---- clustering (bulk-synchronous); counts stay on the device
     sc.emplace(c, kStFirst);
@@ -2699,10 +2775,11 @@ void process_batch(mf_ctx* c, int64_t m) {
     c->stats.clusters += cc;
     c->stats.processed_edges += nproc;
     p = q;
-    seed_base = seed_end[kidx];
-    ++kidx;
-    if (c->max_csr != max_before && p < m) plan(p);  // the cuts after a growth follow the new limit
+    seed_base = seed_base_next;
+    kidx = kidx_next;
+    cur ^= 1;
   }
+  if (front_on_b) MF_CUDA(cudaStreamSynchronize(c->stream_b));
   c->stats.max_csr = c->max_csr;
 }
 
