@@ -225,9 +225,14 @@ void run_batch(mf_ctx* c, int64_t m) {
     // 4 B row entry + 8 B state read and cid write per pushed element
     c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + x[2]);
     c->stage_bytes[mf::kStPushHop] += 12.0 * (double)x[1];
-    if (debug)
+    if (debug) {
       std::fprintf(stderr, "[misfit_gb] batch: push elements seed %llu hop %llu cand %llu; sub-batches %lld\n", x[0],
                    x[1], x[2], (long long)c->stats.sub_batches);
+      std::fprintf(stderr, "[misfit_gb] first hits: calls %lld rows %lld warp-level %lld chunk-level %lld chunks %lld\n",
+                   (long long)c->dbg_first[0], (long long)c->dbg_first[1], (long long)c->dbg_first[2],
+                   (long long)c->dbg_first[3], (long long)c->dbg_first[4]);
+      for (auto& v : c->dbg_first) v = 0;
+    }
   }
   if (c->profile) {
     // algorithmic bytes per stage from the device work counters:

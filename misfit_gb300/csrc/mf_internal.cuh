@@ -500,6 +500,7 @@ struct mf_ctx {
   double stage_bytes[mf::kStCount] = {};
   mf::DBuf<int64_t> lb_offs;           // row-position prefix for lb_rows
   int64_t touched_total = 0;
+  int64_t dbg_first[5] = {};           // debug: first-hit calls, rows, warp-level rows, chunk rows, chunks
 
   // pinned staging for host-input batches
   uint8_t* h_stage = nullptr;

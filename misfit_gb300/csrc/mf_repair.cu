@@ -2303,6 +2303,17 @@ void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, 
   MF_K(k_first_probe<<<lb_grid(c, k_first_probe<P>), kTB, 0, s>>>(g, list, dcnt, pred, c->fpos.p, q));
   MF_K(k_first_warp<<<lb_grid(c, k_first_warp<P>), kTB, 0, s>>>(g, pred, c->fpos.p, q));
   MF_K(k_first_chunks<<<lb_grid(c, k_first_chunks<P>), kTB, 0, s>>>(g, pred, c->fpos.p, q));
+  if (debug_counters()) {
+    unsigned long long v[3] = {0, 0, 0};
+    MF_CUDA(cudaStreamSynchronize(s));
+    MF_CUDA(cudaMemcpy(v, dcnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    MF_CUDA(cudaMemcpy(v + 1, ucnt + 48, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost));
+    c->dbg_first[0] += 1;
+    c->dbg_first[1] += (int64_t)v[0];
+    c->dbg_first[2] += (int64_t)v[1];
+    c->dbg_first[3] += (int64_t)(v[2] >> kChunkShift);
+    c->dbg_first[4] += (int64_t)(v[2] & kChunkMask);
+  }
 }
 
 void next_epoch(mf_ctx* c) {
