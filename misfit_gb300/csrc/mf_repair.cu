@@ -2574,7 +2574,10 @@ void process_batch(mf_ctx* c, int64_t m) {
   };
   plan(0);
 
-  // the first sub-batch's front, on this stream
+  // the first sub-batch's front, on this stream.  Later fronts overlap the
+  // previous sub-batch on the second stream for large graphs; for small ones
+  // the stream switch costs more than the front, which then runs inline.
+  const bool overlap_fronts = c->n >= (1 << 20);
   front_reserve(c, m);
   int cur = 0;
   bool front_on_b = false;
@@ -2657,13 +2660,17 @@ void process_batch(mf_ctx* c, int64_t m) {
     if (q < m) {
       if (kidx_next >= cuts.size()) MF_FAIL(MF_ESTATE, "sub-batch plan ended before the batch");
       const int64_t ns_next = seed_end[kidx_next] - seed_base_next;
-      MF_CUDA(cudaEventRecord(c->ev_a, s));
-      MF_CUDA(cudaStreamWaitEvent(c->stream_b, c->ev_a, 0));
-      g_alloc_stream = c->stream_b;   // any scratch the front's scans grow belongs to its stream
-      front_compute(c, c->front[cur ^ 1], c->seeds_all.p + seed_base_next, ns_next, c->stream_b);
-      g_alloc_stream = s;
-      MF_CUDA(cudaEventRecord(c->ev_b, c->stream_b));
-      front_on_b = true;
+      if (overlap_fronts) {
+        MF_CUDA(cudaEventRecord(c->ev_a, s));
+        MF_CUDA(cudaStreamWaitEvent(c->stream_b, c->ev_a, 0));
+        g_alloc_stream = c->stream_b;   // any scratch the front's scans grow belongs to its stream
+        front_compute(c, c->front[cur ^ 1], c->seeds_all.p + seed_base_next, ns_next, c->stream_b);
+        g_alloc_stream = s;
+        MF_CUDA(cudaEventRecord(c->ev_b, c->stream_b));
+        front_on_b = true;
+      } else {
+        front_compute(c, c->front[cur ^ 1], c->seeds_all.p + seed_base_next, ns_next, s);
+      }
     }
 
     // ---- clustering (bulk-synchronous); counts stay on the device
