@@ -201,6 +201,13 @@ int mf_write_mis_file(const char* path, const uint8_t* mis, int32_t n);
  * (core/cli_setup.h:66-82).  *u and *v are malloc'd 0-based arrays the
  * caller releases with mf_free. */
 int mf_read_batch_file(const char* path, int32_t n, int32_t** u, int32_t** v, int64_t* m);
+
+/* The same parse on the device of ctx, with the same line rules, followed by
+ * the flags against the context's current graph (mf_flag_updates): one call
+ * replaces parse_batch_file plus its isAdjacent flagging
+ * (core/cli_setup.h:66-82).  *u, *v, *ins are malloc'd arrays of *m
+ * entries the caller releases with mf_free. */
+int mf_parse_batch_file(mf_ctx* ctx, const char* path, int32_t** u, int32_t** v, uint8_t** ins, int64_t* m);
 /* Regular files of a folder sorted by the integer value of their stem
  * (core/cli_setup.h:49-59); names joined by '\n' into a malloc'd string. */
 int mf_list_batch_files(const char* folder, char** names, int64_t* count);

@@ -783,6 +783,38 @@ int mf_read_batch_file(const char* path, int32_t n, int32_t** u, int32_t** v, in
   });
 }
 
+int mf_parse_batch_file(mf_ctx* c, const char* path, int32_t** u, int32_t** v, uint8_t** ins, int64_t* m) {
+  return guarded([&] {
+    need(c && path && u && v && ins && m, MF_EINVAL, "null argument");
+    *u = nullptr;
+    *v = nullptr;
+    *ins = nullptr;
+    *m = 0;
+    bind(c);
+    const int64_t cnt = mf::parse_batch_file_device(c, path);
+    if (cnt > 0) mf::flag_updates(c, cnt);
+    const size_t k = (size_t)std::max<int64_t>(cnt, 1);
+    *u = (int32_t*)std::malloc(sizeof(int32_t) * k);
+    *v = (int32_t*)std::malloc(sizeof(int32_t) * k);
+    *ins = (uint8_t*)std::malloc(k);
+    if (!*u || !*v || !*ins) {
+      std::free(*u);
+      std::free(*v);
+      std::free(*ins);
+      *u = *v = nullptr;
+      *ins = nullptr;
+      MF_FAIL(MF_ENOMEM, "host allocation failed");
+    }
+    if (cnt > 0) {
+      MF_CUDA(cudaMemcpyAsync(*u, c->bu.p, sizeof(int32_t) * (size_t)cnt, cudaMemcpyDeviceToHost, c->stream));
+      MF_CUDA(cudaMemcpyAsync(*v, c->bv.p, sizeof(int32_t) * (size_t)cnt, cudaMemcpyDeviceToHost, c->stream));
+      MF_CUDA(cudaMemcpyAsync(*ins, c->bins.p, (size_t)cnt, cudaMemcpyDeviceToHost, c->stream));
+      MF_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    *m = cnt;
+  });
+}
+
 int mf_list_batch_files(const char* folder, char** names, int64_t* count) {
   return guarded([&] {
     need(folder && names && count, MF_EINVAL, "null argument");

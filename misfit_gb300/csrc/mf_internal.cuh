@@ -633,6 +633,8 @@ void rebase(mf_ctx* c);
 void greedy_mis(mf_ctx* c, uint8_t* d_out);
 void check_mis(mf_ctx* c, int64_t* viol, int64_t* uncovered);
 void exact_fixup(mf_ctx* c);                       // exact-MIS mode after a batch
+// mf_parse.cu: batch file -> c->bu / c->bv (valid lines, file order); returns the count
+int64_t parse_batch_file_device(mf_ctx* c, const char* path);
 // mf_repair.cu
 void process_batch(mf_ctx* c, int64_t m);          // everything after the overlay apply
 int64_t initial_max_csr(int32_t n, uint64_t edges);

@@ -4,9 +4,9 @@
 // Same 5 positional arguments (src/misfit/misfit.cu:737-743,
 // core/cli_setup.h:28-41), same inputs and outputs:
 //   * batch files: every regular file of the folder, ordered by the integer
-//     value of its stem, the first <num_batches> parsed before any batch runs,
-//     each line's insert/delete flag taken against the base graph
-//     (src/misfit/misfit.cu:802-828);
+//     value of its stem, the first <num_batches> parsed (on the device) before
+//     any batch runs, each line's insert/delete flag taken against the base
+//     graph (src/misfit/misfit.cu:802-828);
 //   * final MIS written 1-based to datasets/Final_MISs/<stem>_flash_final_mis.txt
 //     under the current directory (src/misfit/misfit.cu:892-907);
 //   * end-of-run compaction over the input .egr unless
@@ -110,20 +110,19 @@ int main(int argc, char** argv) {
   for (const auto& f : files) {
     if ((int)batches.size() >= num_batches) break;
     const std::string path = (std::filesystem::path(argv[3]) / f).string();
+    // parsed and flagged on the device, against the base graph (no batch has run yet)
     int32_t *u = nullptr, *v = nullptr;
+    uint8_t* ins = nullptr;
     int64_t m = 0;
-    st = mf_read_batch_file(path.c_str(), n, &u, &v, &m);
+    st = mf_parse_batch_file(ctx, path.c_str(), &u, &v, &ins, &m);
     if (st != MF_OK) return fail("reading a batch file", st);
     Batch b;
     b.u.assign(u, u + m);
     b.v.assign(v, v + m);
+    b.ins.assign(ins, ins + m);
     mf_free(u);
     mf_free(v);
-    b.ins.resize((size_t)m);
-    if (m > 0) {
-      st = mf_flag_updates(ctx, b.u.data(), b.v.data(), m, b.ins.data());
-      if (st != MF_OK) return fail("flagging a batch", st);
-    }
+    mf_free(ins);
     batches.push_back(std::move(b));
   }
   const int nb = (int)batches.size();

@@ -20,7 +20,7 @@ EXPORTS = [
     "mf_flag_updates", "mf_flag_updates_noalloc", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_sync",
     "mf_last_batch_stats", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
     "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_set_exact", "mf_compact", "mf_read_mis_file",
-    "mf_write_mis_file", "mf_read_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
+    "mf_write_mis_file", "mf_read_batch_file", "mf_parse_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
     "mf_trace_count", "mf_trace_get", "mf_stage_name", "mf_profile_enable", "mf_profile_reset",
     "mf_profile_read", "mf_kernel_launches",
     "mf_pool_create", "mf_pool_destroy", "mf_pool_add_graph", "mf_pool_submit", "mf_pool_wait", "mf_pool_drain",
@@ -106,6 +106,7 @@ def _lib():
         "mf_read_mis_file": (C.c_int, [C.c_char_p, C.c_int32, _U8P, _I64P]),
         "mf_write_mis_file": (C.c_int, [C.c_char_p, _U8P, C.c_int32]),
         "mf_read_batch_file": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(_I32P), C.POINTER(_I32P), _I64P]),
+        "mf_parse_batch_file": (C.c_int, [_P, C.c_char_p, C.POINTER(_I32P), C.POINTER(_I32P), C.POINTER(_U8P), _I64P]),
         "mf_list_batch_files": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), _I64P]),
         "mf_free": (None, [C.c_void_p]),
         "mf_stage_name": (C.c_char_p, [C.c_int]),
@@ -276,6 +277,23 @@ class Graph:
     @max_csr.setter
     def max_csr(self, value):
         _check(_lib().mf_set_max_csr(self._h, int(value)), "mf_set_max_csr")
+
+    def parse_batch_file(self, path):
+        """mf_parse_batch_file: (u, v, ins) of a batch file, parsed and flagged on the device."""
+        pu, pv, pi = _I32P(), _I32P(), _U8P()
+        m = C.c_int64()
+        _check(_lib().mf_parse_batch_file(self._h, os.fsencode(path), C.byref(pu), C.byref(pv), C.byref(pi),
+                                          C.byref(m)), "mf_parse_batch_file")
+        try:
+            k = m.value
+            u = np.ctypeslib.as_array(pu, shape=(max(k, 1),))[:k].copy()
+            v = np.ctypeslib.as_array(pv, shape=(max(k, 1),))[:k].copy()
+            ins = np.ctypeslib.as_array(pi, shape=(max(k, 1),))[:k].copy()
+        finally:
+            _lib().mf_free(C.cast(pu, C.c_void_p))
+            _lib().mf_free(C.cast(pv, C.c_void_p))
+            _lib().mf_free(C.cast(pi, C.c_void_p))
+        return u, v, ins
 
     def set_exact(self, on=True):
         """Exact-MIS mode: independent, maximal membership after every batch."""
