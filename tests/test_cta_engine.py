@@ -1,0 +1,116 @@
+"""The batched form's one-CTA engine (misfit_gb300/csrc/mf_cta.cuh), run on
+the CPU by an emulated CTA, against the oracle batch by batch: membership,
+cluster ids, overlay rows, degrees, MAX_CSR_ELEMENTS and sub-batch counts.
+The same source is the persistent kernel on the GPU
+(tests/test_gpu_batched.py holds that one against the plain path)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from misfit_gb300 import workloads as W
+from tests import _golden as G
+from tests.cta_emul import EmulGraph
+
+
+def _compare(orc, eg, ctx, rows=True):
+    assert np.array_equal(eg.get_mis(), orc.get_mis()), ctx
+    assert np.array_equal(eg.cluster_ids(), orc.cluster_ids()), ctx
+    assert np.array_equal(eg.degrees(), orc.degrees()), ctx
+    assert eg.max_csr == orc.max_csr, ctx
+    if rows:
+        for x in range(orc.n):
+            assert np.array_equal(eg.row(x), orc.row(x)), (ctx, x)
+
+
+def _run(nindex, nlist, batches, threads, mis=None, max_csr=None, rows=True):
+    orc = O.Oracle.from_csr(nindex, nlist)
+    eg = EmulGraph(nindex, nlist)
+    assert eg.max_csr == orc.max_csr
+    if max_csr is not None:
+        orc.max_csr = max_csr
+        eg.max_csr = max_csr
+    if mis is None:
+        mis = O.greedy_mis(nindex, nlist)
+    orc.set_mis(mis)
+    eg.set_mis(mis)
+    for i, (u, v, ins) in enumerate(batches):
+        ns_o = orc.apply_batch(u, v, ins)
+        ns_e = eg.apply_batch(u, v, ins, threads=threads)
+        assert ns_o == ns_e, (i, ns_o, ns_e)
+        _compare(orc, eg, i, rows)
+    return orc, eg
+
+
+@pytest.mark.parametrize("name", G.NAMES)
+def test_engine_golden_streams(name):
+    g = G.load(name)
+    max_csr = int(g["max_csr"]) if "max_csr" in g else None
+    _run(g["nindex"], g["nlist"], G.batches(g), threads=7, mis=g["mis0"], max_csr=max_csr)
+
+
+@pytest.mark.parametrize("threads", [1, 32, 64])
+def test_engine_er_insert_delete(threads):
+    n = 600
+    nindex, nlist = W.er_graph(n, 6, 3)
+    st = W.ToggleStream(n, nindex, nlist, 5)
+    orc = O.Oracle.from_csr(nindex, nlist)
+    batches = []
+    for _ in range(4):
+        u, v = st.next_batch(150)
+        batches.append((u, v, orc.flag_updates(u, v)))
+    _run(nindex, nlist, batches, threads)
+
+
+def test_engine_forced_growth_and_cuts():
+    """A small MAX_CSR_ELEMENTS: many sub-batches, exact sizes and growth."""
+    n, (nindex, nlist) = W.rmat_graph(9, 8, 4)
+    st = W.ToggleStream(n, nindex, nlist, 9)
+    orc = O.Oracle.from_csr(nindex, nlist)
+    batches = []
+    for _ in range(3):
+        u, v = st.next_batch(300)
+        batches.append((u, v, orc.flag_updates(u, v)))
+    orc, eg = _run(nindex, nlist, batches, threads=33, max_csr=3000)
+    assert eg.max_csr > 3000           # the limit grew
+    assert eg.last()[8] > 0            # sub-batches that needed exact sizes
+    assert eg.last()[3] > 1            # several sub-batches
+
+
+def test_engine_free_flags_and_repeats():
+    """Random flags that disagree with adjacency, pairs repeated inside a
+    batch and across batches: every overlay transition (append, kill,
+    tombstone, un-tombstone, re-append)."""
+    rng = np.random.default_rng(12)
+    n = 120
+    nindex, nlist = W.er_graph(n, 5, 8)
+    batches = []
+    pool_u = rng.integers(0, n, 60)
+    pool_v = rng.integers(0, n, 60)
+    keep = pool_u != pool_v
+    pool_u, pool_v = pool_u[keep], pool_v[keep]
+    ui, vi = W.undirected_pairs(n, nindex, nlist)
+    for b in range(5):
+        k = 200
+        pick = rng.integers(0, pool_u.size, k // 2)
+        e = rng.integers(0, ui.size, k // 2)
+        u = np.concatenate([pool_u[pick], ui[e]]).astype(np.int32)
+        v = np.concatenate([pool_v[pick], vi[e]]).astype(np.int32)
+        sw = rng.random(u.size) < 0.5
+        u[sw], v[sw] = v[sw], u[sw].copy()
+        perm = rng.permutation(u.size)
+        u, v = u[perm], v[perm]
+        ins = (rng.random(u.size) < 0.5).astype(np.uint8)
+        batches.append((u, v, ins))
+    _run(nindex, nlist, batches, threads=16)
+
+
+def test_engine_rgg_stream():
+    nindex, nlist = W.rgg_graph(800, 12, 21)
+    n = nindex.size - 1
+    st = W.ToggleStream(n, nindex, nlist, 22)
+    orc = O.Oracle.from_csr(nindex, nlist)
+    batches = []
+    for mode in ("uniform", "low-degree"):
+        u, v = st.next_batch(400, endpoints=mode.replace("-", "_"))
+        batches.append((u, v, orc.flag_updates(u, v)))
+    _run(nindex, nlist, batches, threads=32, rows=False)
