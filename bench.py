@@ -326,9 +326,13 @@ def run_served(args, graphs, mis0):
 def run_batched(args, graphs, mis0):
     """Batched form at reduced scale: independent graphs, one batch each
     (log-uniform 10..50,000 toggles, low-degree and uniform endpoints 50/50),
-    all submitted at once to a pool with room for every graph, against the
-    plain per-graph loop.  Same graphs as the served form, from their initial
-    state."""
+    all applied in one mf_apply_batches step -- the batches one CTA can carry
+    in one persistent kernel driven by a device work queue and launched as a
+    CUDA graph, the rest through the multi-launch path meanwhile -- with the
+    kernel's settings chosen by the autotuner on this workload.  Compared
+    with the plain per-graph loop and with the serving pool given every
+    batch at once; per-graph memberships must be identical."""
+    from misfit_gb300 import autotune
     from misfit_gb300 import workloads as W
     rng = np.random.default_rng(12)
     reqs = []
@@ -338,14 +342,31 @@ def run_batched(args, graphs, mis0):
         mode = "low_degree" if k % 2 == 0 else "uniform"
         u, v, ins = ts.next_batch(size, endpoints=mode, with_flags=True)
         reqs.append((0.0, k, u, v, ins))
+    batches = [(u, v, ins) for _, _, u, v, ins in reqs]
+    updates = sum(int(b[0].size) for b in batches)
     p_rate, _, p_mis = plain_loop(graphs, mis0, reqs)
     s_rate, _, s_mis, st = pooled(graphs, mis0, reqs, args.served_workers, 1.0)
+    opts, report = autotune.tune_batched(graphs, mis0, batches, use_cache=False)
+    secs, b_mis, bst = [], None, None
+    for _ in range(3):
+        sec, b_mis, bst = autotune.run_step(graphs, mis0, batches, opts)
+        secs.append(sec)
+    b_rate = updates / float(np.median(secs))
     same = all(np.array_equal(a, b) for a, b in zip(p_mis, s_mis))
+    same_b = all(np.array_equal(a, b) for a, b in zip(p_mis, b_mis))
+    chosen = {k: getattr(opts, k) for k, _ in opts._fields_}
     return {
         "workload": "%d RGGs (n log-uniform 1e3..2e5), one batch each of log-uniform 10..50000 toggles" % len(graphs),
-        "value": s_rate, "unit": UNIT, "workers": args.served_workers,
+        "value": b_rate, "unit": UNIT,
+        "step_ms": float(np.median(secs)) * 1e3, "kernel_ms": bst["kernel_ms"],
+        "kernel_items": bst["kernel_items"], "path_items": bst["path_items"],
+        "kernel_updates": int(sum(int(b[0].size) for b in batches if b[0].size <= chosen["max_cta_updates"])),
+        "autotuned": chosen, "autotune_trials": [(t["opts"], round(t["seconds"] * 1e3, 2)) for t in report["trials"]],
         "plain_loop": {"value": p_rate, "unit": UNIT},
-        "identical_to_plain_loop": bool(same), "timing": "host wall clock, host buffers in and out",
+        "pool": {"value": s_rate, "unit": UNIT, "workers": args.served_workers,
+                 "identical_to_plain_loop": bool(same)},
+        "identical_to_plain_loop": bool(same_b),
+        "timing": "host wall clock of one step on fresh contexts (median of 3), host buffers in, memberships out",
     }
 
 

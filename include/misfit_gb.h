@@ -300,6 +300,45 @@ int mf_pool_stats_get(mf_pool* pool, mf_pool_stats* out);
 /* Changes the budget; it applies from the next admission on. */
 int mf_pool_set_budget(mf_pool* pool, int64_t hbm_budget);
 
+/* ---- batched form: one batch for each of many graphs in one step ---------
+ * No reference counterpart (the reference runs one graph per process; this
+ * is the batched multi-graph form, with per-graph results equal to
+ * mf_apply_batch's on each context).  Batches small enough for one CTA run
+ * together in ONE persistent kernel: each CTA takes the next graph batch
+ * from a device work queue (largest first) and runs that graph's whole path
+ * -- overlay apply, split rule, neighbourhoods, clustering, assignment,
+ * repair, clear -- with no host round trip.  The step (batch upload, queue
+ * reset, the kernel, the read-back of the per-graph results) is captured
+ * and launched as one CUDA graph.  Larger batches, graphs above the vertex
+ * limit and contexts in exact-MIS mode take the multi-launch path
+ * (mf_apply_batch) on their own streams while the persistent kernel runs. */
+typedef struct mf_batched_opts {
+  int block;                  /* threads per persistent CTA: 64..1024, a multiple of 32 (default 512) */
+  int ctas_per_sm;            /* persistent CTAs per SM (default 2) */
+  int64_t max_cta_updates;    /* batches of at most this many lines take the kernel (default 8192) */
+  int32_t max_cta_vertices;   /* ... on graphs of at most this many vertices (default 2^20) */
+  int use_graph;              /* 1: capture the step as a CUDA graph (default), 0: plain launches */
+} mf_batched_opts;
+
+typedef struct mf_batched_stats {
+  int64_t kernel_items;       /* batches run by the persistent kernel */
+  int64_t path_items;         /* batches run through the multi-launch path */
+  int64_t updates;            /* lines over all batches */
+  double kernel_ms;           /* device time of the persistent-kernel step (CUDA events) */
+  double wall_ms;             /* host time of the whole call */
+} mf_batched_stats;
+
+int mf_batched_default_opts(mf_batched_opts* out);
+/* Applies batch i (u[i], v[i], ins[i]: m[i] host lines, same meaning as
+ * mf_apply_batch) to ctxs[i] for i < count, all in one step.  The contexts
+ * must be distinct, on one GPU, with no asynchronous batch pending.  Every
+ * batch is checked (ids in range, no self-loop) before anything runs, so a
+ * bad batch changes no graph.  opts may be NULL (defaults); stats may be
+ * NULL.  Each context's mf_last_batch_stats describes its batch afterwards. */
+int mf_apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* const* v,
+                     const uint8_t* const* ins, const int64_t* m, int64_t count, const mf_batched_opts* opts,
+                     mf_batched_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

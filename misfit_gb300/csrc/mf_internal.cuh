@@ -465,6 +465,11 @@ struct mf_ctx {
   mf::DBuf<int32_t> rq_idx, rq_v, mq_idx, mq_v;
   mf::DBuf<int64_t> mq_base;
   mf::DBuf<uint8_t> xst, xleave;      // exact-MIS mode: completion states, leave flags
+  // batched form (mf_batched.cu): per-vertex engine scratch kept between
+  // batches (clustering-write tags, row map = -1, three zero bitmaps), its
+  // tag epoch, and the per-batch scratch of one engine item
+  mf::DBuf<uint8_t> cta_vert, cta_ws;
+  uint32_t cta_epoch = 0;
   bool exact = false;                  // exact-MIS mode on
   mf::Front front[2];                 // current and next sub-batch fronts
   cudaStream_t stream_b = nullptr;    // the fronts of later sub-batches run here
@@ -533,7 +538,7 @@ void for_each_buffer(mf_ctx* c, F&& f) {
   f(c->bitmaps); f(c->heavy_bits); f(c->dense_bits); f(c->ncbits); f(c->n2stamp);
   f(c->n2bstamp); f(c->nmark);
   f(c->mis); f(c->bins); f(c->u8a); f(c->akill); f(c->creates); f(c->rp_u8); f(c->plan_flags);
-  f(c->xst); f(c->xleave);
+  f(c->xst); f(c->xleave); f(c->cta_vert); f(c->cta_ws);
   f(c->keys); f(c->app_keys); f(c->rp_keys); f(c->rp_keys2);
   f(c->big_best); f(c->fpos); f(c->work);
   f(c->ws.block_sums); f(c->ws.block_sums2); f(c->ws.hist); f(c->ws.hist_scan); f(c->ws.keys_alt);
@@ -569,7 +574,8 @@ inline void release_device_state(mf_ctx* c) {
 inline void release_batch_scratch(mf_ctx* c) {
   const void* keep[] = {&c->nindex, &c->nlist, &c->live, &c->dead, &c->rcnt, &c->deg, &c->aoff, &c->aadj,
                         &c->aown, &c->mis, &c->cid, &c->v2i, &c->bval, &c->wval, &c->f1, &c->nmark,
-                        &c->nlist_need, &c->touched, &c->hlist, &c->acnt_new, &c->aoff_alt, &c->counters};
+                        &c->nlist_need, &c->touched, &c->hlist, &c->acnt_new, &c->aoff_alt, &c->counters,
+                        &c->cta_vert};
   for_each_buffer(c, [&](auto& b) {
     for (const void* k : keep)
       if (k == static_cast<const void*>(&b)) return;

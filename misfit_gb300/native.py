@@ -25,6 +25,7 @@ EXPORTS = [
     "mf_profile_read", "mf_kernel_launches",
     "mf_pool_create", "mf_pool_destroy", "mf_pool_add_graph", "mf_pool_submit", "mf_pool_wait", "mf_pool_drain",
     "mf_pool_get_mis", "mf_pool_stats_get", "mf_pool_set_budget",
+    "mf_batched_default_opts", "mf_apply_batches",
 ]
 
 
@@ -45,6 +46,23 @@ class PoolStats(C.Structure):
         ("graphs", C.c_int64), ("completed", C.c_int64), ("updates", C.c_int64), ("errors", C.c_int64),
         ("evictions", C.c_int64), ("restores", C.c_int64), ("trims", C.c_int64), ("over_budget", C.c_int64),
         ("resident_bytes", C.c_int64), ("peak_resident_bytes", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchedOpts(C.Structure):
+    _fields_ = [
+        ("block", C.c_int), ("ctas_per_sm", C.c_int), ("max_cta_updates", C.c_int64),
+        ("max_cta_vertices", C.c_int32), ("use_graph", C.c_int),
+    ]
+
+
+class BatchedStats(C.Structure):
+    _fields_ = [
+        ("kernel_items", C.c_int64), ("path_items", C.c_int64), ("updates", C.c_int64),
+        ("kernel_ms", C.c_double), ("wall_ms", C.c_double),
     ]
 
     def as_dict(self):
@@ -126,6 +144,9 @@ def _lib():
         "mf_pool_get_mis": (C.c_int, [_P, C.c_int32, _U8P, C.c_int64]),
         "mf_pool_stats_get": (C.c_int, [_P, C.POINTER(PoolStats)]),
         "mf_pool_set_budget": (C.c_int, [_P, C.c_int64]),
+        "mf_batched_default_opts": (C.c_int, [C.POINTER(BatchedOpts)]),
+        "mf_apply_batches": (C.c_int, [C.POINTER(_P), C.POINTER(_I32P), C.POINTER(_I32P), C.POINTER(_U8P), _I64P,
+                                       C.c_int64, C.POINTER(BatchedOpts), C.POINTER(BatchedStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -454,3 +475,37 @@ class Pool:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def batched_opts(**kw):
+    """mf_batched_opts with the library defaults, then the given fields."""
+    o = BatchedOpts()
+    _check(_lib().mf_batched_default_opts(C.byref(o)), "mf_batched_default_opts")
+    for k, val in kw.items():
+        setattr(o, k, val)
+    return o
+
+
+def apply_batches(graphs, batches, opts=None):
+    """One batch per graph in one step (mf_apply_batches): graphs is a list of
+    Graph, batches a list of (u, v, ins).  Returns the step's stats dict."""
+    if len(graphs) != len(batches):
+        raise ValueError("one batch per graph")
+    k = len(graphs)
+    keep = []
+    hs = (_P * k)()
+    us, vs, ins_ = (_I32P * k)(), (_I32P * k)(), (_U8P * k)()
+    ms = np.zeros(max(k, 1), dtype=np.int64)
+    for j, (g, (u, v, ins)) in enumerate(zip(graphs, batches)):
+        u, v, ins = _i32(u), _i32(v), _u8(ins)
+        keep.extend([u, v, ins])
+        hs[j] = g._h.value
+        us[j] = _ptr(u, C.c_int32)
+        vs[j] = _ptr(v, C.c_int32)
+        ins_[j] = _ptr(ins, C.c_uint8)
+        ms[j] = u.size
+    st = BatchedStats()
+    o = opts if opts is not None else batched_opts()
+    _check(_lib().mf_apply_batches(hs, us, vs, ins_, _ptr(ms, C.c_int64), k, C.byref(o), C.byref(st)),
+           "mf_apply_batches")
+    return st.as_dict()
