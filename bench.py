@@ -68,6 +68,9 @@ def parse_args():
     ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrivals per second")
     ap.add_argument("--served-workers", type=int, default=8)
     ap.add_argument("--served-budget", type=float, default=0.6, help="HBM budget as a fraction of the footprint")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run only the batched-form leg and print its JSON (profiling runs)")
+    ap.add_argument("--no-autotune", action="store_true", help="batched leg with the library's default settings")
     return ap.parse_args()
 
 
@@ -260,12 +263,16 @@ def plain_loop(graphs, mis0, reqs):
     return updates / span, lat, out
 
 
-def pooled(graphs, mis0, reqs, workers, budget_frac):
+def pooled(graphs, mis0, reqs, workers, budget_frac, batching=None):
     """The same requests through a serving pool: submitted at their arrival
     times, served by `workers` threads under budget_frac of the graphs' HBM
-    footprint.  Returns (updates/s, latencies ms, memberships, pool stats)."""
+    footprint (with `batching` mf_batched_opts: small requests in
+    continuous-batching steps of the persistent kernel).  Returns
+    (updates/s, latencies ms, memberships, pool stats)."""
     from misfit_gb300 import native
     pool = native.Pool(1 << 40, workers=workers)
+    if batching is not None:
+        pool.set_batching(batching)
     gids = [pool.add_graph(nindex, nlist, m) for (n, nindex, nlist), m in zip(graphs, mis0)]
     footprint = pool.stats()["resident_bytes"]
     pool.set_budget(max(1, int(footprint * budget_frac)))
@@ -286,7 +293,7 @@ def pooled(graphs, mis0, reqs, workers, budget_frac):
     return updates / span, lat, out, st
 
 
-def run_served(args, graphs, mis0):
+def run_served(args, graphs, mis0, batching=None):
     """Serving form at reduced scale: graphs drawn as in the batched form,
     requests arriving as a Poisson stream, each one batch of log-uniform
     10..20,000 toggles to a graph chosen Zipf(1.1), endpoints uniform,
@@ -308,6 +315,15 @@ def run_served(args, graphs, mis0):
     p_rate, p_lat, p_mis = plain_loop(graphs, mis0, reqs)
     s_rate, s_lat, s_mis, st = pooled(graphs, mis0, reqs, args.served_workers, args.served_budget)
     same = all(np.array_equal(a, b) for a, b in zip(p_mis, s_mis))
+    cb = None
+    if batching is not None:
+        c_rate, c_lat, c_mis, cst = pooled(graphs, mis0, reqs, args.served_workers, args.served_budget, batching)
+        cb = {"value": c_rate, "unit": UNIT, "p50_ms": float(np.percentile(c_lat, 50)),
+              "p99_ms": float(np.percentile(c_lat, 99)), "steps": cst["batched_steps"],
+              "requests_in_steps": cst["batched_requests"], "evictions": cst["evictions"],
+              "restores": cst["restores"],
+              "settings": {k: getattr(batching, k) for k, _ in batching._fields_},
+              "identical_to_plain_loop": bool(all(np.array_equal(a, b) for a, b in zip(p_mis, c_mis)))}
     return {
         "workload": "%d RGGs (n log-uniform 1e3..2e5, mean degree 4..32); %d requests, Poisson %.0f/s, "
                     "batches log-uniform 10..20000 toggles, graph Zipf(1.1), endpoints uniform/preferential/"
@@ -320,6 +336,7 @@ def run_served(args, graphs, mis0):
         "plain_loop": {"value": p_rate, "unit": UNIT, "p50_ms": float(np.percentile(p_lat, 50)),
                        "p99_ms": float(np.percentile(p_lat, 99))},
         "identical_to_plain_loop": bool(same), "timing": "host wall clock, host buffers in and out",
+        "continuous_batching": cb,
     }
 
 
@@ -346,7 +363,11 @@ def run_batched(args, graphs, mis0):
     updates = sum(int(b[0].size) for b in batches)
     p_rate, _, p_mis = plain_loop(graphs, mis0, reqs)
     s_rate, _, s_mis, st = pooled(graphs, mis0, reqs, args.served_workers, 1.0)
-    opts, report = autotune.tune_batched(graphs, mis0, batches, use_cache=False)
+    if getattr(args, "no_autotune", False):
+        from misfit_gb300 import native
+        opts, report = native.batched_opts(), {"trials": []}
+    else:
+        opts, report = autotune.tune_batched(graphs, mis0, batches, use_cache=False)
     secs, b_mis, bst = [], None, None
     for _ in range(3):
         sec, b_mis, bst = autotune.run_step(graphs, mis0, batches, opts)
@@ -367,7 +388,7 @@ def run_batched(args, graphs, mis0):
                  "identical_to_plain_loop": bool(same)},
         "identical_to_plain_loop": bool(same_b),
         "timing": "host wall clock of one step on fresh contexts (median of 3), host buffers in, memberships out",
-    }
+    }, opts
 
 
 def main():
@@ -389,6 +410,12 @@ def main():
     torch.cuda.set_device(local)
     from misfit_gb300 import build, native
     build.build()
+    if args.batched_only:
+        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        res, _ = run_batched(args, graphs, initial_mis(graphs))
+        res["gpu_launches_total"] = int(native.load_library().mf_kernel_launches())
+        print(json.dumps(res))
+        return
     n, nindex, nlist, stream = make_workload(args, "cuda:%d" % local)
     g = native.Graph.from_csr(nindex, nlist, gpu=local)
     g.set_mis(g.greedy_mis())
@@ -531,8 +558,8 @@ def main():
     if rank == 0 and not args.no_served:
         graphs = graph_set(args.served_graphs, 1000, 200000, 11)
         mis0 = initial_mis(graphs)
-        line["served"] = run_served(args, graphs, mis0)
-        line["batched"] = run_batched(args, graphs, mis0)
+        line["batched"], tuned = run_batched(args, graphs, mis0)
+        line["served"] = run_served(args, graphs, mis0, tuned)
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist_barrier()

@@ -274,6 +274,8 @@ typedef struct mf_pool_stats {
   int64_t over_budget;          /* admissions made while over the budget */
   int64_t resident_bytes;       /* device bytes of the resident graphs now */
   int64_t peak_resident_bytes;  /* the largest value seen */
+  int64_t batched_steps;        /* mf_apply_batches steps run by the batched dispatch */
+  int64_t batched_requests;     /* requests those steps carried */
 } mf_pool_stats;
 
 /* A pool on device `gpu` that keeps at most `hbm_budget` bytes of graph state
@@ -338,6 +340,15 @@ int mf_batched_default_opts(mf_batched_opts* out);
 int mf_apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* const* v,
                      const uint8_t* const* ins, const int64_t* m, int64_t count, const mf_batched_opts* opts,
                      mf_batched_stats* stats);
+/* Batched dispatch for a pool (continuous batching): with opts non-NULL,
+ * every request whose batch mf_apply_batches would give to its persistent
+ * kernel (size and vertex limits of opts, compat mode) goes to one
+ * dispatcher thread instead of the workers.  The dispatcher takes every such
+ * request that is ready -- one per graph, graphs restored under the budget
+ * first -- and applies them in one mf_apply_batches step; requests that
+ * arrive meanwhile form the next step.  Larger requests stay with the
+ * workers.  opts NULL turns it off.  Results per graph are unchanged. */
+int mf_pool_set_batching(mf_pool* pool, const mf_batched_opts* opts);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "mf_cta.cuh"
@@ -149,6 +150,47 @@ mf_batched_opts default_opts() {
 
 double host_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// The multi-launch path for the batches above the kernel's limits: each
+// one is host-driven (sizes read back between stages), so they run on
+// host threads, each graph on its own stream, largest first.  Returns the
+// first failure's status (its message in *error).
+int run_path_items(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* const* v, const uint8_t* const* ins,
+                   const int64_t* m, std::vector<int64_t> items, std::string* error) {
+  if (items.empty()) return MF_OK;
+  std::sort(items.begin(), items.end(), [&](int64_t a, int64_t b) { return m[a] > m[b]; });
+  constexpr size_t kMaxThreads = 8;
+  const size_t nt = std::min(kMaxThreads, items.size());
+  std::mutex mu;
+  size_t next = 0;
+  int status = MF_OK;
+  auto drive = [&] {
+    for (;;) {
+      int64_t i;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (next >= items.size()) return;
+        i = items[next++];
+      }
+      const int r = mf_apply_batch(ctxs[i], u[i], v[i], ins[i], m[i]);
+      if (r != MF_OK) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (status == MF_OK) {
+          status = r;
+          *error = mf_last_error();
+        }
+      }
+    }
+  };
+  if (nt == 1) {
+    drive();
+  } else {
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t) th.emplace_back(drive);
+    for (auto& t : th) t.join();
+  }
+  return status;
 }
 
 void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* const* v, const uint8_t* const* ins,
@@ -359,15 +401,8 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
     MF_CUDA(cudaEventRecord(E.e1, E.s));
 
     // the batches above the kernel's limits, on their own streams meanwhile
-    int path_status = MF_OK;
     std::string path_error;
-    for (int64_t i : path_items) {
-      const int r = mf_apply_batch(ctxs[i], u[i], v[i], ins[i], m[i]);
-      if (r != MF_OK && path_status == MF_OK) {
-        path_status = r;
-        path_error = mf::get_error();
-      }
-    }
+    const int path_status = run_path_items(ctxs, u, v, ins, m, path_items, &path_error);
     MF_CUDA(cudaSetDevice(device));
     const cudaError_t se = cudaStreamSynchronize(E.s);
     if (exec) cudaGraphExecDestroy(exec);
@@ -402,10 +437,9 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
     }
     if (path_status != MF_OK) MF_FAIL(path_status, path_error);
   } else {
-    for (int64_t i : path_items) {
-      const int r = mf_apply_batch(ctxs[i], u[i], v[i], ins[i], m[i]);
-      if (r != MF_OK) MF_FAIL(r, mf::get_error());
-    }
+    std::string path_error;
+    const int r = run_path_items(ctxs, u, v, ins, m, path_items, &path_error);
+    if (r != MF_OK) MF_FAIL(r, path_error);
   }
   stats.wall_ms = host_ms() - t_start;
   if (st) *st = stats;

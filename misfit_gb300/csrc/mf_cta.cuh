@@ -898,12 +898,22 @@ CTA_FN void run_item(const Item& it, int32_t* hist, int64_t* sh) {
       });
     }
     CTA_SYNC();
-    for (int64_t i = tid; i < R; i += nt) {
-      if (it.rowcid[i] < 0) continue;
-      seq_until(g, it.rows[i], i < S, [&](int32_t y) {
-        it.cid[y] = it.rowcid[it.win[y] & kTagMask];
-        return false;
-      });
+    // every element tagged in this epoch takes its winner's id: a sweep of
+    // the tag array when that is shorter than the rows (loose is their
+    // length), else a second walk of the rows
+    if ((int64_t)n <= loose) {
+      for (int32_t y = tid; y < n; y += nt) {
+        const uint32_t w = it.win[y];
+        if ((w >> kTagBits) == epoch) it.cid[y] = it.rowcid[w & kTagMask];
+      }
+    } else {
+      for (int64_t i = tid; i < R; i += nt) {
+        if (it.rowcid[i] < 0) continue;
+        seq_until(g, it.rows[i], i < S, [&](int32_t y) {
+          it.cid[y] = it.rowcid[it.win[y] & kTagMask];
+          return false;
+        });
+      }
     }
     CTA_SYNC();
 

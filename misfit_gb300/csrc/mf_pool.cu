@@ -138,6 +138,15 @@ struct mf_pool {
   std::deque<int32_t> ready;   // graphs with queued batches and no running one
   std::unordered_map<int64_t, Request*> reqs;
   std::vector<std::thread> workers;
+  // batched dispatch (mf_pool_set_batching): small front requests are
+  // routed to one dispatcher thread, which applies all of them that are
+  // ready in one mf_apply_batches step while later arrivals queue for the
+  // next step
+  bool batching = false;
+  mf_batched_opts bopts{};
+  std::deque<int32_t> ready_small;
+  std::condition_variable cv_batch;
+  std::thread dispatcher;
   bool stop = false;
   int64_t next_rid = 1;
   uint64_t tick = 0;
@@ -200,10 +209,151 @@ struct mf_pool {
         st.errors += 1;
       }
       if (!v.queue.empty()) {
-        ready.push_back(victim);
-        cv_work.notify_one();
+        enqueue_ready(victim);
       }
     }
+  }
+
+  bool small(const Graph& gr, const Request* rq) const {
+    return (int64_t)rq->u.size() <= bopts.max_cta_updates && gr.ctx->n <= bopts.max_cta_vertices &&
+           !gr.ctx->exact;
+  }
+
+  // A graph with a queued batch and none running becomes ready: for the
+  // dispatcher when batching is on and its front batch is small, else for
+  // the workers.  Called with the lock held.
+  void enqueue_ready(int32_t gid) {
+    const Graph& gr = graphs[(size_t)gid];
+    if (batching && !gr.queue.empty() && small(gr, gr.queue.front())) {
+      ready_small.push_back(gid);
+      cv_batch.notify_one();
+    } else {
+      ready.push_back(gid);
+      cv_work.notify_one();
+    }
+  }
+
+  void dispatch_loop() {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    while (true) {
+      cv_batch.wait(lk, [&] { return stop || !ready_small.empty(); });
+      if (stop && ready_small.empty()) return;
+      std::vector<int32_t> group;
+      while (!ready_small.empty()) {
+        const int32_t g = ready_small.front();
+        ready_small.pop_front();
+        Graph& x = graphs[(size_t)g];
+        if (x.busy || x.queue.empty()) continue;
+        if (!batching || !small(x, x.queue.front())) {
+          ready.push_back(g);
+          cv_work.notify_one();
+          continue;
+        }
+        x.busy = true;
+        group.push_back(g);
+      }
+      if (!group.empty()) run_group(lk, group);
+    }
+  }
+
+  // One batched step over the front requests of `group` (graphs marked busy).
+  void run_group(std::unique_lock<std::mutex>& lk, const std::vector<int32_t>& group) {
+    const size_t k = group.size();
+    std::vector<int> status(k, MF_OK);
+    std::vector<std::string> err(k);
+    std::vector<Request*> rqs(k);
+    for (size_t j = 0; j < k; ++j) {
+      Graph& x = graphs[(size_t)group[j]];
+      Request* rq = x.queue.front();
+      rqs[j] = rq;
+      // the step refuses a whole call with a bad batch in it: check each here
+      for (size_t t = 0; t < rq->u.size(); ++t) {
+        const int32_t a = rq->u[t], b = rq->v[t];
+        if (a < 0 || a >= x.ctx->n || b < 0 || b >= x.ctx->n || a == b) {
+          status[j] = MF_EINVAL;
+          err[j] = "update endpoints out of range or equal";
+          break;
+        }
+      }
+      if (status[j] != MF_OK || x.resident) continue;
+      make_room(lk, x.bytes, group[j]);
+      lk.unlock();
+      try {
+        mf::bind_device(x.ctx);
+        mf::restore(x.ctx, x.snap);
+      } catch (const mf::Failure& f) {
+        status[j] = f.status;
+        err[j] = mf_last_error();
+      }
+      mf::g_alloc_stream = nullptr;
+      lk.lock();
+      if (status[j] == MF_OK) {
+        x.resident = true;
+        resident_bytes += x.bytes;
+        st.restores += 1;
+      }
+    }
+    std::vector<mf_ctx*> ctxs;
+    std::vector<const int32_t*> us, vs;
+    std::vector<const uint8_t*> is;
+    std::vector<int64_t> ms;
+    const double t0 = mf::now_ms_host();
+    for (size_t j = 0; j < k; ++j) {
+      rqs[j]->t_start = t0;
+      if (status[j] != MF_OK) continue;
+      ctxs.push_back(graphs[(size_t)group[j]].ctx);
+      us.push_back(rqs[j]->u.data());
+      vs.push_back(rqs[j]->v.data());
+      is.push_back(rqs[j]->ins.data());
+      ms.push_back((int64_t)rqs[j]->u.size());
+    }
+    const mf_batched_opts opts = bopts;
+    lk.unlock();
+    int rc = MF_OK;
+    std::string rerr;
+    if (!ctxs.empty()) {
+      rc = mf_apply_batches(ctxs.data(), us.data(), vs.data(), is.data(), ms.data(), (int64_t)ctxs.size(), &opts,
+                            nullptr);
+      if (rc != MF_OK) rerr = mf_last_error();
+    }
+    std::vector<int64_t> bytes(k, -1);
+    for (size_t j = 0; j < k; ++j)
+      if (status[j] == MF_OK && rc == MF_OK) bytes[j] = mf::ctx_device_bytes(graphs[(size_t)group[j]].ctx);
+    lk.lock();
+    const double t1 = mf::now_ms_host();
+    for (size_t j = 0; j < k; ++j) {
+      const int32_t gid = group[j];
+      Graph& gr = graphs[(size_t)gid];
+      Request* rq = rqs[j];
+      if (status[j] == MF_OK && rc != MF_OK) {
+        status[j] = rc;
+        err[j] = rerr;
+      }
+      rq->t_done = t1;
+      rq->status = status[j];
+      rq->error = err[j];
+      rq->done = true;
+      if (bytes[j] >= 0) {
+        resident_bytes += bytes[j] - gr.bytes;
+        gr.bytes = bytes[j];
+      }
+      gr.trimmed = false;
+      gr.queue.pop_front();
+      gr.busy = false;
+      gr.last_use = ++tick;
+      st.completed += 1;
+      st.updates += (int64_t)rq->u.size();
+      if (status[j] != MF_OK) st.errors += 1;
+      if (!gr.queue.empty()) enqueue_ready(gid);
+    }
+    st.batched_steps += 1;
+    st.batched_requests += (int64_t)ctxs.size();
+    st.resident_bytes = resident_bytes;
+    st.peak_resident_bytes = std::max(st.peak_resident_bytes, resident_bytes);
+    cv_done.notify_all();
+    if (resident_bytes > budget) make_room(lk, 0, -1);
+    st.resident_bytes = resident_bytes;
   }
 
   void worker() {
@@ -262,8 +412,7 @@ struct mf_pool {
       st.resident_bytes = resident_bytes;
       st.peak_resident_bytes = std::max(st.peak_resident_bytes, resident_bytes);
       if (!gr.queue.empty()) {
-        ready.push_back(gid);
-        cv_work.notify_one();
+        enqueue_ready(gid);
       }
       cv_done.notify_all();
       // the batch may have grown its scratch: back under the budget
@@ -322,7 +471,9 @@ int mf_pool_destroy(mf_pool* p) {
       p->stop = true;
     }
     p->cv_work.notify_all();
+    p->cv_batch.notify_all();
     for (auto& t : p->workers) t.join();
+    if (p->dispatcher.joinable()) p->dispatcher.join();
     for (auto& gr : p->graphs) {
       if (gr.ctx) mf_close(gr.ctx);
       if (gr.snap.host) cudaFreeHost(gr.snap.host);
@@ -367,8 +518,7 @@ int mf_pool_add_graph(mf_pool* p, int32_t n, const int64_t* nindex, const int32_
       me.busy = false;
       p->st.evictions += 1;
       if (!me.queue.empty()) {
-        p->ready.push_back(id);
-        p->cv_work.notify_one();
+        p->enqueue_ready(id);
       }
     }
     p->st.graphs = (int64_t)p->graphs.size();
@@ -398,8 +548,7 @@ int mf_pool_submit(mf_pool* p, int32_t gid, const int32_t* u, const int32_t* v, 
     gr.queue.push_back(r);
     p->reqs[r->rid] = r;
     if (gr.queue.size() == 1 && !gr.busy) {
-      p->ready.push_back(gid);
-      p->cv_work.notify_one();
+      p->enqueue_ready(gid);
     }
     *rid = r->rid;
   });
@@ -462,6 +611,30 @@ int mf_pool_set_budget(mf_pool* p, int64_t hbm_budget) {
     need_arg(p != nullptr && hbm_budget > 0, "bad arguments");
     std::lock_guard<std::mutex> lk(p->mu);
     p->budget = hbm_budget;
+  });
+}
+
+int mf_pool_set_batching(mf_pool* p, const mf_batched_opts* opts) {
+  return pool_guarded([&] {
+    need_arg(p != nullptr, "null pool");
+    mf_batched_opts o{};
+    if (opts) {
+      o = *opts;
+      need_arg(o.block >= 64 && o.block <= 1024 && o.block % 32 == 0 && o.ctas_per_sm >= 1 && o.ctas_per_sm <= 32 &&
+                   o.max_cta_updates >= 0 && o.max_cta_updates <= mf::kMaxBatchEdges,
+               "bad batched options");
+    }
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->batching = opts != nullptr;
+    p->bopts = o;
+    if (p->batching && !p->dispatcher.joinable()) p->dispatcher = std::thread([p] { p->dispatch_loop(); });
+    if (!p->batching) {
+      while (!p->ready_small.empty()) {
+        p->ready.push_back(p->ready_small.front());
+        p->ready_small.pop_front();
+        p->cv_work.notify_one();
+      }
+    }
   });
 }
 

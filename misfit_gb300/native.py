@@ -25,7 +25,7 @@ EXPORTS = [
     "mf_profile_read", "mf_kernel_launches",
     "mf_pool_create", "mf_pool_destroy", "mf_pool_add_graph", "mf_pool_submit", "mf_pool_wait", "mf_pool_drain",
     "mf_pool_get_mis", "mf_pool_stats_get", "mf_pool_set_budget",
-    "mf_batched_default_opts", "mf_apply_batches",
+    "mf_batched_default_opts", "mf_apply_batches", "mf_pool_set_batching",
 ]
 
 
@@ -46,6 +46,7 @@ class PoolStats(C.Structure):
         ("graphs", C.c_int64), ("completed", C.c_int64), ("updates", C.c_int64), ("errors", C.c_int64),
         ("evictions", C.c_int64), ("restores", C.c_int64), ("trims", C.c_int64), ("over_budget", C.c_int64),
         ("resident_bytes", C.c_int64), ("peak_resident_bytes", C.c_int64),
+        ("batched_steps", C.c_int64), ("batched_requests", C.c_int64),
     ]
 
     def as_dict(self):
@@ -145,6 +146,7 @@ def _lib():
         "mf_pool_stats_get": (C.c_int, [_P, C.POINTER(PoolStats)]),
         "mf_pool_set_budget": (C.c_int, [_P, C.c_int64]),
         "mf_batched_default_opts": (C.c_int, [C.POINTER(BatchedOpts)]),
+        "mf_pool_set_batching": (C.c_int, [_P, C.POINTER(BatchedOpts)]),
         "mf_apply_batches": (C.c_int, [C.POINTER(_P), C.POINTER(_I32P), C.POINTER(_I32P), C.POINTER(_U8P), _I64P,
                                        C.c_int64, C.POINTER(BatchedOpts), C.POINTER(BatchedStats)]),
     }
@@ -456,6 +458,15 @@ class Pool:
         out = np.zeros(self._n[gid], dtype=np.uint8)
         _check(_lib().mf_pool_get_mis(self._h, gid, _ptr(out, C.c_uint8), out.size), "mf_pool_get_mis")
         return out
+
+    def set_batching(self, opts=None, on=True):
+        """Continuous batching of small requests through mf_apply_batches
+        (mf_pool_set_batching); opts None = library defaults; on=False stops it."""
+        if not on:
+            _check(_lib().mf_pool_set_batching(self._h, None), "mf_pool_set_batching")
+            return
+        o = opts if opts is not None else batched_opts()
+        _check(_lib().mf_pool_set_batching(self._h, C.byref(o)), "mf_pool_set_batching")
 
     def set_budget(self, hbm_budget):
         _check(_lib().mf_pool_set_budget(self._h, int(hbm_budget)), "mf_pool_set_budget")

@@ -99,3 +99,33 @@ def test_pool_errors(gpu_lib):
         ok = pool.submit(gid, np.array([0], np.int32), np.array([1], np.int32), np.array([1], np.uint8))
         pool.wait(ok)
         assert pool.stats()["errors"] == 1
+
+
+def test_pool_batched_dispatch_matches_dedicated_contexts(gpu_lib):
+    """Continuous batching (mf_pool_set_batching): small requests are applied
+    in mf_apply_batches steps by the dispatcher, large ones by the workers,
+    under a budget that forces evictions; every graph's membership equals the
+    dedicated context's, and a bad request fails alone."""
+    graphs = _graphs(12, 15)
+    plans = _streams(graphs, 3, 700)
+    budget = int(3 * max((ni.size - 1) * 200 + nl.size * 8 for ni, nl in graphs))
+    with native.Pool(budget, workers=3) as pool:
+        pool.set_batching(native.batched_opts(max_cta_updates=1500))
+        gids = [pool.add_graph(ni, nl, plans[k][0]) for k, (ni, nl) in enumerate(graphs)]
+        rids = []
+        for b in range(3):
+            for k, gid in enumerate(gids):
+                u, v, ins = plans[k][1][b]
+                rids.append(pool.submit(gid, u, v, ins))
+        bad = pool.submit(gids[0], np.array([0, 3], np.int32), np.array([0, 4], np.int32), np.array([1, 1], np.uint8))
+        lat = [pool.wait(r) for r in rids]
+        assert all(x >= 0 for x in lat)
+        with pytest.raises(native.MisfitError):
+            pool.wait(bad)
+        for k, gid in enumerate(gids):
+            assert np.array_equal(pool.get_mis(gid), plans[k][2][-1]), k
+        st = pool.stats()
+    assert st["completed"] == 3 * len(graphs) + 1
+    assert st["errors"] == 1
+    assert st["batched_steps"] > 0 and 0 < st["batched_requests"] < 3 * len(graphs)
+    assert st["evictions"] > 0
