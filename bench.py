@@ -71,6 +71,9 @@ def parse_args():
     ap.add_argument("--batched-only", action="store_true",
                     help="run only the batched-form leg and print its JSON (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true", help="batched leg with the library's default settings")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="one batched step only (every batch in the persistent kernel, plain launch, batches "
+                         "capped at 8192 lines, no plain-loop or pool legs): the command profiled by ncu")
     return ap.parse_args()
 
 
@@ -410,6 +413,22 @@ def main():
     torch.cuda.set_device(local)
     from misfit_gb300 import build, native
     build.build()
+    if args.profile_step:
+        from misfit_gb300 import autotune
+        from misfit_gb300 import workloads as W
+        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        mis0 = initial_mis(graphs)
+        rng = np.random.default_rng(12)
+        batches = []
+        for k, (n, ni, nl) in enumerate(graphs):
+            size = min(8192, int(round(np.exp(rng.uniform(np.log(10), np.log(50000))))))
+            u, v, ins = W.ToggleStream(n, ni, nl, 900 + k).next_batch(size, with_flags=True)
+            batches.append((u, v, ins))
+        opts = native.batched_opts(max_cta_updates=1 << 20, use_graph=0)
+        sec, _, st = autotune.run_step(graphs, mis0, batches, opts)
+        print(json.dumps({"graphs": len(graphs), "updates": int(sum(b[0].size for b in batches)),
+                          "step_ms": sec * 1e3, **st}))
+        return
     if args.batched_only:
         graphs = graph_set(args.served_graphs, 1000, 200000, 11)
         res, _ = run_batched(args, graphs, initial_mis(graphs))
