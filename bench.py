@@ -68,6 +68,9 @@ def parse_args():
     ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrivals per second")
     ap.add_argument("--served-workers", type=int, default=8)
     ap.add_argument("--served-budget", type=float, default=0.6, help="HBM budget as a fraction of the footprint")
+    ap.add_argument("--served-cta-limit", type=int, default=512,
+                    help="largest request the served form's continuous batching gives to the persistent kernel")
+    ap.add_argument("--served-only", action="store_true", help="run only the served leg and print its JSON")
     ap.add_argument("--batched-only", action="store_true",
                     help="run only the batched-form leg and print its JSON (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true", help="batched leg with the library's default settings")
@@ -320,12 +323,17 @@ def run_served(args, graphs, mis0, batching=None):
     same = all(np.array_equal(a, b) for a, b in zip(p_mis, s_mis))
     cb = None
     if batching is not None:
-        c_rate, c_lat, c_mis, cst = pooled(graphs, mis0, reqs, args.served_workers, args.served_budget, batching)
+        # serving is latency-bound: the dispatcher takes only the small
+        # requests (one CTA each finishes in a few ms), the workers the rest
+        from misfit_gb300 import native
+        lat_opts = native.batched_opts(block=batching.block, ctas_per_sm=batching.ctas_per_sm,
+                                       max_cta_updates=min(int(args.served_cta_limit), batching.max_cta_updates))
+        c_rate, c_lat, c_mis, cst = pooled(graphs, mis0, reqs, args.served_workers, args.served_budget, lat_opts)
         cb = {"value": c_rate, "unit": UNIT, "p50_ms": float(np.percentile(c_lat, 50)),
               "p99_ms": float(np.percentile(c_lat, 99)), "steps": cst["batched_steps"],
               "requests_in_steps": cst["batched_requests"], "evictions": cst["evictions"],
               "restores": cst["restores"],
-              "settings": {k: getattr(batching, k) for k, _ in batching._fields_},
+              "settings": {k: getattr(lat_opts, k) for k, _ in lat_opts._fields_},
               "identical_to_plain_loop": bool(all(np.array_equal(a, b) for a, b in zip(p_mis, c_mis)))}
     return {
         "workload": "%d RGGs (n log-uniform 1e3..2e5, mean degree 4..32); %d requests, Poisson %.0f/s, "
@@ -428,6 +436,10 @@ def main():
         sec, _, st = autotune.run_step(graphs, mis0, batches, opts)
         print(json.dumps({"graphs": len(graphs), "updates": int(sum(b[0].size for b in batches)),
                           "step_ms": sec * 1e3, **st}))
+        return
+    if args.served_only:
+        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        print(json.dumps(run_served(args, graphs, initial_mis(graphs), native.batched_opts())))
         return
     if args.batched_only:
         graphs = graph_set(args.served_graphs, 1000, 200000, 11)
