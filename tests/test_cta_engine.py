@@ -114,3 +114,15 @@ def test_engine_rgg_stream():
         u, v = st.next_batch(400, endpoints=mode.replace("-", "_"))
         batches.append((u, v, orc.flag_updates(u, v)))
     _run(nindex, nlist, batches, threads=32, rows=False)
+
+
+def test_engine_full_block_width():
+    """512 threads, a block size the kernel launches with: every chunked
+    scan and window at full width, and the radix sort (2,200 endpoint slots,
+    above the rank-sort limit)."""
+    n = 800
+    nindex, nlist = W.er_graph(n, 6, 31)
+    st = W.ToggleStream(n, nindex, nlist, 32)
+    orc = O.Oracle.from_csr(nindex, nlist)
+    u, v = st.next_batch(1100)
+    _run(nindex, nlist, [(u, v, orc.flag_updates(u, v))], 512, rows=False)
