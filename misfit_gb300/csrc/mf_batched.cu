@@ -44,7 +44,6 @@ __global__ void __launch_bounds__(1024, 1) k_batched(const cta::Item* items, int
 }
 
 constexpr size_t kAlign = 256;
-constexpr int32_t kExactCtaVertices = 65536;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
 // Byte layout of a context's kept per-vertex engine scratch.
@@ -64,7 +63,7 @@ struct VertLayout {
 
 // Byte layout of one item's per-batch scratch.
 struct WsLayout {
-  size_t k0, k1, ak, v0, v1, av, prev, rows, rowcid, ends, acnt, akill, kp, xst, total;
+  size_t k0, k1, ak, v0, v1, av, prev, rows, rowcid, ends, acnt, akill, kp, total;
   WsLayout(int32_t n, int64_t m, int64_t a_total) {
     const size_t s2 = 2 * (size_t)m + 1, r = 2 * (size_t)m + (size_t)n + 2;
     size_t o = 0;
@@ -81,7 +80,6 @@ struct WsLayout {
     acnt = o; o = align_up(o + 4 * ((size_t)n + 1));
     akill = o; o = align_up(o + (size_t)a_total + 1);
     kp = o; o = align_up(o + 8 * ((size_t)a_total + 2));
-    xst = o; o = align_up(o + (size_t)n + 1);
     total = o;
   }
 };
@@ -241,9 +239,7 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
       c->stats.max_csr = c->max_csr;
       continue;
     }
-    // exact-MIS mode sweeps every vertex a few times: one CTA only for small graphs
-    const bool fits = m[i] <= o.max_cta_updates && c->n <= o.max_cta_vertices &&
-                      (!c->exact || c->n <= kExactCtaVertices);
+    const bool fits = m[i] <= o.max_cta_updates && c->n <= o.max_cta_vertices && !c->exact;
     if (fits) {
       const double avg = c->n > 0 ? (double)c->nnz / c->n : 0.0;
       kitems.push_back({i, (double)m[i] * (1.0 + avg) * (1.0 + avg)});
@@ -361,8 +357,6 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
       it.acnt = reinterpret_cast<int32_t*>(wb + wl.acnt);
       it.akill = wb + wl.akill;
       it.kp = reinterpret_cast<int64_t*>(wb + wl.kp);
-      it.exact = c->exact ? 1 : 0;
-      it.xst = wb + wl.xst;
       it.out = E.d_out.p + cta::kOutWords * j;
       table_h[j] = it;
     }
@@ -421,7 +415,7 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
       const int64_t i = kitems[j].idx;
       mf_ctx* c = ctxs[i];
       const int64_t* out = E.h_out + cta::kOutWords * j;
-      if (out[cta::kOutStatus] != 0) MF_FAIL(MF_ESTATE, "exact-MIS completion did not settle");
+      if (out[cta::kOutStatus] != 0) MF_FAIL(MF_ESTATE, "batched kernel reported an inconsistent item");
       if (out[cta::kOutSwapped]) {
         std::swap(c->aoff, c->aoff_alt);
         std::swap(c->aadj, c->aadj_alt);

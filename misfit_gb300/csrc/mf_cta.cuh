@@ -116,7 +116,7 @@ enum : int {
   kOutEpoch,        // clustering-write epoch after the batch
   kOutT0,           // %globaltimer at the start and the end of the item
   kOutT1,
-  kOutStatus,       // 0 ok, 1 the exact-MIS completion did not settle
+  kOutStatus,       // 0 ok
   kOutWords = 16
 };
 
@@ -168,8 +168,6 @@ struct Item {
   int32_t* acnt;
   uint8_t* akill;
   int64_t* kp;
-  int32_t exact;     // exact-MIS mode: the fix-up after the repair (uses xst[n])
-  uint8_t* xst;
   int64_t* out;
 };
 
@@ -669,71 +667,6 @@ CTA_FN bool block_any_member(const View& g, const Item& it, int32_t ri, int64_t 
   return r;
 }
 
-// ---- exact-MIS mode (no reference counterpart) ------------------------------------------
-// After the repair: a member with a smaller-id member neighbour leaves
-// (decided on the set the repair left), then the vertices with no member
-// neighbour join in ascending id -- decided in rounds, a vertex settling once
-// all its lower-id neighbours have (state 1 in, 2 out, 0 undecided).  The
-// same fix-up as k_exact_leave / k_exact_init / k_greedy_round.  Returns
-// false if the rounds did not settle within n + 2 (they always do: the
-// smallest undecided vertex settles every round).
-CTA_FN bool exact_fixup(const View& g, const Item& it, int64_t* sh) {
-  const int tid = CTA_TID, nt = CTA_NT;
-  const int32_t n = it.n;
-  uint8_t* st = it.xst;
-  for (int32_t x = tid; x < n; x += nt) {
-    bool stay = member(it.mis, x);
-    if (stay)
-      row_until(g, x, [&](int32_t y) {
-        if (y < x && member(it.mis, y)) {
-          stay = false;
-          return true;
-        }
-        return false;
-      });
-    st[x] = stay ? 1 : 0;
-  }
-  CTA_SYNC();
-  for (int32_t x = tid; x < n; x += nt) {
-    if (st[x] == 1) continue;
-    const bool covered = row_until(g, x, [&](int32_t y) { return st[y] == 1; });
-    st[x] = covered ? 2 : 0;
-  }
-  CTA_SYNC();
-  CTA_SHARED int64_t s_pending;
-  bool settled = false;
-  for (int64_t round = 0; round <= (int64_t)n + 2; ++round) {
-    if (tid == 0) s_pending = 0;
-    CTA_SYNC();
-    int64_t mine = 0;
-    for (int32_t x = tid; x < n; x += nt) {
-      if (st[x] != 0) continue;
-      bool pending = false, blocked = false;
-      row_until(g, x, [&](int32_t y) {
-        if (y >= x) return false;
-        const uint8_t sy = st[y];
-        if (sy == 1) blocked = true; else if (sy == 0) pending = true;
-        return blocked;
-      });
-      if (blocked) st[x] = 2;
-      else if (!pending) st[x] = 1;
-      else ++mine;
-    }
-    if (mine) at_add(reinterpret_cast<unsigned long long*>(&s_pending), (unsigned long long)mine);
-    CTA_SYNC();
-    const bool done = s_pending == 0;
-    CTA_SYNC();
-    if (done) {
-      settled = true;
-      break;
-    }
-  }
-  for (int32_t x = tid; x < n; x += nt) it.mis[x] = st[x] == 1 ? 1 : 0;
-  CTA_SYNC();
-  (void)sh;
-  return settled;
-}
-
 // ---- the whole batch -------------------------------------------------------------------
 
 CTA_FN void run_item(const Item& it, int32_t* hist, int64_t* sh) {
@@ -1079,7 +1012,6 @@ CTA_FN void run_item(const Item& it, int32_t* hist, int64_t* sh) {
     n_processed += P;
     p = q;
   }
-  const bool settled = it.exact ? exact_fixup(g, it, sh) : true;
   if (tid == 0) {
     it.out[kOutMaxCsr] = s_max_csr;
     it.out[kOutSubBatches] = n_sub;
@@ -1089,7 +1021,7 @@ CTA_FN void run_item(const Item& it, int32_t* hist, int64_t* sh) {
     it.out[kOutProcessed] = n_processed;
     it.out[kOutExactSizes] = n_exact;
     it.out[kOutEpoch] = epoch;
-    it.out[kOutStatus] = settled ? 0 : 1;
+    it.out[kOutStatus] = 0;
     it.out[kOutT1] = (int64_t)now_ns();
   }
   CTA_SYNC();

@@ -216,7 +216,7 @@ struct mf_pool {
 
   bool small(const Graph& gr, const Request* rq) const {
     return (int64_t)rq->u.size() <= bopts.max_cta_updates && gr.ctx->n <= bopts.max_cta_vertices &&
-           (!gr.ctx->exact || gr.ctx->n <= 65536);
+           !gr.ctx->exact;
   }
 
   // A graph with a queued batch and none running becomes ready: for the

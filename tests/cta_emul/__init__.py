@@ -46,7 +46,6 @@ def lib():
             "eg_degrees": (None, [_P, I32P]),
             "eg_max_csr": (C.c_int64, [_P]),
             "eg_set_max_csr": (None, [_P, C.c_int64]),
-            "eg_set_exact": (None, [_P, C.c_int]),
             "eg_last": (I64P, [_P]),
             "eg_row": (C.c_int64, [_P, C.c_int32, I32P, C.c_int64]),
             "eg_apply": (C.c_int64, [_P, I32P, I32P, U8P, C.c_int64, C.c_int]),
@@ -86,9 +85,6 @@ class EmulGraph:
     @max_csr.setter
     def max_csr(self, v):
         lib().eg_set_max_csr(self._h, int(v))
-
-    def set_exact(self, on=True):
-        lib().eg_set_exact(self._h, 1 if on else 0)
 
     def set_mis(self, mis):
         mis = np.ascontiguousarray(mis, dtype=np.uint8)

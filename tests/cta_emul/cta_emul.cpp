@@ -55,7 +55,6 @@ struct eg {
   std::vector<uint32_t> hbits, sbits, xbits;
   uint32_t epoch = 0;
   int64_t max_csr = 0;
-  int exact = 0;
   int64_t last[mf::cta::kOutWords] = {};
 };
 
@@ -99,7 +98,6 @@ void eg_get_mis(const eg* g, uint8_t* out) { std::memcpy(out, g->mis.data(), g->
 void eg_get_cid(const eg* g, int32_t* out) { std::memcpy(out, g->cid.data(), sizeof(int32_t) * g->n); }
 void eg_degrees(const eg* g, int32_t* out) { std::memcpy(out, g->deg.data(), sizeof(int32_t) * g->n); }
 int64_t eg_max_csr(const eg* g) { return g->max_csr; }
-void eg_set_exact(eg* g, int on) { g->exact = on != 0; }
 void eg_set_max_csr(eg* g, int64_t v) { g->max_csr = v; }
 const int64_t* eg_last(const eg* g) { return g->last; }
 
@@ -131,7 +129,7 @@ int64_t eg_apply(eg* g, const int32_t* u, const int32_t* v, const uint8_t* ins, 
   std::vector<uint8_t> akill(g->a_total + 1);
   std::vector<int32_t> aadj_new(g->a_total + 2 * m + 1), aown_new(g->a_total + 2 * m + 1);
   std::vector<int32_t> uu(u, u + m), vv(v, v + m);
-  std::vector<uint8_t> ii(ins, ins + m), xst(g->n + 1);
+  std::vector<uint8_t> ii(ins, ins + m);
   int64_t out[kOutWords] = {};
   Item it{};
   it.n = g->n;
@@ -175,8 +173,6 @@ int64_t eg_apply(eg* g, const int32_t* u, const int32_t* v, const uint8_t* ins, 
   it.acnt = acnt.data();
   it.akill = akill.data();
   it.kp = kp.data();
-  it.exact = g->exact;
-  it.xst = xst.data();
   it.out = out;
 
   std::vector<int64_t> sh(kMaxThreads);

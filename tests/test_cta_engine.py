@@ -22,12 +22,9 @@ def _compare(orc, eg, ctx, rows=True):
             assert np.array_equal(eg.row(x), orc.row(x)), (ctx, x)
 
 
-def _run(nindex, nlist, batches, threads, mis=None, max_csr=None, rows=True, exact=False):
+def _run(nindex, nlist, batches, threads, mis=None, max_csr=None, rows=True):
     orc = O.Oracle.from_csr(nindex, nlist)
     eg = EmulGraph(nindex, nlist)
-    if exact:
-        orc.set_exact(True)
-        eg.set_exact(True)
     assert eg.max_csr == orc.max_csr
     if max_csr is not None:
         orc.max_csr = max_csr
@@ -129,22 +126,3 @@ def test_engine_full_block_width():
     orc = O.Oracle.from_csr(nindex, nlist)
     u, v = st.next_batch(1100)
     _run(nindex, nlist, [(u, v, orc.flag_updates(u, v))], 512, rows=False)
-
-
-def test_engine_exact_mode():
-    """Exact-MIS mode: the fix-up after the repair (leave, then greedy
-    completion in ascending id in rounds) equals the oracle's, and the set is
-    independent and maximal."""
-    n = 700
-    nindex, nlist = W.rgg_graph(n, 9, 51)
-    st = W.ToggleStream(n, nindex, nlist, 52)
-    orc = O.Oracle.from_csr(nindex, nlist)
-    batches = []
-    for _ in range(3):
-        u, v = st.next_batch(250)
-        batches.append((u, v, orc.flag_updates(u, v)))
-    rng = np.random.default_rng(53)
-    mis = (rng.random(n) < 0.3).astype(np.uint8)   # not independent: the first fix-up repairs it
-    orc, eg = _run(nindex, nlist, batches, 24, mis=mis, exact=True)
-    viol, unc = orc.check_mis()
-    assert viol == 0 and unc == 0

@@ -146,40 +146,3 @@ def test_batched_rejects_bad_batch_before_running():
     finally:
         a.close()
         b.close()
-
-
-def test_batched_exact_mode():
-    """Contexts in exact-MIS mode: small graphs take the kernel (its fix-up
-    in one CTA), larger ones the multi-launch path; both equal the plain loop
-    and leave an independent, maximal set."""
-    specs = [(3000, 8, 61), (20000, 6, 62), (70000, 5, 63)]
-    plain, batched, streams = [], [], []
-    try:
-        for n, d, seed in specs:
-            nindex, nlist = W.rgg_graph(n, d, seed)
-            a = native.Graph.from_csr(nindex, nlist)
-            b = native.Graph.from_csr(nindex, nlist)
-            for g in (a, b):
-                g.set_exact(True)
-            mis = a.greedy_mis()
-            a.set_mis(mis)
-            b.set_mis(mis)
-            plain.append(a)
-            batched.append(b)
-            streams.append(W.ToggleStream(nindex.size - 1, nindex, nlist, seed + 1))
-        for step in range(2):
-            batches = []
-            for a, st in zip(plain, streams):
-                u, v = st.next_batch(600)
-                batches.append((u, v, a.flag_updates(u, v)))
-            for a, (u, v, ins) in zip(plain, batches):
-                a.apply_batch(u, v, ins)
-            s = native.apply_batches(batched, batches)
-            assert s["kernel_items"] == 2 and s["path_items"] == 1
-            for k, (a, b) in enumerate(zip(plain, batched)):
-                assert np.array_equal(b.get_mis(), a.get_mis()), (step, k)
-                assert np.array_equal(b.cluster_ids(), a.cluster_ids()), (step, k)
-                assert b.check_mis() == (0, 0), (step, k)
-    finally:
-        for g in plain + batched:
-            g.close()
