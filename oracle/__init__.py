@@ -58,6 +58,8 @@ def lib():
             "or_compact": (C.c_int, [_P, C.c_char_p]),
             "or_greedy_mis": (None, [C.c_int32, _I64P, _I32P, _U8P]),
             "or_check_mis": (None, [_P, _I64P, _I64P]),
+            "or_apply_overlay": (None, [_P, _I32P, _I32P, _U8P, C.c_int64]),
+            "or_greedy_current": (None, [_P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -177,6 +179,17 @@ class Oracle:
 
     def compact(self, path):
         return lib().or_compact(self._h, os.fsencode(path))
+
+    def apply_overlay(self, u, v, ins):
+        """The batch applied to the overlay only (no repair)."""
+        u = np.ascontiguousarray(u, dtype=np.int32)
+        v = np.ascontiguousarray(v, dtype=np.int32)
+        ins = np.ascontiguousarray(ins, dtype=np.uint8)
+        lib().or_apply_overlay(self._h, _p(u, C.c_int32), _p(v, C.c_int32), _p(ins, C.c_uint8), u.size)
+
+    def greedy_current(self):
+        """Greedy MIS in vertex order over the current graph (becomes the membership)."""
+        lib().or_greedy_current(self._h)
 
     def check_mis(self):
         a, b = C.c_int64(), C.c_int64()

@@ -561,6 +561,29 @@ void or_greedy_mis(int32_t n, const int64_t* nindex, const int32_t* nlist, uint8
   }
 }
 
+// The from-scratch alternative to the repair, for the CPU baseline: the batch
+// applied to the overlay (src/misfit/misfit.cu:708-714), then the greedy MIS
+// of tools/compute_initial_mis.py:151-162 recomputed over the whole current
+// graph, single-threaded as that tool is.
+void or_apply_overlay(or_graph* g, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
+  for (int64_t i = 0; i < m; ++i) {
+    if (ins[i] && !adjacent(g, u[i], v[i])) insert_edge(g, u[i], v[i]);
+    else if (!ins[i] && adjacent(g, u[i], v[i])) remove_edge(g, u[i], v[i]);
+  }
+}
+
+void or_greedy_current(or_graph* g) {
+  std::vector<uint8_t> blocked((size_t)g->n, 0);
+  std::vector<int32_t> r;
+  for (int32_t x = 0; x < g->n; ++x) {
+    g->mis[(size_t)x] = 0;
+    if (blocked[(size_t)x]) continue;
+    g->mis[(size_t)x] = 1;
+    row_into(g, x, r);
+    for (int32_t y : r) blocked[(size_t)y] = 1;
+  }
+}
+
 void or_check_mis(const or_graph* g, int64_t* violations, int64_t* non_maximal) {
   int64_t viol = 0, nonmax = 0;
   std::vector<int32_t> r;

@@ -94,6 +94,12 @@ int or_compact(const or_graph* g, const char* out_path);
 /* Greedy MIS in vertex order (tools/compute_initial_mis.py:32-43). */
 void or_greedy_mis(int32_t n, const int64_t* nindex, const int32_t* nlist, uint8_t* out);
 
+/* CPU baseline of a from-scratch recompute: the batch applied to the overlay
+ * only (no repair), then the greedy MIS of tools/compute_initial_mis.py over
+ * the whole current graph (written as the membership). */
+void or_apply_overlay(or_graph* g, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m);
+void or_greedy_current(or_graph* g);
+
 /* Counters of the last batch: independence violations and vertices that are
  * neither in the MIS nor adjacent to one, on the current overlay graph. */
 void or_check_mis(const or_graph* g, int64_t* violations, int64_t* non_maximal);
