@@ -26,7 +26,7 @@ CACHE_ENV = "MISFIT_GB_AUTOTUNE_CACHE"
 
 # Coordinate search: the batch-size limit first (it moves the most work),
 # then block size and CTAs per SM at the best limit.
-LIMITS = (2048, 8192, 32768, 65536)
+LIMITS = (2048, 4096, 8192, 16384, 32768)
 SHAPES = ((512, 2), (256, 4), (1024, 1), (256, 2))
 
 

@@ -61,7 +61,7 @@ def test_search_keeps_fastest_and_caches(monkeypatch, tmp_path):
 
 def test_search_refuses_disagreeing_settings(monkeypatch, tmp_path):
     def results(o):
-        return [np.full(3, 1 if o.max_cta_updates == 65536 else 0, np.uint8)]
+        return [np.full(3, 1 if o.max_cta_updates == autotune.LIMITS[-1] else 0, np.uint8)]
 
     graphs, batches, _ = _setup(monkeypatch, tmp_path, lambda o: 1.0, results)
     with pytest.raises(RuntimeError):
