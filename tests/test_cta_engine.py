@@ -126,3 +126,45 @@ def test_engine_full_block_width():
     orc = O.Oracle.from_csr(nindex, nlist)
     u, v = st.next_batch(1100)
     _run(nindex, nlist, [(u, v, orc.flag_updates(u, v))], 512, rows=False)
+
+
+def test_engine_random_cases():
+    """Seeded random cases: ER, RGG, R-MAT and general graphs (asymmetric,
+    unsorted rows, repeated entries), initial sets that may not be
+    independent, random flags, small MAX_CSR_ELEMENTS, thread counts from 1
+    to 33."""
+    rng = np.random.default_rng(77)
+    for case in range(14):
+        kind = case % 4
+        n = int(rng.integers(20, 500))
+        if kind == 0:
+            ni, nl = W.er_graph(n, float(rng.uniform(1, 10)), int(rng.integers(1 << 30)))
+        elif kind == 1:
+            ni, nl = W.rgg_graph(n, float(rng.uniform(2, 14)), int(rng.integers(1 << 30)))
+        elif kind == 2:
+            _, (ni, nl) = W.rmat_graph(int(rng.integers(5, 9)), 6, int(rng.integers(1 << 30)))
+        else:
+            m0 = int(rng.integers(n, 6 * n))
+            src, dst = rng.integers(0, n, m0), rng.integers(0, n, m0)
+            keep = src != dst
+            src, dst = src[keep], dst[keep]
+            order = np.argsort(src, kind="stable")
+            src, dst = src[order], dst[order]
+            ni = np.zeros(n + 1, np.int64)
+            np.add.at(ni, src + 1, 1)
+            ni, nl = np.cumsum(ni), dst.astype(np.int32)
+        n = ni.size - 1
+        orc = O.Oracle.from_csr(ni, nl)
+        batches = []
+        for _ in range(2):
+            m = int(rng.integers(1, 300))
+            u, v = rng.integers(0, n, m).astype(np.int32), rng.integers(0, n, m).astype(np.int32)
+            ok = u != v
+            u, v = u[ok], v[ok]
+            if u.size == 0:
+                continue
+            ins = orc.flag_updates(u, v) if rng.random() < 0.5 else (rng.random(u.size) < 0.5).astype(np.uint8)
+            batches.append((u, v, ins))
+        mis = (rng.random(n) < 0.2).astype(np.uint8) if case % 2 else None
+        max_csr = int(rng.integers(50, 5000)) if case % 3 == 0 else None
+        _run(ni, nl, batches, int(rng.choice([1, 5, 33])), mis=mis, max_csr=max_csr)
