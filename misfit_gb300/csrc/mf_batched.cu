@@ -17,7 +17,6 @@
 #include <chrono>
 #include <cstring>
 #include <mutex>
-#include <numeric>
 #include <string>
 #include <thread>
 #include <vector>

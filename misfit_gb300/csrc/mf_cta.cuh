@@ -581,34 +581,36 @@ CTA_FN bool any_member_seq(const View& g, const Item& it, int32_t i, int64_t n_s
   return seq_until(g, it.rows[i], i < n_seeds, [&](int32_t z) { return z != except && member(it.mis, z); });
 }
 
-// Insertion rule candidate test: w not a member, mapped, and no member in its row.
-CTA_FN bool eligible(const View& g, const Item& it, int32_t w, int64_t n_seeds) {
-  if (member(it.mis, w)) return false;
+// Insertion rule candidate test: w not a member, mapped, and no member in
+// its row.  `removed` is the endpoint the rule has just taken out of the set:
+// it counts as a non-member (its membership byte is cleared at the commit).
+CTA_FN bool eligible(const View& g, const Item& it, int32_t w, int64_t n_seeds, int32_t removed) {
+  if (w != removed && member(it.mis, w)) return false;
   const int32_t i = it.map[w];
   if (i < 0) return false;
-  return !any_member_seq(g, it, i, n_seeds, -1);
+  return !any_member_seq(g, it, i, n_seeds, removed);
 }
 
+constexpr unsigned long long kNone = ~0ull;
+
 // First w (in packed-row order of vertex x = rows[ri]) that is eligible;
-// -1 if none.  Block-cooperative; the result is uniform.
-CTA_FN int32_t block_first_eligible(const View& g, const Item& it, int32_t ri, int64_t n_seeds) {
+// -1 if none.  Block-cooperative; the result is uniform.  b1 and b2 are
+// shared result slots holding kNone on entry (the caller resets them).
+// Ends with a barrier after which the slots are only read.
+CTA_FN int32_t block_first_eligible(const View& g, const Item& it, int32_t ri, int64_t n_seeds, int32_t removed,
+                                    unsigned long long* b1, unsigned long long* b2) {
   const int tid = CTA_TID, nt = CTA_NT;
   const int32_t x = it.rows[ri];
   const bool seed = ri < n_seeds;
-  CTA_SHARED unsigned long long s_best;
-  const unsigned long long kNone = ~0ull;
   // x itself (seeds) and row(x): position 0 is x, position 1 + k is row position k.
   const int64_t np = row_positions(g, x);
-  if (tid == 0) s_best = kNone;
-  CTA_SYNC();
   for (int64_t p = (seed ? 0 : 1) + tid; p < 1 + np; p += nt) {
-    if ((unsigned long long)p > s_best) break;
+    if ((unsigned long long)p > *b1) break;
     const int32_t w = p == 0 ? x : row_at(g, x, p - 1);
-    if (w >= 0 && eligible(g, it, w, n_seeds)) at_min(&s_best, (unsigned long long)p);
+    if (w >= 0 && eligible(g, it, w, n_seeds, removed)) at_min(b1, (unsigned long long)p);
   }
   CTA_SYNC();
-  unsigned long long best = s_best;
-  CTA_SYNC();
+  const unsigned long long best = *b1;
   if (best != kNone) {
     const int64_t p = (int64_t)best;
     return p == 0 ? x : row_at(g, x, p - 1);
@@ -616,6 +618,8 @@ CTA_FN int32_t block_first_eligible(const View& g, const Item& it, int32_t ri, i
   if (!seed) return -1;
   // rows of the row's elements: thread per element h (in row order), its
   // row scanned in order; the first (h position, inner position) wins.
+  // Chunks share b2, so each takes two barriers: every thread reads b2
+  // before the next chunk may write it.
   for (int64_t h0 = 0; h0 < np; h0 += nt) {
     const int64_t hp = h0 + tid;
     if (hp < np) {
@@ -624,47 +628,45 @@ CTA_FN int32_t block_first_eligible(const View& g, const Item& it, int32_t ri, i
         const int64_t nq = row_positions(g, h);
         for (int64_t q = 0; q < nq; ++q) {
           const unsigned long long key = ((unsigned long long)hp << 32) | (unsigned long long)q;
-          if (key > s_best) break;
+          if (key > *b2) break;
           const int32_t w = row_at(g, h, q);
-          if (w >= 0 && eligible(g, it, w, n_seeds)) {
-            at_min(&s_best, key);
+          if (w >= 0 && eligible(g, it, w, n_seeds, removed)) {
+            at_min(b2, key);
             break;
           }
         }
       }
     }
     CTA_SYNC();
-    best = s_best;
+    const unsigned long long best2 = *b2;
     CTA_SYNC();
-    if (best != kNone) {
-      const int32_t h = row_at(g, x, (int64_t)(best >> 32));
-      return row_at(g, h, (int64_t)(best & 0xffffffffull));
+    if (best2 != kNone) {
+      const int32_t h = row_at(g, x, (int64_t)(best2 >> 32));
+      return row_at(g, h, (int64_t)(best2 & 0xffffffffull));
     }
   }
   return -1;
 }
 
-// Any member other than `except` in the packed row of rows[ri].  Block-cooperative.
-CTA_FN bool block_any_member(const View& g, const Item& it, int32_t ri, int64_t n_seeds, int32_t except) {
+// Any member other than `except` in the packed row of rows[ri].
+// Block-cooperative; fd is a shared flag holding 0 on entry (the caller
+// resets it).  Ends with a barrier after which the flag is only read.
+CTA_FN bool block_any_member(const View& g, const Item& it, int32_t ri, int64_t n_seeds, int32_t except, int* fd) {
   const int tid = CTA_TID, nt = CTA_NT;
   const int32_t x = it.rows[ri];
   const bool seed = ri < n_seeds;
-  CTA_SHARED int s_found;
-  if (tid == 0) s_found = (seed && x != except && member(it.mis, x)) ? 1 : 0;
-  CTA_SYNC();
+  if (tid == 0 && seed && x != except && member(it.mis, x)) *fd = 1;
   const int64_t np = row_positions(g, x);
   for (int64_t p = tid; p < np; p += nt) {
-    if (s_found) break;
+    if (*fd) break;
     const int32_t z = row_at(g, x, p);
     if (z < 0) continue;
     bool f = z != except && member(it.mis, z);
     if (!f && seed) f = row_until(g, z, [&](int32_t w) { return w != except && member(it.mis, w); });
-    if (f) s_found = 1;
+    if (f) *fd = 1;
   }
   CTA_SYNC();
-  const bool r = s_found != 0;
-  CTA_SYNC();
-  return r;
+  return *fd != 0;
 }
 
 // ---- the whole batch -------------------------------------------------------------------
@@ -694,9 +696,10 @@ CTA_FN void run_item(const Item& it, int32_t* hist, int64_t* sh) {
   CTA_SYNC();
 
   CTA_SHARED int64_t s_est;
-  CTA_SHARED unsigned long long s_cut, s_cnt, s_first;
+  CTA_SHARED unsigned long long s_cut, s_cnt;
   CTA_SHARED int64_t s_max_csr;
-  CTA_SHARED int32_t s_x, s_keep, s_row, s_kind;
+  CTA_SHARED unsigned long long s_win[2], s_b1[2], s_b2[2];
+  CTA_SHARED int s_fd[2];
   if (tid == 0) s_max_csr = it.max_csr;
   CTA_SYNC();
   int64_t n_sub = 0, n_seeds_total = 0, n_cands_total = 0, n_clusters = 0, n_processed = 0, n_exact = 0;
@@ -935,60 +938,86 @@ CTA_FN void run_item(const Item& it, int32_t* hist, int64_t* sh) {
     CTA_SYNC();
     sort_pairs(it.k0, it.v0, it.k1, it.v1, P, 32 + bits_for(limit > 0 ? limit : 1), hist, sh);
 
-    // ---- repair (:277-349): the edges in that order, one after another;
-    // edges that change nothing are skipped a window at a time
+    // ---- repair (:277-349): the edges in that order, one after another.
+    // Edges that change nothing are skipped a window at a time: every
+    // thread tests one edge against the membership, and the first edge
+    // that acts is applied.  Three barriers per applied edge -- the
+    // window's, the evaluation's, the commit's.  The shared slots are
+    // double-buffered so that no slot is reset while another thread may
+    // still read it: windows alternate between two first-hit slots (an
+    // unused one stays kNone; the one that hit is reset after the commit
+    // barrier), and applied edges alternate between two sets of result
+    // slots (the set of the next edge is reset before the commit barrier).
+    if (tid == 0) {
+      s_win[0] = s_win[1] = kNone;
+      s_b1[0] = s_b1[1] = s_b2[0] = s_b2[1] = kNone;
+      s_fd[0] = s_fd[1] = 0;
+    }
+    CTA_SYNC();
     int64_t k = 0;
+    int wp = 0, ap = 0;
     for (;;) {
-      if (tid == 0) s_first = ~0ull;
-      CTA_SYNC();
+      unsigned long long f = kNone;
+      int hb = 0;
       for (int64_t w0 = k; w0 < P; w0 += nt) {
         const int64_t e = w0 + tid;
         if (e < P) {
           const uint32_t t = it.v0[e];
           const bool ma = member(it.mis, it.u[t]), mb = member(it.mis, it.v[t]);
           const bool act = it.ins[t] ? (ma && mb) : (ma != mb);
-          if (act) at_min(&s_first, (unsigned long long)e);
+          if (act) at_min(&s_win[wp], (unsigned long long)e);
         }
         CTA_SYNC();
-        const bool hit = s_first != ~0ull;
-        CTA_SYNC();  // every thread has read s_first before the next window writes it
-        if (hit) break;
+        f = s_win[wp];
+        hb = wp;
+        wp ^= 1;
+        if (f != kNone) break;
       }
-      const unsigned long long f = s_first;
-      CTA_SYNC();
-      if (f == ~0ull) break;
-      if (tid == 0) {
-        const uint32_t t = it.v0[f];
-        const int32_t a = it.u[t], b = it.v[t];
-        if (it.ins[t]) {
-          const int32_t r = a > b ? a : b;
-          it.mis[r] = 0;
-          s_kind = 1;
-          s_x = r;
-          s_keep = -1;
-        } else {
-          const bool ma = member(it.mis, a);
-          s_kind = 2;
-          s_x = ma ? b : a;
-          s_keep = ma ? a : b;
-        }
-        s_row = it.map[s_x];
-      }
-      CTA_SYNC();
-      const int32_t kind = s_kind, x = s_x, keep = s_keep, ri = s_row;
-      CTA_SYNC();
-      if (kind == 1) {
+      if (f == kNone) break;
+      // every thread derives the rule of edge f from the same membership
+      const uint32_t t = it.v0[f];
+      const int32_t a = it.u[t], b = it.v[t];
+      int32_t r = -1, w = -1, y = -1;
+      bool any = true, evaluated = false;
+      if (it.ins[t]) {
+        r = a > b ? a : b;
+        const int32_t ri = it.map[r];
         if (ri >= 0) {
-          const int32_t w = block_first_eligible(g, it, ri, S);
-          if (tid == 0 && w >= 0) it.mis[w] = 1;
+          w = block_first_eligible(g, it, ri, S, r, &s_b1[ap], &s_b2[ap]);
+          evaluated = true;
         }
       } else {
-        const bool any = ri >= 0 && block_any_member(g, it, ri, S, keep);
-        if (tid == 0 && !any) it.mis[x] = 1;
+        const bool ma = member(it.mis, a);
+        y = ma ? b : a;
+        const int32_t keep = ma ? a : b;
+        const int32_t ri = it.map[y];
+        if (ri >= 0) {
+          any = block_any_member(g, it, ri, S, keep, &s_fd[ap]);
+          evaluated = true;
+        } else {
+          any = false;
+        }
       }
+      // the evaluations end with a barrier; without one, this barrier makes
+      // every thread derive the rule before the commit changes the membership
+      if (!evaluated) CTA_SYNC();
+      if (tid == 0) {
+        if (r >= 0) {
+          it.mis[r] = 0;
+          if (w >= 0) it.mis[w] = 1;
+        } else if (!any) {
+          it.mis[y] = 1;
+        }
+        s_b1[ap ^ 1] = kNone;
+        s_b2[ap ^ 1] = kNone;
+        s_fd[ap ^ 1] = 0;
+      }
+      ap ^= 1;
       CTA_SYNC();
+      if (tid == 0) s_win[hb] = kNone;
       k = (int64_t)f + 1;
     }
+    CTA_SYNC();
 
     // ---- clear (:351-358): mapped vertices only; marks for the next sub-batch
     for (int64_t i = tid; i < R; i += nt) {
