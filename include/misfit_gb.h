@@ -61,7 +61,9 @@ typedef struct mf_batch_stats {
 
 /* ---- lifetime -------------------------------------------------------- */
 
-/* Version of this ABI (major*10000 + minor*100 + patch). */
+/* Version of this ABI (major*10000 + minor*100 + patch).  1.1 added the
+ * batched form (mf_apply_batches, mf_batched_*), mf_pool_set_batching and the
+ * two batched_* fields at the end of mf_pool_stats. */
 int mf_version(void);
 const char* mf_status_string(int status);
 /* Last error on the calling thread ("" when none). */
