@@ -168,3 +168,17 @@ def test_engine_random_cases():
         mis = (rng.random(n) < 0.2).astype(np.uint8) if case % 2 else None
         max_csr = int(rng.integers(50, 5000)) if case % 3 == 0 else None
         _run(ni, nl, batches, int(rng.choice([1, 5, 33])), mis=mis, max_csr=max_csr)
+
+
+def test_engine_config1_stream():
+    """The plain-method small configuration: ER G(10000, avg 8), seed 42,
+    10 batches of 2000 toggles (half deletes of existing edges, half inserts
+    of non-adjacent pairs), flags against the base graph; membership,
+    cluster ids and degrees equal to the oracle after every batch."""
+    n = 10000
+    ni, nl = W.er_graph(n, 8, 42)
+    ts = W.ToggleStream(n, ni, nl, 42)
+    bs = [ts.next_batch(2000) for _ in range(10)]
+    base = O.Oracle.from_csr(ni, nl)
+    batches = [(u, v, base.flag_updates(u, v)) for u, v in bs]
+    _run(ni, nl, batches, 16, rows=False)
