@@ -65,12 +65,13 @@ def build(verbose=False):
                                        cli_src, "-o", exe + ".tmp", "-L" + LIB_DIR, "-lmisfit_gb",
                                        "-Wl,-rpath,$ORIGIN/../lib"])
                 os.replace(exe + ".tmp", exe)
-    # offline tool: .mtx edge list -> .egr (host code only)
-    tool_src = os.path.join(CSRC, "mf_mtx2egr.cpp")
-    tool = os.path.join(BIN_DIR, "mtx2egr")
-    if os.path.exists(tool_src) and _stale(tool, [tool_src]):
-        subprocess.check_call(["g++", "-O2", "-std=c++17", tool_src, "-o", tool + ".tmp"])
-        os.replace(tool + ".tmp", tool)
+    # offline tools (host code only): .mtx edge list -> .egr, batch folders
+    for src_name, tool_name in (("mf_mtx2egr.cpp", "mtx2egr"), ("mf_mkbatches.cpp", "mkbatches")):
+        tool_src = os.path.join(CSRC, src_name)
+        tool = os.path.join(BIN_DIR, tool_name)
+        if os.path.exists(tool_src) and _stale(tool, [tool_src]):
+            subprocess.check_call(["g++", "-O2", "-std=c++17", tool_src, "-o", tool + ".tmp"])
+            os.replace(tool + ".tmp", tool)
     if verbose:
         print(LIB)
     return LIB
