@@ -89,3 +89,17 @@ def test_refusals(tool, graph, tmp_path):
     bad.write_bytes(b"\x05\x00\x00\x00")
     r = _run(tool, str(bad), tmp_path / "x", 1, 1)
     assert r.returncode == 1
+
+
+def test_folder_reads_through_the_library(tool, graph, tmp_path):
+    """The folder is what the drop-in binaries read: mf_list_batch_files
+    orders it 1..k, mf_read_batch_file returns every line, 0-based."""
+    from misfit_gb300 import native
+    native.load_library()
+    egr, n, ni, nl = graph
+    assert _run(tool, egr, tmp_path / "f", 50, 12, "low_degree", 5).returncode == 0
+    assert native.list_batch_files(str(tmp_path / "f")) == ["%d.mtx" % k for k in range(1, 13)]
+    for k in (1, 12):
+        u, v = native.read_batch_file(str(tmp_path / "f" / ("%d.mtx" % k)), n)
+        uu, vv = W.read_batch_file(str(tmp_path / "f" / ("%d.mtx" % k)))
+        assert np.array_equal(u, uu) and np.array_equal(v, vv) and u.size == 50
