@@ -69,6 +69,9 @@ def parse_args():
     ap.add_argument("--no-served", action="store_true", help="skip the served and batched legs")
     ap.add_argument("--no-exact", action="store_true", help="skip the exact-MIS leg")
     ap.add_argument("--served-graphs", type=int, default=64)
+    ap.add_argument("--graphs-nmax", type=int, default=200000,
+                    help="largest vertex count of the served/batched graph set (the batched configuration "
+                         "goes to 1,000,000 with 256 graphs)")
     ap.add_argument("--served-requests", type=int, default=300)
     ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrivals per second")
     ap.add_argument("--served-workers", type=int, default=8)
@@ -362,9 +365,9 @@ def run_served(args, graphs, mis0, batching=None):
               "settings": {k: getattr(lat_opts, k) for k, _ in lat_opts._fields_},
               "identical_to_plain_loop": bool(all(np.array_equal(a, b) for a, b in zip(p_mis, c_mis)))}
     return {
-        "workload": "%d RGGs (n log-uniform 1e3..2e5, mean degree 4..32); %d requests, Poisson %.0f/s, "
+        "workload": "%d RGGs (n log-uniform 1e3..%.0e, mean degree 4..32); %d requests, Poisson %.0f/s, "
                     "batches log-uniform 10..20000 toggles, graph Zipf(1.1), endpoints uniform/preferential/"
-                    "low-degree" % (len(graphs), len(reqs), args.served_rate),
+                    "low-degree" % (len(graphs), args.graphs_nmax, len(reqs), args.served_rate),
         "value": s_rate, "unit": UNIT, "p50_ms": float(np.percentile(s_lat, 50)),
         "p99_ms": float(np.percentile(s_lat, 99)), "workers": args.served_workers,
         "hbm_budget_fraction": args.served_budget, "evictions": st["evictions"], "restores": st["restores"],
@@ -414,7 +417,8 @@ def run_batched(args, graphs, mis0):
     same_b = all(np.array_equal(a, b) for a, b in zip(p_mis, b_mis))
     chosen = {k: getattr(opts, k) for k, _ in opts._fields_}
     return {
-        "workload": "%d RGGs (n log-uniform 1e3..2e5), one batch each of log-uniform 10..50000 toggles" % len(graphs),
+        "workload": "%d RGGs (n log-uniform 1e3..%.0e), one batch each of log-uniform 10..50000 toggles" % (
+            len(graphs), args.graphs_nmax),
         "value": b_rate, "unit": UNIT,
         "step_ms": float(np.median(secs)) * 1e3, "kernel_ms": bst["kernel_ms"],
         "kernel_items": bst["kernel_items"], "path_items": bst["path_items"],
@@ -450,7 +454,7 @@ def main():
     if args.profile_step:
         from misfit_gb300 import autotune
         from misfit_gb300 import workloads as W
-        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
         mis0 = initial_mis(graphs)
         rng = np.random.default_rng(12)
         batches = []
@@ -464,11 +468,11 @@ def main():
                           "step_ms": sec * 1e3, **st}))
         return
     if args.served_only:
-        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
         print(json.dumps(run_served(args, graphs, initial_mis(graphs), native.batched_opts())))
         return
     if args.batched_only:
-        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
         res, _ = run_batched(args, graphs, initial_mis(graphs))
         res["gpu_launches_total"] = int(native.load_library().mf_kernel_launches())
         print(json.dumps(res))
@@ -617,7 +621,7 @@ def main():
             line["cpu_greedy_recompute"] = {"error": str(e)}
     g.close()
     if rank == 0 and not args.no_served:
-        graphs = graph_set(args.served_graphs, 1000, 200000, 11)
+        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
         mis0 = initial_mis(graphs)
         line["batched"], tuned = run_batched(args, graphs, mis0)
         line["served"] = run_served(args, graphs, mis0, tuned)
