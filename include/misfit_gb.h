@@ -315,7 +315,8 @@ int mf_pool_set_budget(mf_pool* pool, int64_t hbm_budget);
  * reset, the kernel, the read-back of the per-graph results) is captured
  * and launched as one CUDA graph.  Larger batches, graphs above the vertex
  * limit and contexts in exact-MIS mode take the multi-launch path
- * (mf_apply_batch) on their own streams while the persistent kernel runs. */
+ * (mf_apply_batch, from up to 8 host threads, each graph on its own stream)
+ * while the persistent kernel runs. */
 typedef struct mf_batched_opts {
   int block;                  /* threads per persistent CTA: 64..1024, a multiple of 32 (default 512) */
   int ctas_per_sm;            /* persistent CTAs per SM (default 2) */
