@@ -43,6 +43,7 @@ def lib():
             "or_max_csr": (C.c_int64, [_P]),
             "or_set_max_csr": (None, [_P, C.c_int64]),
             "or_set_exact": (None, [_P, C.c_int]),
+            "or_set_serial_clustering": (None, [_P, C.c_int]),
             "or_set_mis": (None, [_P, _U8P]),
             "or_get_mis": (None, [_P, _U8P]),
             "or_get_cluster_ids": (None, [_P, _I32P]),
@@ -113,6 +114,11 @@ class Oracle:
     def set_exact(self, on=True):
         """Exact-MIS mode: independent, maximal membership after every batch."""
         lib().or_set_exact(self._h, 1 if on else 0)
+
+    def set_serial_clustering(self, on=True):
+        """Clustering schedule: serial (rows one after another, each seeing the
+        earlier rows' writes) instead of the default bulk-synchronous one."""
+        lib().or_set_serial_clustering(self._h, 1 if on else 0)
 
     def set_mis(self, mis):
         mis = np.ascontiguousarray(mis, dtype=np.uint8)
@@ -302,3 +308,135 @@ def ref_list_batch_files(folder):
     buf = C.create_string_buffer(1 << 20)
     k = L.ref_list_batch_files(os.fsencode(folder), buf, 1 << 20)
     return [x for x in buf.raw[:k].decode().split("\n") if x]
+
+
+# ---- the reference's whole engines, run on the CPU (oracle/_ref/*_emul.so) ----
+
+_EMUL = {}
+
+
+def ref_emul_lib(engine="sync", build_if_possible=True):
+    """libref_{sync,async}_emul.so (oracle/build.py, build_ref_emul), or None
+    when it is neither built nor buildable here."""
+    if engine in _EMUL:
+        return _EMUL[engine]
+    paths = _build.build_ref_emul() if build_if_possible else None
+    path = (paths or {}).get(engine) or _build.EMUL_SO[engine]
+    if not os.path.exists(path):
+        return None
+    L = C.CDLL(path)
+    sig = {
+        "re_main": (C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),
+        "re_set_schedule": (None, [C.c_int]),
+        "re_launches": (C.c_longlong, []),
+    }
+    if engine == "sync":
+        sig.update({
+            "re_open": (_P, [C.c_char_p, C.c_longlong]),
+            "re_close": (None, [_P]),
+            "re_num_nodes": (C.c_int, [_P]),
+            "re_set_mis": (None, [_P, _U8P]),
+            "re_apply_batch": (C.c_longlong, [_P, _I32P, _I32P, _U8P, C.c_longlong]),
+            "re_sub_batch": (C.c_int, [_P, C.c_longlong, _I64P]),
+            "re_get_mis": (None, [_P, _U8P]),
+            "re_get_cluster_ids": (None, [_P, _I32P]),
+            "re_max_csr": (C.c_longlong, [_P]),
+            "re_degree": (C.c_int, [_P, C.c_int]),
+        })
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _EMUL[engine] = L
+    return L
+
+
+BULK_SYNCHRONOUS, SERIAL = 0, 1
+
+
+class RefEngine:
+    """The reference's sync engine (src/misfit/misfit.cu) on one graph, run on
+    the CPU: HybridGraph + GPUVertexClusteringGraph driven one batch at a time
+    through processBatchGPUVertexClustering, the kernels emulated thread by
+    thread.  `schedule` selects how the clustering kernel's threads
+    interleave (BULK_SYNCHRONOUS: every thread reads the pre-launch cluster
+    ids, the highest thread index writes last -- the oracle's and the
+    library's schedule; SERIAL: threads run one after another)."""
+
+    def __init__(self, egr_path, max_csr, schedule=BULK_SYNCHRONOUS):
+        L = ref_emul_lib("sync")
+        if L is None:
+            raise RuntimeError("reference engine emulation unavailable")
+        self.L = L
+        self.schedule = schedule
+        self._h = C.c_void_p(L.re_open(os.fsencode(egr_path), int(max_csr)))
+        self.n = L.re_num_nodes(self._h)
+
+    def close(self):
+        if self._h:
+            self.L.re_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_mis(self, mis):
+        mis = np.ascontiguousarray(mis, dtype=np.uint8)
+        self.L.re_set_mis(self._h, _p(mis, C.c_uint8))
+
+    def apply_batch(self, u, v, ins):
+        """Returns [(edges, rows, clusters)] per sub-batch, in order."""
+        u = np.ascontiguousarray(u, dtype=np.int32)
+        v = np.ascontiguousarray(v, dtype=np.int32)
+        ins = np.ascontiguousarray(ins, dtype=np.uint8)
+        self.L.re_set_schedule(self.schedule)
+        k = self.L.re_apply_batch(self._h, _p(u, C.c_int32), _p(v, C.c_int32), _p(ins, C.c_uint8), u.size)
+        out = np.zeros(3, np.int64)
+        recs = []
+        for i in range(k):
+            self.L.re_sub_batch(self._h, i, _p(out, C.c_int64))
+            recs.append(tuple(int(x) for x in out))
+        return recs
+
+    def get_mis(self):
+        out = np.zeros(self.n, np.uint8)
+        self.L.re_get_mis(self._h, _p(out, C.c_uint8))
+        return out
+
+    def cluster_ids(self):
+        out = np.zeros(self.n, np.int32)
+        self.L.re_get_cluster_ids(self._h, _p(out, C.c_int32))
+        return out
+
+    @property
+    def max_csr(self):
+        return self.L.re_max_csr(self._h)
+
+
+def run_reference_main(engine, args, cwd, schedule=BULK_SYNCHRONOUS, skip_compaction=False, timeout=600):
+    """Run the reference engine's own main() (the 5-argument CLI of
+    bin/misfit or bin/misfit_async) on the CPU in a child process whose
+    working directory is `cwd`.  Returns (exit code, stdout)."""
+    import subprocess
+    import sys
+    if ref_emul_lib(engine) is None:
+        raise RuntimeError("reference engine emulation unavailable")
+    path = _build.EMUL_SO[engine]
+    code = ("import ctypes,sys\n"
+            "L=ctypes.CDLL(sys.argv[1]); L.re_set_schedule(int(sys.argv[2]))\n"
+            "a=[x.encode() for x in sys.argv[3:]]\n"
+            "arr=(ctypes.c_char_p*len(a))(*a)\n"
+            "sys.stdout.flush(); rc=L.re_main(len(a),arr)\n"
+            "sys.exit(rc)\n")
+    env = dict(os.environ)
+    if skip_compaction:
+        env["MISFIT_SKIP_COMPACTION"] = "1"
+    else:
+        env.pop("MISFIT_SKIP_COMPACTION", None)
+    argv0 = "misfit" if engine == "sync" else "misfit_async"
+    r = subprocess.run([sys.executable, "-c", code, path, str(schedule), argv0] + [str(a) for a in args],
+                       cwd=cwd, env=env, capture_output=True, text=True, timeout=timeout)
+    return r.returncode, r.stdout + r.stderr

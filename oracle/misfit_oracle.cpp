@@ -59,6 +59,7 @@ struct or_graph {
   int64_t max_csr = 0;
   bool trace = false;
   bool exact = false;   // exact-MIS mode: fix-up after every batch (no reference counterpart)
+  bool serial_clustering = false;   // clustering schedule switch (or_set_serial_clustering)
   std::vector<SubBatchTrace> traces;
 };
 
@@ -202,17 +203,30 @@ void run_kernels(or_graph* g, const int32_t* u, const int32_t* v, const uint8_t*
   // every row reads the cluster ids as they were before the kernel.
   std::vector<int64_t> rowcid(nrows, -2);  // -2 = row returned early
   int64_t cluster_count = 0;
-  for (int64_t i = 0; i < nrows; ++i) {
-    if (g->cid[sb.mapped[i]] != -1) continue;
-    int64_t found = -1;
-    for (int32_t y : sb.rows[i])
-      if (g->cid[y] != -1) { found = g->cid[y]; break; }
-    rowcid[i] = found != -1 ? found : cluster_count++;
-  }
-  // Writes land in row order, so the highest row index writes last.
-  for (int64_t i = 0; i < nrows; ++i) {
-    if (rowcid[i] == -2) continue;
-    for (int32_t y : sb.rows[i]) g->cid[y] = (int32_t)rowcid[i];
+  if (g->serial_clustering) {
+    // Alternative schedule: the rows run one after another, each reading the
+    // writes of the rows before it (also a legal run of the racy kernel).
+    for (int64_t i = 0; i < nrows; ++i) {
+      if (g->cid[sb.mapped[i]] != -1) continue;
+      int64_t found = -1;
+      for (int32_t y : sb.rows[i])
+        if (g->cid[y] != -1) { found = g->cid[y]; break; }
+      rowcid[i] = found != -1 ? found : cluster_count++;
+      for (int32_t y : sb.rows[i]) g->cid[y] = (int32_t)rowcid[i];
+    }
+  } else {
+    for (int64_t i = 0; i < nrows; ++i) {
+      if (g->cid[sb.mapped[i]] != -1) continue;
+      int64_t found = -1;
+      for (int32_t y : sb.rows[i])
+        if (g->cid[y] != -1) { found = g->cid[y]; break; }
+      rowcid[i] = found != -1 ? found : cluster_count++;
+    }
+    // Writes land in row order, so the highest row index writes last.
+    for (int64_t i = 0; i < nrows; ++i) {
+      if (rowcid[i] == -2) continue;
+      for (int32_t y : sb.rows[i]) g->cid[y] = (int32_t)rowcid[i];
+    }
   }
   if (tr) tr->cid_after = g->cid;
 
@@ -333,6 +347,7 @@ int64_t or_base_entries(const or_graph* g) { return (int64_t)g->edges; }
 int64_t or_max_csr(const or_graph* g) { return g->max_csr; }
 void or_set_max_csr(or_graph* g, int64_t v) { g->max_csr = v; }
 void or_set_exact(or_graph* g, int on) { g->exact = on != 0; }
+void or_set_serial_clustering(or_graph* g, int on) { g->serial_clustering = on != 0; }
 
 // setMISFromHost / getMISToHost (src/misfit/misfit.cu:448-462).
 void or_set_mis(or_graph* g, const uint8_t* mis) {

@@ -53,6 +53,12 @@ void or_set_max_csr(or_graph* g, int64_t v);
  * member with a smaller-id member neighbour leaves, then the uncovered
  * vertices are completed greedily in ascending id. */
 void or_set_exact(or_graph* g, int on);
+/* Schedule switch for vertex_clustering_csr_kernel: 0 (default) the
+ * bulk-synchronous schedule above; 1 the serial one, rows one after another
+ * in ascending index, each seeing the writes of the rows before it.  Both are
+ * legal runs of the racy kernel; the serial one is what a launch of the
+ * reference's kernel with one thread at a time gives. */
+void or_set_serial_clustering(or_graph* g, int on);
 
 void or_set_mis(or_graph* g, const uint8_t* mis);
 void or_get_mis(const or_graph* g, uint8_t* out);

@@ -3,7 +3,7 @@ bytes that the reference's own converter (tools/efficient_converter.py,
 imported from the reference tree) writes for each.  Run where the reference
 tree is present; the tests read only the JSON.
 
-Usage: python tests/golden/make_mtx_golden.py [reference_root]
+Usage: python tests/golden/make_mtx_golden.py <reference_root>  (or set MISFIT_REF_ROOT)
 """
 import hashlib
 import importlib.util
@@ -72,4 +72,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MISFIT_REF_ROOT")
+    if not root:
+        raise SystemExit("usage: make_mtx_golden.py <reference_root>  (or set MISFIT_REF_ROOT)")
+    main(root)

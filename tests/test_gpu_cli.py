@@ -21,8 +21,8 @@ def _setup(tmp_path, name="sample"):
     g = G.load(name)
     n = int(g["n"])
     egr = tmp_path / (name + ".egr")
-    W.write_egr(str(egr), n, g["nindex"], g["nlist"], wide=bool(g["wide"]))
-    W.write_mis_file(str(tmp_path / "mis.txt"), g["mis0"])
+    W.write_egr(str(egr), n, g["nindex"], g["nlist"], wide=bool(g["wide"]) if "wide" in g else False)
+    W.write_mis_file(str(tmp_path / "mis.txt"), G.mis0(g))
     folder = tmp_path / "batches"
     W.write_batch_folder(str(folder), [(u, v) for u, v, _ in G.batches(g)])
     return g, n, egr, folder
@@ -40,6 +40,8 @@ def test_cli_final_mis_and_compaction(engine, gpu_lib, tmp_path):
     assert out.returncode == 0, out.stderr
     mis = W.read_mis_file(str(tmp_path / "datasets" / "Final_MISs" / "er1500_flash_final_mis.txt"), n)
     assert np.array_equal(mis, g["b%d_mis_oracle" % (nb - 1)])
+    # the reference's own binary (its main() run on the CPU) wrote this file
+    assert np.array_equal(mis, G.main_final_mis(g, "sync" if engine == "misfit" else "async"))
     assert "Total processing time:" in out.stdout
     assert re.search(r"Final MIS cardinality:\s+%d" % int(mis.sum()), out.stdout)
     if engine == "misfit":
@@ -55,6 +57,24 @@ def test_cli_final_mis_and_compaction(engine, gpu_lib, tmp_path):
     after = egr.read_bytes()
     assert after != before
     assert hashlib.sha256(after).digest() == bytes(g["compact_sha256"])
+    assert hashlib.sha256(after).digest() == bytes(g["main_%s_compact_sha256" % ("sync" if engine == "misfit" else "async")])
+
+
+@pytest.mark.parametrize("engine", ["misfit", "misfit_async"])
+def test_cli_config1_against_reference_binary(engine, gpu_lib, tmp_path):
+    """Config 1 (ER G(10000, 8), 10 x 2000 toggles) through the drop-in binary:
+    the final-MIS file and the in-place compaction equal what the reference's
+    own bin/misfit / bin/misfit_async (main() run on the CPU) wrote."""
+    g, n, egr, folder = _setup(tmp_path, "cfg1")
+    nb = int(g["num_batches"])
+    exe = os.path.abspath(os.path.join(BIN, engine))
+    out = subprocess.run([exe, str(egr), str(tmp_path / "mis.txt"), str(folder), str(nb), "0"], cwd=str(tmp_path),
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    mis = W.read_mis_file(str(tmp_path / "datasets" / "Final_MISs" / "cfg1_flash_final_mis.txt"), n)
+    ref = "sync" if engine == "misfit" else "async"
+    assert np.array_equal(mis, G.main_final_mis(g, ref))
+    assert hashlib.sha256(egr.read_bytes()).digest() == bytes(g["main_%s_compact_sha256" % ref])
 
 
 def test_cli_usage_and_errors(gpu_lib, tmp_path):

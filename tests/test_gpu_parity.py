@@ -62,6 +62,30 @@ def test_golden_streams(name, gpu_lib, tmp_path):
     gr.close()
 
 
+@pytest.mark.parametrize("name", G.REF_NAMES)
+def test_reference_engine_golden(name, gpu_lib):
+    """The library against the reference's own sync engine (src/misfit/misfit.cu
+    run on the CPU with its kernels emulated thread by thread, clustering
+    under the bulk-synchronous schedule), after every batch: the membership,
+    every cluster id (stale ones included), each sub-batch's edges, rows and
+    cluster count, and MAX_CSR_ELEMENTS."""
+    g = G.load(name)
+    gr = native.Graph.from_csr(g["nindex"], g["nlist"])
+    assert gr.max_csr == int(g["initial_max_csr"])
+    gr.max_csr = G.initial_max_csr(g)
+    gr.set_mis(G.mis0(g))
+    for i, (u, v, ins) in enumerate(G.batches(g)):
+        gr.trace(True)
+        gr.apply_batch(u, v, ins)
+        assert np.array_equal(gr.get_mis(), G.mis_ref(g, i)), i
+        assert G.cid_sha(gr.cluster_ids()) == bytes(g["b%d_cid_ref_sha" % i]), i
+        hdr = np.stack([r[0] for r in gr.trace_records()])
+        got = np.stack([hdr[:, 1] - hdr[:, 0], hdr[:, 8], hdr[:, 6]], axis=1)
+        assert np.array_equal(got, g["b%d_sb_ref" % i]), i
+        assert gr.max_csr == int(g["b%d_maxcsr_ref" % i]), i
+    gr.close()
+
+
 def _stream(kind, seed, batches, size, endpoints="uniform"):
     if kind == "er":
         n = 3000

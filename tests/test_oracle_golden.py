@@ -94,3 +94,44 @@ def test_oracle_exact_mode_is_a_mis():
             assert orc.check_mis() == (0, 0)
     finally:
         orc.close()
+
+
+@pytest.mark.parametrize("serial", [False, True], ids=["bulk_synchronous", "serial"])
+@pytest.mark.parametrize("name", G.REF_NAMES)
+def test_oracle_matches_reference_engine_golden(name, serial):
+    """The oracle against the reference's own sync engine (src/misfit/misfit.cu
+    run on the CPU, kernels emulated thread by thread), batch after batch:
+    membership, every cluster id (stale ones included), each sub-batch's
+    edges, rows and cluster count, and MAX_CSR_ELEMENTS -- under the
+    bulk-synchronous clustering schedule, and the membership under the serial
+    one."""
+    g = G.load(name)
+    orc = O.Oracle.from_csr(g["nindex"], g["nlist"])
+    orc.max_csr = G.initial_max_csr(g)
+    orc.set_serial_clustering(serial)
+    orc.set_mis(G.mis0(g))
+    for i, (u, v, ins) in enumerate(G.batches(g)):
+        orc.trace(True)
+        orc.apply_batch(u, v, ins)
+        assert np.array_equal(orc.get_mis(), G.mis_ref(g, i, serial)), i
+        if serial:
+            continue
+        assert G.cid_sha(orc.cluster_ids()) == bytes(g["b%d_cid_ref_sha" % i]), i
+        hdr = np.stack([r[0] for r in orc.trace_records()])
+        got = np.stack([hdr[:, 1] - hdr[:, 0], hdr[:, 8], hdr[:, 6]], axis=1)
+        assert np.array_equal(got, g["b%d_sb_ref" % i]), i
+        assert orc.max_csr == int(g["b%d_maxcsr_ref" % i]), i
+
+
+@pytest.mark.parametrize("name", ["sample", "er1500", "cfg1"])
+def test_reference_mains_agree_with_their_engine(name):
+    """bin/misfit and bin/misfit_async (the reference's own main(), run on the
+    CPU) write the same final MIS as the engine stepped a batch at a time, and
+    both compact to the bytes the reference's compactor writes."""
+    g = G.load(name)
+    nb = int(g["num_batches"])
+    for engine in ("sync", "async"):
+        assert np.array_equal(G.main_final_mis(g, engine), G.mis_ref(g, nb - 1)), engine
+    if "compact_sha256" in g:
+        assert bytes(g["main_sync_compact_sha256"]) == bytes(g["compact_sha256"])
+        assert bytes(g["main_async_compact_sha256"]) == bytes(g["compact_sha256"])
