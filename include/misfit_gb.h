@@ -126,6 +126,10 @@ int mf_flag_updates(mf_ctx* ctx, const int32_t* u, const int32_t* v, int64_t m, 
  *   - The first call on a device finds the array's address once
  *     (cudaGetSymbolAddress).  Make that first call, which may have
  *     m = 0, before any stream capture.
+ *   - The address is looked up again whenever a context is opened on the
+ *     device (mf_open_egr / mf_open_csr, outside any capture).  After a
+ *     cudaDeviceReset the cached address is stale: open a new context on
+ *     that device before the next call.
  *   - m > MF_NOALLOC_MAX_UPDATES returns MF_ELIMIT and does nothing.
  *   - Each call zeroes the array's invalid-pair counter itself.
  *   - Invalid endpoints return MF_EINVAL without writing ins_out, as in
@@ -148,11 +152,23 @@ int mf_apply_batch(mf_ctx* ctx, const int32_t* u, const int32_t* v, const uint8_
 int mf_apply_batch_device(mf_ctx* ctx, const int32_t* d_u, const int32_t* d_v,
                           const uint8_t* d_ins, int64_t m);
 
-/* Enqueue a batch and return after the host-side part; the host arrays must
- * stay valid until the next mf_sync.  Pairs with mf_sync like
- * launchBatch / syncAndCollect of the pipelined engine
- * (src/misfit_async/misfit_async.cu:484-700). */
+/* The pipelined engine: launchBatch / syncAndCollect of misfit_async
+ * (src/misfit_async/misfit_async.cu:484-700, its loop :826-876).
+ * mf_apply_batch_async queues the batch for the context's worker thread and
+ * returns at once; the worker runs queued batches one after another, in
+ * order, with the same results as mf_apply_batch.  The host arrays must stay
+ * valid until the batch is collected.  Several batches may be queued (the
+ * reference's loop keeps two: batch i+1 is launched before batch i is
+ * collected).  Bad pointers or a negative m fail at once; everything else
+ * (including invalid endpoints) is reported when the batch is collected.
+ * mf_collect waits for the oldest uncollected batch, writes its statistics
+ * (out may be NULL) and returns its status and error message.
+ * mf_sync collects every queued batch and returns the first failure, if any.
+ * While batches are uncollected, mf_apply_batch / mf_apply_batch_device /
+ * mf_apply_batches reject the context (MF_EINVAL); every other call on the
+ * context first waits until the queued batches have run. */
 int mf_apply_batch_async(mf_ctx* ctx, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m);
+int mf_collect(mf_ctx* ctx, mf_batch_stats* out);
 int mf_sync(mf_ctx* ctx);
 
 int mf_last_batch_stats(mf_ctx* ctx, mf_batch_stats* out);
@@ -233,6 +249,11 @@ int mf_profile_reset(mf_ctx* ctx);
 int mf_profile_read(mf_ctx* ctx, double* ms, int64_t* calls, double* bytes, int cap);
 /* Kernels launched by this library in this process so far. */
 int64_t mf_kernel_launches(void);
+/* Device and pinned-host allocations (cudaMalloc, cudaMallocAsync,
+ * cudaMallocHost) made by this library in this process so far; a call that
+ * leaves it unchanged allocated nothing.  No reference counterpart (a
+ * diagnostic of this library). */
+int64_t mf_allocations(void);
 
 /* ---- trace (parity tests) ---------------------------------------------- */
 

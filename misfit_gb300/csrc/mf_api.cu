@@ -6,7 +6,10 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <cstdio>
 #include <cstdlib>
@@ -27,6 +30,7 @@ thread_local std::string g_error;
 }
 
 std::atomic<long long> g_launches{0};
+std::atomic<long long> g_allocs{0};
 thread_local cudaStream_t g_alloc_stream = nullptr;
 
 namespace {
@@ -156,6 +160,7 @@ mf_ctx* new_ctx(int gpu) {
   mf_ctx* c = new mf_ctx();
   c->device = gpu;
   try {
+    mf::noalloc_refresh(gpu);
     MF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     mf::g_alloc_stream = c->stream;
     // keep freed stream-ordered memory in this process's pool for reuse
@@ -169,6 +174,7 @@ mf_ctx* new_ctx(int gpu) {
     MF_CUDA(cudaStreamCreateWithFlags(&c->stream_b, cudaStreamNonBlocking));
     MF_CUDA(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
     MF_CUDA(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
+    mf::note_alloc();
     MF_CUDA(cudaMallocHost(&c->h_counters, sizeof(int64_t) * 64));
     c->counters.reserve(64);
   } catch (...) {
@@ -179,7 +185,13 @@ mf_ctx* new_ctx(int gpu) {
   return c;
 }
 
+void quiesce(const mf_ctx* c);
+
+// Every entry point that touches a context first waits until the context's
+// pipelined batches (mf_apply_batch_async) have finished running, then binds
+// its device and stream to the calling thread.
 void bind(const mf_ctx* c) {
+  quiesce(c);
   MF_CUDA(cudaSetDevice(c->device));
   mf::g_alloc_stream = c->stream;
 }
@@ -271,6 +283,129 @@ void stage_inputs(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* 
   if (c->h_counters[0] != 0) MF_FAIL(MF_EINVAL, "update endpoints must be distinct vertex ids in [0, n)");
 }
 
+// ---- the pipelined engine ---------------------------------------------------------
+//
+// The reference's misfit_async launches batch i+1 before it collects batch i
+// (src/misfit_async/misfit_async.cu:826-876): launchBatch does the host-side
+// work and queues the device work, syncAndCollect waits for it.  Here every
+// stage of a batch runs on the device and the host only orchestrates, so the
+// orchestration itself moves off the caller's thread: mf_apply_batch_async
+// queues the batch for the context's worker thread and returns at once, the
+// worker runs the queued batches one after another on the context's stream
+// (so the results are those of mf_apply_batch in the same order), and
+// mf_collect waits for the oldest one.  The caller's thread is free between
+// the calls, as the reference's host thread is free while its GPU works.
+
+}  // namespace
+
+namespace mf {
+struct AsyncJob {
+  const int32_t* u = nullptr;
+  const int32_t* v = nullptr;
+  const uint8_t* ins = nullptr;
+  int64_t m = 0;
+  bool done = false;
+  int status = MF_OK;
+  std::string error;
+  mf_batch_stats stats{};
+};
+
+struct AsyncQueue {
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<std::shared_ptr<AsyncJob>> todo;     // queued, not started
+  std::deque<std::shared_ptr<AsyncJob>> issued;   // every uncollected batch, oldest first
+  bool busy = false;                              // the worker is running a batch
+  bool stop = false;
+  std::thread worker;
+};
+}  // namespace mf
+
+namespace {
+
+void async_worker(mf_ctx* c) {
+  mf::AsyncQueue& q = *c->aq;
+  for (;;) {
+    std::shared_ptr<mf::AsyncJob> j;
+    {
+      std::unique_lock<std::mutex> lk(q.mu);
+      q.cv.wait(lk, [&] { return q.stop || !q.todo.empty(); });
+      if (q.todo.empty()) return;
+      j = q.todo.front();
+      q.todo.pop_front();
+      q.busy = true;
+    }
+    const int st = guarded([&] {
+      mf::bind_device(c);
+      stage_inputs(c, j->u, j->v, j->ins, j->m, cudaMemcpyHostToDevice);
+      run_batch(c, j->m);
+    });
+    {
+      std::lock_guard<std::mutex> lk(q.mu);
+      j->status = st;
+      if (st != MF_OK) j->error = mf::get_error();
+      j->stats = c->stats;
+      j->done = true;
+      q.busy = false;
+    }
+    q.cv.notify_all();
+  }
+}
+
+void enqueue_async(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
+  if (!c->aq) {
+    c->aq = new mf::AsyncQueue();
+    c->aq->worker = std::thread(async_worker, c);
+  }
+  auto j = std::make_shared<mf::AsyncJob>();
+  j->u = u;
+  j->v = v;
+  j->ins = ins;
+  j->m = m;
+  {
+    std::lock_guard<std::mutex> lk(c->aq->mu);
+    c->aq->todo.push_back(j);
+    c->aq->issued.push_back(j);
+    c->pending = true;
+  }
+  c->aq->cv.notify_all();
+}
+
+// Waits for the oldest uncollected batch and removes it; null if none.
+std::shared_ptr<mf::AsyncJob> collect_oldest(mf_ctx* c) {
+  if (!c->aq) return nullptr;
+  std::unique_lock<std::mutex> lk(c->aq->mu);
+  if (c->aq->issued.empty()) return nullptr;
+  std::shared_ptr<mf::AsyncJob> j = c->aq->issued.front();
+  c->aq->cv.wait(lk, [&] { return j->done; });
+  c->aq->issued.pop_front();
+  c->pending = !c->aq->issued.empty();
+  return j;
+}
+
+// Waits until the worker has nothing queued or running (results stay
+// uncollected).
+void quiesce(const mf_ctx* c) {
+  mf::AsyncQueue* q = c->aq;
+  if (!q) return;
+  std::unique_lock<std::mutex> lk(q->mu);
+  q->cv.wait(lk, [&] { return q->todo.empty() && !q->busy; });
+}
+
+void stop_async(mf_ctx* c) {
+  if (!c->aq) return;
+  quiesce(c);
+  {
+    std::lock_guard<std::mutex> lk(c->aq->mu);
+    c->aq->stop = true;
+  }
+  c->aq->cv.notify_all();
+  if (c->aq->worker.joinable()) c->aq->worker.join();
+  delete c->aq;
+  c->aq = nullptr;
+  c->pending = false;
+}
+
 // ---- .egr ----------------------------------------------------------------------
 
 struct EgrHeader {
@@ -339,7 +474,9 @@ mf_ctx* open_egr(const char* path, int gpu) {
     const size_t chunk = (size_t)64 << 20;
     void* pin[2] = {nullptr, nullptr};
     cudaEvent_t done[2];
+    mf::note_alloc();
     MF_CUDA(cudaMallocHost(&pin[0], chunk));
+    mf::note_alloc();
     MF_CUDA(cudaMallocHost(&pin[1], chunk));
     MF_CUDA(cudaEventCreate(&done[0]));
     MF_CUDA(cudaEventCreate(&done[1]));
@@ -392,6 +529,11 @@ int write_egr_int64(const std::string& out_path, int32_t n, const std::vector<in
     std::remove(tmp.c_str());
     MF_FAIL(MF_EIO, "failed writing " + tmp);
   }
+  // Fault injection for the crash-safety test: end the process after the
+  // temporary file is complete and flushed, before it replaces out_path --
+  // the moment core/flash_compactor.h:88-104 guards against.
+  if (const char* x = std::getenv("MISFIT_GB_EXIT_BEFORE_RENAME"))
+    if (std::strcmp(x, "1") == 0) std::_Exit(86);
   if (std::rename(tmp.c_str(), out_path.c_str()) != 0) MF_FAIL(MF_EIO, "rename " + tmp + " -> " + out_path + " failed");
   std::string dir = ".";
   const size_t slash = out_path.find_last_of('/');
@@ -455,6 +597,7 @@ int mf_open_csr(int32_t n, const int64_t* nindex, const int32_t* nlist, int gpu,
 
 int mf_close(mf_ctx* c) {
   if (!c) return MF_OK;
+  stop_async(c);
   return guarded([&] {
     cudaSetDevice(c->device);
     mf::g_alloc_stream = c->stream;
@@ -549,7 +692,7 @@ int mf_flag_updates_noalloc(mf_ctx* c, const int32_t* u, const int32_t* v, int64
 int mf_apply_batch(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
   return guarded([&] {
     need(c && m >= 0 && (m == 0 || (u && v && ins)), MF_EINVAL, "bad arguments");
-    need(!c->pending, MF_EINVAL, "an asynchronous batch is pending; call mf_sync first");
+    need(!c->pending, MF_EINVAL, "asynchronous batches are pending; collect them (mf_collect / mf_sync) first");
     bind(c);
     stage_inputs(c, u, v, ins, m, cudaMemcpyHostToDevice);
     run_batch(c, m);
@@ -559,7 +702,7 @@ int mf_apply_batch(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t*
 int mf_apply_batch_device(mf_ctx* c, const int32_t* d_u, const int32_t* d_v, const uint8_t* d_ins, int64_t m) {
   return guarded([&] {
     need(c && m >= 0 && (m == 0 || (d_u && d_v && d_ins)), MF_EINVAL, "bad arguments");
-    need(!c->pending, MF_EINVAL, "an asynchronous batch is pending; call mf_sync first");
+    need(!c->pending, MF_EINVAL, "asynchronous batches are pending; collect them (mf_collect / mf_sync) first");
     bind(c);
     stage_inputs(c, d_u, d_v, d_ins, m, cudaMemcpyDeviceToDevice);
     run_batch(c, m);
@@ -567,26 +710,49 @@ int mf_apply_batch_device(mf_ctx* c, const int32_t* d_u, const int32_t* d_v, con
 }
 
 int mf_apply_batch_async(mf_ctx* c, const int32_t* u, const int32_t* v, const uint8_t* ins, int64_t m) {
-  // The device path reads sizes back between stages, so the batch runs to
-  // completion here; the call exists so that pipelined callers keep the
-  // launch/collect structure of the reference's async engine.
   return guarded([&] {
     need(c && m >= 0 && (m == 0 || (u && v && ins)), MF_EINVAL, "bad arguments");
-    need(!c->pending, MF_EINVAL, "an asynchronous batch is pending; call mf_sync first");
-    bind(c);
-    stage_inputs(c, u, v, ins, m, cudaMemcpyHostToDevice);
-    run_batch(c, m);
-    c->pending = true;
+    enqueue_async(c, u, v, ins, m);
   });
 }
 
+int mf_collect(mf_ctx* c, mf_batch_stats* out) {
+  if (!c) {
+    mf::set_error("null context");
+    return MF_EINVAL;
+  }
+  std::shared_ptr<mf::AsyncJob> j = collect_oldest(c);
+  if (!j) {
+    mf::set_error("no asynchronous batch to collect");
+    return MF_EINVAL;
+  }
+  if (out) *out = j->stats;
+  mf::set_error(j->error);
+  return j->status;
+}
+
 int mf_sync(mf_ctx* c) {
-  return guarded([&] {
-    need(c != nullptr, MF_EINVAL, "null context");
+  if (!c) {
+    mf::set_error("null context");
+    return MF_EINVAL;
+  }
+  int first = MF_OK;
+  std::string err;
+  while (std::shared_ptr<mf::AsyncJob> j = collect_oldest(c)) {
+    if (first == MF_OK && j->status != MF_OK) {
+      first = j->status;
+      err = j->error;
+    }
+  }
+  const int st = guarded([&] {
     bind(c);
     MF_CUDA(cudaStreamSynchronize(c->stream));
-    c->pending = false;
   });
+  if (first != MF_OK) {
+    mf::set_error(err);
+    return first;
+  }
+  return st;
 }
 
 int mf_last_batch_stats(mf_ctx* c, mf_batch_stats* out) {
@@ -883,6 +1049,7 @@ int mf_profile_read(mf_ctx* c, double* ms, int64_t* calls, double* bytes, int ca
 }
 
 int64_t mf_kernel_launches(void) { return (int64_t)mf::g_launches.load(); }
+int64_t mf_allocations(void) { return (int64_t)mf::g_allocs.load(); }
 
 int mf_trace_enable(mf_ctx* c, int on) {
   return guarded([&] {

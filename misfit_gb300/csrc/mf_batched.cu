@@ -117,6 +117,7 @@ void pinned_reserve(uint8_t** p, size_t* cap, size_t need) {
   if (*p) cudaFreeHost(*p);
   *p = nullptr;
   *cap = 0;
+  note_alloc();
   MF_CUDA(cudaMallocHost(reinterpret_cast<void**>(p), need));
   *cap = need;
 }
@@ -219,7 +220,7 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
     mf_ctx* c = ctxs[i];
     need(c != nullptr, MF_EINVAL, "null context");
     need(c->device == device, MF_EINVAL, "contexts must be on one GPU");
-    need(!c->pending, MF_EINVAL, "an asynchronous batch is pending; call mf_sync first");
+    need(!c->pending, MF_EINVAL, "asynchronous batches are pending; collect them (mf_collect / mf_sync) first");
     need(m[i] >= 0 && (m[i] == 0 || (u[i] && v[i] && ins[i])), MF_EINVAL, "bad batch arrays");
     for (int64_t k = 0; k < m[i]; ++k) {
       const int32_t a = u[i][k], b = v[i][k];
@@ -410,11 +411,18 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
     float kms = 0.f;
     MF_CUDA(cudaEventElapsedTime(&kms, E.e0, E.e1));
     stats.kernel_ms = kms;
+    // Every item the kernel completed gets its host-side state first; the
+    // items that reported an inconsistency are named afterwards, so that no
+    // completed context is left with host state that lags its device state.
+    std::vector<int64_t> bad_items;
     for (int64_t j = 0; j < k; ++j) {
       const int64_t i = kitems[j].idx;
       mf_ctx* c = ctxs[i];
       const int64_t* out = E.h_out + cta::kOutWords * j;
-      if (out[cta::kOutStatus] != 0) MF_FAIL(MF_ESTATE, "batched kernel reported an inconsistent item");
+      if (out[cta::kOutStatus] != 0) {
+        bad_items.push_back(i);
+        continue;
+      }
       if (out[cta::kOutSwapped]) {
         std::swap(c->aoff, c->aoff_alt);
         std::swap(c->aadj, c->aadj_alt);
@@ -433,6 +441,14 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
       c->stats.exact_sizes = out[cta::kOutExactSizes];
       c->stats.max_csr = c->max_csr;
       c->stats.device_ms = (double)(out[cta::kOutT1] - out[cta::kOutT0]) / 1e6;
+    }
+    if (!bad_items.empty()) {
+      std::string msg = "batched kernel reported an inconsistent state for batch";
+      msg += bad_items.size() > 1 ? "es" : "";
+      for (size_t b = 0; b < bad_items.size(); ++b) msg += (b ? ", " : " ") + std::to_string(bad_items[b]);
+      msg += "; those contexts must be rebuilt (the other batches completed)";
+      if (path_status != MF_OK) msg += "; multi-launch path: " + path_error;
+      MF_FAIL(MF_ESTATE, msg);
     }
     if (path_status != MF_OK) MF_FAIL(path_status, path_error);
   } else {

@@ -60,6 +60,10 @@ struct Failure {
 // launches can be reported (mf_kernel_launches).
 extern std::atomic<long long> g_launches;
 inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// Every device or pinned-host allocation of the library counts here
+// (mf_allocations), so that a caller can check that a call allocated nothing.
+extern std::atomic<long long> g_allocs;
+inline void note_alloc() { g_allocs.fetch_add(1, std::memory_order_relaxed); }
 // Per-kernel timing (MISFIT_GB_KTIME=1): the device is synchronised around
 // every launch and the host-timed milliseconds are summed per kernel name and
 // printed to stderr at exit.  Off by default; it slows everything down and is
@@ -115,9 +119,11 @@ struct DBuf {
     release();
     int64_t c = count < 16 ? 16 : count;
     if (g_alloc_stream) {
+      note_alloc();
       MF_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), sizeof(T) * (size_t)c, g_alloc_stream));
       s = g_alloc_stream;
     } else {
+      note_alloc();
       MF_CUDA(cudaMalloc(&p, sizeof(T) * (size_t)c));
     }
     cap = c;
@@ -132,6 +138,8 @@ struct DBuf {
     s = nullptr;
   }
 };
+
+struct AsyncQueue;   // mf_api.cu
 
 // ---- read-only view of the current graph ----------------------------------
 
@@ -510,6 +518,10 @@ struct mf_ctx {
   // pinned staging for host-input batches
   uint8_t* h_stage = nullptr;
   int64_t h_stage_cap = 0;
+  // the pipelined engine: batches enqueued by mf_apply_batch_async run in
+  // order on this context's worker thread (made on first use); `pending`
+  // counts the ones not yet collected
+  mf::AsyncQueue* aq = nullptr;
   bool pending = false;
 
   mf::GraphView view() const {
@@ -634,6 +646,7 @@ void apply_overlay(mf_ctx* c, int64_t m);          // uses c->bu/bv/bins
 void flag_updates(mf_ctx* c, int64_t m);           // c->bu/bv -> c->bins
 // host u/v -> host ins_out through a fixed device array; m <= MF_NOALLOC_MAX_UPDATES
 void flag_updates_noalloc(mf_ctx* c, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out);
+void noalloc_refresh(int device);   // scratch address of the no-allocation flags, looked up again
 void compact_graph(mf_ctx* c, std::vector<int64_t>& nindex_out, std::vector<int32_t>& nlist_out);
 void rebase(mf_ctx* c);
 void greedy_mis(mf_ctx* c, uint8_t* d_out);

@@ -721,6 +721,17 @@ unsigned char* noalloc_scratch(int device) {
 
 }  // namespace
 
+// Looks the scratch address up again for `device` (current on the calling
+// thread).  Contexts call this when they are created, so that a device
+// whose primary context was reset and re-created gets the new address.
+void noalloc_refresh(int device) {
+  if (device < 0 || device >= kNaMaxDevices) return;
+  void* p = nullptr;
+  MF_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  g_na_base[device] = static_cast<unsigned char*>(p);
+}
+
 void flag_updates_noalloc(mf_ctx* c, const int32_t* u, const int32_t* v, int64_t m, uint8_t* ins_out) {
   if (m > (int64_t)MF_NOALLOC_MAX_UPDATES)
     MF_FAIL(MF_ELIMIT, "mf_flag_updates_noalloc takes at most 65536 updates per call");

@@ -59,6 +59,7 @@ void evict(mf_ctx* c, PinnedSnapshot& snap) {
     if (snap.host) cudaFreeHost(snap.host);
     snap.host = nullptr;
     snap.cap = 0;
+    mf::note_alloc();
     MF_CUDA(cudaMallocHost(&snap.host, need));
     snap.cap = need;
   }
@@ -194,6 +195,12 @@ struct mf_pool {
       mf::g_alloc_stream = nullptr;
       lk.lock();
       v.busy = false;
+      // mf_pool_drain and mf_pool_get_mis wait on cv_done for "not busy":
+      // clearing the flag must wake them, or a waiter that checked while the
+      // move ran sleeps forever once the pool goes quiet (the stall of the
+      // eviction test: the last request's completion notified, then started
+      // this move).
+      cv_done.notify_all();
       if (status == MF_OK) {
         if (full) {
           v.resident = false;
@@ -510,12 +517,22 @@ int mf_pool_add_graph(mf_pool* p, int32_t n, const int64_t* nindex, const int32_
       me.busy = true;
       p->resident_bytes -= me.bytes;
       lk.unlock();
-      mf::bind_device(c);
-      mf::evict(c, me.snap);
+      try {
+        mf::bind_device(c);
+        mf::evict(c, me.snap);
+      } catch (...) {
+        mf::g_alloc_stream = nullptr;
+        lk.lock();
+        me.busy = false;   // the graph stays listed as resident; wake any waiter
+        p->resident_bytes += me.bytes;
+        p->cv_done.notify_all();
+        throw;
+      }
       mf::g_alloc_stream = nullptr;
       lk.lock();
       me.resident = false;
       me.busy = false;
+      p->cv_done.notify_all();
       p->st.evictions += 1;
       if (!me.queue.empty()) {
         p->enqueue_ready(id);

@@ -17,12 +17,12 @@ LIB_PATH = os.path.join(_HERE, "lib", "libmisfit_gb.so")
 EXPORTS = [
     "mf_version", "mf_status_string", "mf_last_error", "mf_open_egr", "mf_open_csr", "mf_close",
     "mf_num_nodes", "mf_num_base_entries", "mf_set_mis", "mf_get_mis", "mf_mis_size", "mf_greedy_mis",
-    "mf_flag_updates", "mf_flag_updates_noalloc", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_sync",
+    "mf_flag_updates", "mf_flag_updates_noalloc", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_collect", "mf_sync",
     "mf_last_batch_stats", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
     "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_set_exact", "mf_compact", "mf_read_mis_file",
     "mf_write_mis_file", "mf_read_batch_file", "mf_parse_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
     "mf_trace_count", "mf_trace_get", "mf_stage_name", "mf_profile_enable", "mf_profile_reset",
-    "mf_profile_read", "mf_kernel_launches",
+    "mf_profile_read", "mf_kernel_launches", "mf_allocations",
     "mf_pool_create", "mf_pool_destroy", "mf_pool_add_graph", "mf_pool_submit", "mf_pool_wait", "mf_pool_drain",
     "mf_pool_get_mis", "mf_pool_stats_get", "mf_pool_set_budget",
     "mf_batched_default_opts", "mf_apply_batches", "mf_pool_set_batching",
@@ -111,6 +111,7 @@ def _lib():
         "mf_apply_batch": (C.c_int, [_P, _I32P, _I32P, _U8P, C.c_int64]),
         "mf_apply_batch_device": (C.c_int, [_P, _P, _P, _P, C.c_int64]),
         "mf_apply_batch_async": (C.c_int, [_P, _I32P, _I32P, _U8P, C.c_int64]),
+        "mf_collect": (C.c_int, [_P, C.c_void_p]),
         "mf_sync": (C.c_int, [_P]),
         "mf_last_batch_stats": (C.c_int, [_P, C.POINTER(BatchStats)]),
         "mf_get_row": (C.c_int, [_P, C.c_int32, _I32P, C.c_int64, _I64P]),
@@ -133,6 +134,7 @@ def _lib():
         "mf_profile_reset": (C.c_int, [_P]),
         "mf_profile_read": (C.c_int, [_P, C.POINTER(C.c_double), _I64P, C.POINTER(C.c_double), C.c_int]),
         "mf_kernel_launches": (C.c_int64, []),
+        "mf_allocations": (C.c_int64, []),
         "mf_trace_enable": (C.c_int, [_P, C.c_int]),
         "mf_trace_count": (C.c_int, [_P, _I64P]),
         "mf_trace_get": (C.c_int, [_P, C.c_int64, C.c_int, C.c_void_p, C.c_int64, _I64P]),
@@ -264,6 +266,30 @@ class Graph:
         _check(_lib().mf_apply_batch_device(self._h, C.c_void_p(d_u), C.c_void_p(d_v), C.c_void_p(d_ins), m),
                "mf_apply_batch_device")
 
+    def apply_batch_async(self, u, v, ins):
+        """Queue a batch for the pipelined engine; it runs on the context's
+        worker thread.  The arrays are kept alive here until collected."""
+        u, v, ins = _i32(u), _i32(v), _u8(ins)
+        _check(_lib().mf_apply_batch_async(self._h, _ptr(u, C.c_int32), _ptr(v, C.c_int32),
+                                           _ptr(ins, C.c_uint8), u.size), "mf_apply_batch_async")
+        self._queued = getattr(self, "_queued", []) + [(u, v, ins)]
+
+    def collect(self):
+        """Wait for the oldest queued batch; its statistics (raises its error)."""
+        st = BatchStats()
+        try:
+            _check(_lib().mf_collect(self._h, C.c_void_p(C.addressof(st))), "mf_collect")
+        finally:
+            q = getattr(self, "_queued", [])
+            self._queued = q[1:]
+        return st.as_dict()
+
+    def sync(self):
+        try:
+            _check(_lib().mf_sync(self._h), "mf_sync")
+        finally:
+            self._queued = []
+
     def stats(self):
         st = BatchStats()
         _check(_lib().mf_last_batch_stats(self._h, C.byref(st)), "mf_last_batch_stats")
@@ -376,6 +402,12 @@ class Graph:
 def kernel_launches():
     """Kernels launched by libmisfit_gb in this process so far."""
     return int(_lib().mf_kernel_launches())
+
+
+def allocations():
+    """Device and pinned-host allocations made by libmisfit_gb in this
+    process so far."""
+    return int(_lib().mf_allocations())
 
 
 def read_mis_file(path, n):

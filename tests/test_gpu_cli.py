@@ -83,3 +83,30 @@ def test_cli_usage_and_errors(gpu_lib, tmp_path):
     assert out.returncode == 1 and "Usage" in out.stderr
     out = subprocess.run([exe, str(tmp_path / "none.egr"), "m", "b", "1", "0"], capture_output=True, text=True)
     assert out.returncode == 1 and "ERROR" in out.stderr
+
+
+def test_cli_compaction_interrupted_before_rename(gpu_lib, tmp_path):
+    """Crash safety of the end-of-run compaction (core/flash_compactor.h:88-104:
+    write <egr>.tmp.<pid>, fsync, rename over the input, fsync the folder).
+    The process is ended after the temporary file is complete and before the
+    rename: the input .egr must be untouched and the final MIS already saved;
+    the temporary file holds the whole compacted graph; a rerun from the same
+    inputs then compacts normally."""
+    g, n, egr, folder = _setup(tmp_path, "er1500")
+    nb = int(g["num_batches"])
+    exe = os.path.abspath(os.path.join(BIN, "misfit"))
+    before = egr.read_bytes()
+    env = dict(os.environ, MISFIT_GB_EXIT_BEFORE_RENAME="1")
+    out = subprocess.run([exe, str(egr), str(tmp_path / "mis.txt"), str(folder), str(nb), "0"], cwd=str(tmp_path),
+                         env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 86, (out.returncode, out.stderr)
+    assert egr.read_bytes() == before
+    mis = W.read_mis_file(str(tmp_path / "datasets" / "Final_MISs" / "er1500_flash_final_mis.txt"), n)
+    assert np.array_equal(mis, G.main_final_mis(g, "sync"))
+    tmps = [p for p in os.listdir(str(tmp_path)) if p.startswith(egr.name + ".tmp.")]
+    assert len(tmps) == 1
+    assert hashlib.sha256((tmp_path / tmps[0]).read_bytes()).digest() == bytes(g["compact_sha256"])
+    out = subprocess.run([exe, str(egr), str(tmp_path / "mis.txt"), str(folder), str(nb), "0"], cwd=str(tmp_path),
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    assert hashlib.sha256(egr.read_bytes()).digest() == bytes(g["compact_sha256"])

@@ -86,6 +86,57 @@ def test_reference_engine_golden(name, gpu_lib):
     gr.close()
 
 
+def test_pipelined_engine(gpu_lib):
+    """mf_apply_batch_async / mf_collect in the loop of the reference's
+    misfit_async (batch i+1 launched before batch i is collected): the same
+    memberships as the plain engine, batch by batch; the queue's rules."""
+    g = G.load("er1500")
+    bs = G.batches(g)
+    plain = native.Graph.from_csr(g["nindex"], g["nlist"])
+    piped = native.Graph.from_csr(g["nindex"], g["nlist"])
+    plain.set_mis(g["mis0"])
+    piped.set_mis(g["mis0"])
+    want = []
+    for u, v, ins in bs:
+        plain.apply_batch(u, v, ins)
+        want.append((plain.get_mis(), plain.stats()))
+    piped.apply_batch_async(*bs[0])
+    for i in range(len(bs)):
+        if i + 1 < len(bs):
+            piped.apply_batch_async(*bs[i + 1])
+        st = piped.collect()
+        assert st["updates"] == bs[i][0].size
+        assert st["sub_batches"] == want[i][1]["sub_batches"] and st["clusters"] == want[i][1]["clusters"]
+    assert np.array_equal(piped.get_mis(), want[-1][0])
+    assert np.array_equal(piped.get_mis(), g["b%d_mis_oracle" % (len(bs) - 1)])
+    # nothing left to collect
+    with pytest.raises(native.MisfitError) as e:
+        piped.collect()
+    assert e.value.status == -1
+    # the plain entry point refuses a context with uncollected batches
+    u, v, ins = bs[0]
+    piped.apply_batch_async(u, v, ins)
+    with pytest.raises(native.MisfitError) as e:
+        piped.apply_batch(u, v, ins)
+    assert e.value.status == -1
+    piped.sync()
+    # a bad batch fails when collected; the batch queued after it still runs
+    ref = native.Graph.from_csr(g["nindex"], g["nlist"])
+    ref.set_mis(piped.get_mis())
+    bad = (np.array([0, 5], np.int32), np.array([1, 5], np.int32), np.zeros(2, np.uint8))
+    piped.apply_batch_async(*bad)
+    piped.apply_batch_async(*bs[1])
+    with pytest.raises(native.MisfitError) as e:
+        piped.collect()
+    assert e.value.status == -1
+    piped.collect()
+    for u, v, ins in (bs[0], bs[1]):
+        ref.apply_batch(u, v, ins)
+    assert np.array_equal(piped.get_mis(), ref.get_mis())
+    for gr in (plain, piped, ref):
+        gr.close()
+
+
 def _stream(kind, seed, batches, size, endpoints="uniform"):
     if kind == "er":
         n = 3000

@@ -129,3 +129,27 @@ def test_pool_batched_dispatch_matches_dedicated_contexts(gpu_lib):
     assert st["errors"] == 1
     assert st["batched_steps"] > 0 and 0 < st["batched_requests"] < 3 * len(graphs)
     assert st["evictions"] > 0
+
+
+@pytest.mark.timeout(240, method="thread")
+def test_pool_drain_wakes_after_eviction(gpu_lib):
+    """A request's completion can push the pool over its budget, so the
+    worker evicts an idle graph right after it reports the request done.
+    mf_pool_drain and mf_pool_get_mis wait for every graph to be idle; they
+    must wake when that eviction ends, not only when a request completes.
+    Many submit-then-drain cycles at a budget that evicts on every
+    completion; the timeout turns a lost wake-up into a failure."""
+    graphs = _graphs(4, 41)
+    plans = _streams(graphs, 2, 400)
+    budget = int(1.2 * max((ni.size - 1) * 200 + nl.size * 8 for ni, nl in graphs))
+    with native.Pool(budget, workers=2) as pool:
+        gids = [pool.add_graph(ni, nl, plans[k][0]) for k, (ni, nl) in enumerate(graphs)]
+        for b in range(2):
+            for k, gid in enumerate(gids):
+                u, v, ins = plans[k][1][b]
+                rid = pool.submit(gid, u, v, ins)
+                pool.drain()
+                assert pool.wait(rid) >= 0
+                assert np.array_equal(pool.get_mis(gid), plans[k][2][b]), (b, k)
+        st = pool.stats()
+    assert st["errors"] == 0 and st["evictions"] > 0

@@ -65,6 +65,26 @@ def test_noalloc_flags_match_two_calls_in_a_row(gpu_lib, shuffle_rows):
         g.close()
 
 
+def test_noalloc_first_call_on_a_fresh_context_allocates_nothing(gpu_lib):
+    """The first call on a new context, at the largest size, before any
+    other entry point has grown the context's staging buffers: the
+    library's allocation counter does not move, and a second call after it
+    still matches mf_flag_updates."""
+    nindex, nlist = _graph(False, 13)
+    g = native.Graph.from_csr(nindex, nlist)
+    try:
+        q = _queries(nindex, nlist, MAXM, 31)
+        before = native.allocations()
+        got = g.flag_updates_noalloc(*q)
+        again = g.flag_updates_noalloc(q[0][:1000], q[1][:1000])
+        assert native.allocations() == before
+        assert np.array_equal(got, g.flag_updates(*q))
+        assert np.array_equal(again, got[:1000])
+        assert native.allocations() > before   # mf_flag_updates grew the staging buffers
+    finally:
+        g.close()
+
+
 def test_noalloc_limits_and_errors(gpu_lib):
     nindex, nlist = _graph(False, 12)
     g = native.Graph.from_csr(nindex, nlist)
