@@ -233,59 +233,154 @@ __device__ __forceinline__ void warp_row_each(const GraphView& g, int32_t x, F f
 
 // Load-balanced traversal of the rows of list[0..cnt): offs is the exclusive
 // prefix of the row position counts (base positions + added entries; a
-// count of 0 skips the row), cnt+1 entries.  Every warp takes chunks of
-// 256 consecutive positions, so a hub row is spread over many warps.
-// f(i, x, y) is called for every live element y of row(x = list[i]).
-// Returns the number of elements visited by the calling thread.
+// count of 0 skips the row), cnt+1 entries.  f(i, x, y, aux) is called for
+// every live element y of row(x = list[i]); aux(i, x) is evaluated once per
+// visited row (a per-row value such as the row's push tag).
+//
+// Every warp owns one contiguous span of positions (the total split evenly
+// over the grid's warps), so a hub row is spread over many warps and the
+// work per warp is even.  The warp finds the row of its first position once,
+// with a 32-way cooperative search over offs, then walks its span 32 rows at
+// a time: the rows' ends and metadata (base offset, length, added offset,
+// tombstone flag, aux) are loaded in one round of parallel loads into shared
+// memory; each lane then maps its position to its row with at most five
+// shared-memory probes (none when the whole 32-position window lies in one
+// row) and the element loads of four windows are issued before any is used.
+// Kernels that call it run blocks of kLbThreads threads.
+constexpr int kLbThreads = 256;
+constexpr int kLbWarps = kLbThreads / 32;
+constexpr int kLbUnroll = 4;
+
+struct LbStage {
+  int64_t end[32];    // end position (exclusive) of staged row k
+  int64_t b0[32];     // nindex[x]
+  int64_t a0[32];     // aoff[x]
+  int32_t x[32];
+  int32_t nb[32];     // base positions of row(x)
+  uint32_t aux[32];
+  int64_t start;      // start position of staged row 0
+  uint32_t filt;      // bit k: row k has tombstoned base entries
+};
+
+struct NoAux {
+  __device__ __forceinline__ uint32_t operator()(int64_t, int32_t) const { return 0u; }
+};
+
+template <class A, class F>
+__device__ __forceinline__ int64_t lb_rows_aux(const GraphView& g, const int32_t* list, const int64_t* offs, int64_t cnt,
+                                               A aux, F f) {
+  __shared__ LbStage lb_stage[kLbWarps];
+  const int lane = threadIdx.x & 31;
+  LbStage& st = lb_stage[(threadIdx.x >> 5) & (kLbWarps - 1)];
+  const int64_t total = offs[cnt];
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t per = (((total + nwarps - 1) / nwarps) + 31) & ~(int64_t)31;
+  int64_t pos = w * per;
+  const int64_t stop = pos + per < total ? pos + per : total;
+  if (pos >= stop) return 0;
+  // the row holding pos: offs[lo] <= pos < offs[hi]
+  int64_t lo = 0, hi = cnt;
+  while (hi - lo > 1) {
+    const int64_t step = (hi - lo + 31) >> 5;
+    const int64_t idx = lo + (int64_t)lane * step;
+    const bool le = idx < hi && offs[idx] <= pos;
+    const unsigned m = __ballot_sync(0xffffffffu, le);
+    const int k = 31 - __clz(m);
+    lo += (int64_t)k * step;
+    const int64_t nh = lo + step;
+    hi = nh < hi ? nh : hi;
+  }
+  int64_t ri = lo;
+  int64_t visited = 0;
+  while (pos < stop) {
+    // stage rows ri .. ri+31
+    __syncwarp();
+    const int64_t r = ri + lane;
+    int64_t e = total, b0 = 0, a0 = 0;
+    int32_t x = 0, nb = 0;
+    bool tomb = false;
+    uint32_t av = 0;
+    if (r < cnt) {
+      const int64_t s0 = offs[r];
+      e = offs[r + 1];
+      if (lane == 0) st.start = s0;
+      if (e > s0) {
+        x = list[r];
+        b0 = g.nindex[x];
+        nb = (int32_t)(g.nindex[x + 1] - b0);
+        a0 = g.aoff[x];
+        tomb = g.dead[x] != 0;
+        av = aux(r, x);
+      }
+    }
+    st.end[lane] = e;
+    st.b0[lane] = b0;
+    st.a0[lane] = a0;
+    st.x[lane] = x;
+    st.nb[lane] = nb;
+    st.aux[lane] = av;
+    const unsigned fm = __ballot_sync(0xffffffffu, tomb);
+    if (lane == 0) st.filt = fm;
+    __syncwarp();
+    const int64_t last = st.end[31];
+    const int64_t cover = last < stop ? last : stop;
+    for (; pos < cover; pos += 32 * kLbUnroll) {
+      // first staged row that ends after pos (the ends are sorted)
+      const int kb = __popc(__ballot_sync(0xffffffffu, st.end[lane] <= pos));
+      int32_t yv[kLbUnroll];
+      int kr[kLbUnroll];
+      bool ok[kLbUnroll];
+#pragma unroll
+      for (int q = 0; q < kLbUnroll; ++q) {
+        const int64_t wbase = pos + 32 * q;
+        const int64_t p = wbase + lane;
+        ok[q] = false;
+        kr[q] = 0;
+        yv[q] = 0;
+        if (p < cover) {
+          int k = kb;
+          if (st.end[kb] <= wbase + 31) {
+            int l = kb, h = 31;
+            while (l < h) {
+              const int mid = (l + h) >> 1;
+              if (st.end[mid] > p) h = mid; else l = mid + 1;
+            }
+            k = l;
+          }
+          const int64_t rs = k == 0 ? st.start : st.end[k - 1];
+          const int64_t j = p - rs;
+          const int32_t nbk = st.nb[k];
+          if (j < nbk) {
+            const int64_t gk = st.b0[k] + j;
+            yv[q] = __ldg(g.nlist + gk);
+            ok[q] = !((st.filt >> k) & 1u) || live_at(g.live, gk);
+          } else {
+            yv[q] = g.aadj[st.a0[k] + (j - nbk)];
+            ok[q] = true;
+          }
+          kr[q] = k;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kLbUnroll; ++q) {
+        if (ok[q]) {
+          ++visited;
+          f(ri + kr[q], st.x[kr[q]], yv[q], st.aux[kr[q]]);
+        }
+      }
+    }
+    pos = cover;
+    ri += 32;
+  }
+  return visited;
+}
+
 template <class F>
 __device__ __forceinline__ int64_t lb_rows(const GraphView& g, const int32_t* list, const int64_t* offs, int64_t cnt,
                                            F f) {
-  constexpr int64_t kChunk = 256;
-  const int64_t total = offs[cnt];
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t visited = 0;
-  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kChunk; base < total;
-       base += nwarps * kChunk) {
-    int64_t i = 0;
-    if (lane == 0) {
-      int64_t lo = 0, hi = cnt;  // last i with offs[i] <= base
-      while (hi - lo > 1) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (offs[mid] <= base) lo = mid; else hi = mid;
-      }
-      i = lo;
-    }
-    i = __shfl_sync(0xffffffffu, i, 0);
-    const int64_t end = base + kChunk < total ? base + kChunk : total;
-    int64_t cur = -1, next_off = 0, row_off = 0, nb = 0, b0 = 0, a0 = 0;
-    int32_t x = 0;
-    bool filt = false;
-    for (int64_t e = base + lane; e < end; e += 32) {
-      if (cur < 0 || e >= next_off) {
-        while (offs[i + 1] <= e) ++i;
-        cur = i;
-        x = list[i];
-        row_off = offs[i];
-        next_off = offs[i + 1];
-        b0 = g.nindex[x];
-        nb = g.nindex[x + 1] - b0;
-        a0 = g.aoff[x];
-        filt = g.dead[x] != 0;
-      }
-      const int64_t j = e - row_off;
-      int32_t y;
-      if (j < nb) {
-        if (filt && !live_at(g.live, b0 + j)) continue;
-        y = __ldg(g.nlist + b0 + j);
-      } else {
-        y = g.aadj[a0 + (j - nb)];
-      }
-      ++visited;
-      f(i, x, y);
-    }
-  }
-  return visited;
+  return lb_rows_aux(g, list, offs, cnt, NoAux{},
+                     [&](int64_t i, int32_t x, int32_t y, uint32_t) { f(i, x, y); });
 }
 
 __device__ __forceinline__ int64_t row_positions(const GraphView& g, int32_t x) {

@@ -42,6 +42,7 @@ int64_t initial_max_csr(int32_t n, uint64_t edges) {
 namespace {
 
 constexpr int kTB = 256;
+static_assert(kTB == kLbThreads, "lb_rows kernels run kLbThreads-thread blocks");
 constexpr int32_t kSkip = -2;
 
 inline unsigned grid_for(int64_t n, int per = kTB) {
@@ -228,8 +229,11 @@ constexpr int kBitsWords = kBitsThreads * kBitsPerThread;       // words per blo
 
 // One pass over the seed rows: the hop-1 bit of every element, and per seed
 // the sum of len(h) over row(s) for the packed-size upper bound (uacc).
-__global__ void k_lb_hop1_bound(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t* hbits,
-                                unsigned long long* uacc, unsigned long long* work) {
+// deg[y] (DeltaOverlay::degree) is at least the overlay row length of y (a
+// tombstone removes at least one base entry), so the sums stay upper bounds.
+__global__ void __launch_bounds__(kLbThreads) k_lb_hop1_bound(GraphView g, const int32_t* deg, const int32_t* seeds,
+                                                              const int64_t* offs, int64_t ns, uint32_t* hbits,
+                                                              unsigned long long* uacc, unsigned long long* work) {
   int64_t cur = -1;
   unsigned long long acc = 0;
   const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
@@ -239,7 +243,7 @@ __global__ void k_lb_hop1_bound(GraphView g, const int32_t* seeds, const int64_t
       cur = i;
       acc = 0;
     }
-    acc += (unsigned long long)row_len(g, y);
+    acc += (unsigned long long)__ldg(deg + y);
   });
   if (cur >= 0 && acc) atomicAdd(uacc + cur, acc);
   add_work(work, vis);
@@ -741,13 +745,62 @@ __device__ __forceinline__ void cq_push(const ChunkQueue& q, int32_t idx, int32_
 }
 
 // Slot of chunk c: the last slot whose base is <= c (bases grow with slots).
+// Warp-cooperative (all lanes call it with the same c): a 32-way search, so
+// the dependent loads are log32(rows) rounds instead of log2(rows).
 __device__ __forceinline__ int64_t cq_slot(const ChunkQueue& q, int64_t rows, int64_t c) {
+  const int lane = threadIdx.x & 31;
   int64_t lo = 0, hi = rows;
   while (hi - lo > 1) {
-    const int64_t mid = (lo + hi) >> 1;
-    if (q.base[mid] <= c) lo = mid; else hi = mid;
+    const int64_t step = (hi - lo + 31) >> 5;
+    const int64_t idx = lo + (int64_t)lane * step;
+    const unsigned m = __ballot_sync(0xffffffffu, idx < hi && q.base[idx] <= c);
+    lo += (int64_t)(31 - __clz(m)) * step;
+    const int64_t nh = lo + step;
+    hi = nh < hi ? nh : hi;
   }
   return lo;
+}
+
+// Warp-cooperative: first position k in [k0, k1) of row(x) (nb base
+// positions, then the added entries) whose element is live and satisfies
+// pred, or -1.  Four 32-position windows are loaded before any is tested,
+// so each lane has four element loads (then four predicate loads) in
+// flight; the answer is the first window's lowest hit.
+template <class P>
+__device__ __forceinline__ int64_t warp_first_range(const GraphView& g, int32_t x, int64_t nb, int64_t k0, int64_t k1,
+                                                    P pred) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b0 = g.nindex[x];
+  const int64_t a0 = g.aoff[x];
+  const bool filt = g.dead[x] != 0;
+  for (int64_t base = k0; base < k1; base += 128) {
+    int32_t y[4];
+    bool live[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t k = base + 32 * q + lane;
+      y[q] = -1;
+      live[q] = false;
+      if (k < k1) {
+        if (k < nb) {
+          y[q] = __ldg(g.nlist + b0 + k);
+          live[q] = !filt || live_at(g.live, b0 + k);
+        } else {
+          y[q] = g.aadj[a0 + (k - nb)];
+          live[q] = true;
+        }
+      }
+    }
+    bool ok[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ok[q] = live[q] && pred(y[q]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const unsigned m = __ballot_sync(0xffffffffu, ok[q]);
+      if (m) return base + 32 * q + (__ffs(m) - 1);
+    }
+  }
+  return -1;
 }
 
 struct FirstQueues {
@@ -794,23 +847,12 @@ __global__ void k_first_warp(GraphView g, P pred, unsigned long long* firstpos, 
     const int64_t nb = g.nindex[x + 1] - g.nindex[x];
     const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
     const int64_t lim = np < kFirstBound ? np : kFirstBound;
-    bool found = false;
-    for (int64_t k0 = kProbe; k0 < lim; k0 += 32) {
-      const int64_t k = k0 + lane;
-      bool ok = false;
-      if (k < lim) {
-        const int32_t y = row_elem(g, x, k, nb);
-        ok = y >= 0 && pred(y);
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, ok);
-      if (m) {
-        if (lane == 0) firstpos[i] = (unsigned long long)(k0 + __ffs(m) - 1);
-        found = true;
-        break;
-      }
-    }
-    if (!found && np > kFirstBound && lane == 0)
+    const int64_t hit = warp_first_range(g, x, nb, kProbe, lim, pred);
+    if (hit >= 0) {
+      if (lane == 0) firstpos[i] = (unsigned long long)hit;
+    } else if (np > kFirstBound && lane == 0) {
       cq_push(q.rest, i, x, (np - kFirstBound + kFirstChunk - 1) / kFirstChunk);
+    }
   }
 }
 
@@ -821,9 +863,7 @@ __global__ void k_first_chunks(GraphView g, P pred, unsigned long long* firstpos
   const int64_t rows = (int64_t)(pk >> kChunkShift), chunks = (int64_t)(pk & kChunkMask);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t c = warp_id(); c < chunks; c += nw) {
-    int64_t slot = 0;
-    if (lane == 0) slot = cq_slot(q.rest, rows, c);
-    slot = __shfl_sync(0xffffffffu, slot, 0);
+    const int64_t slot = cq_slot(q.rest, rows, c);
     const int32_t i = q.rest.idx[slot];
     const int32_t x = q.rest.v[slot];
     const int64_t p0 = kFirstBound + (c - q.rest.base[slot]) * kFirstChunk;
@@ -836,19 +876,8 @@ __global__ void k_first_chunks(GraphView g, P pred, unsigned long long* firstpos
     const int64_t nb = g.nindex[x + 1] - g.nindex[x];
     const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
     const int64_t end = min(p0 + kFirstChunk, np);
-    for (int64_t k0 = p0; k0 < end; k0 += 32) {
-      const int64_t k = k0 + lane;
-      bool ok = false;
-      if (k < end) {
-        const int32_t y = row_elem(g, x, k, nb);
-        ok = y >= 0 && pred(y);
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, ok);
-      if (m) {
-        if (lane == 0) atomicMin(firstpos + i, (unsigned long long)(k0 + __ffs(m) - 1));
-        break;
-      }
-    }
+    const int64_t hit = warp_first_range(g, x, nb, p0, end, pred);
+    if (hit >= 0 && lane == 0) atomicMin(firstpos + i, (unsigned long long)hit);
   }
 }
 
@@ -911,9 +940,7 @@ __global__ void k_mark_need(GraphView g, ChunkQueue mq, uint32_t epoch, uint32_t
   const int64_t rows = (int64_t)(pk >> kChunkShift), chunks = (int64_t)(pk & kChunkMask);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t c = warp_id(); c < chunks; c += nw) {
-    int64_t slot = 0;
-    if (lane == 0) slot = cq_slot(mq, rows, c);
-    slot = __shfl_sync(0xffffffffu, slot, 0);
+    const int64_t slot = cq_slot(mq, rows, c);
     const int32_t x = mq.v[slot];
     const int64_t p0 = (c - mq.base[slot]) * kFirstChunk;
     const int64_t nb = g.nindex[x + 1] - g.nindex[x];
@@ -987,9 +1014,13 @@ __global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, co
   if ((t >> kRowBits) == epoch) push_w(wval, x, t);
 }
 
-__global__ void k_lb_push_hop(GraphView g, const int32_t* list, const int64_t* offs, int64_t cnt, uint32_t epoch,
-                              const uint32_t* bval, uint32_t* wval, unsigned long long* work) {
-  const int64_t vis = lb_rows(g, list, offs, cnt, [&](int64_t, int32_t x, int32_t y) { push_w(wval, y, bval[x]); });
+__global__ void __launch_bounds__(kLbThreads) k_lb_push_hop(GraphView g, const int32_t* list, const int64_t* offs,
+                                                            int64_t cnt, uint32_t epoch, const uint32_t* bval,
+                                                            uint32_t* wval, unsigned long long* work) {
+  // the row's tag is staged once per row with the row's metadata
+  const int64_t vis = lb_rows_aux(
+      g, list, offs, cnt, [&](int64_t, int32_t x) { return bval[x]; },
+      [&](int64_t, int32_t, int32_t y, uint32_t t) { push_w(wval, y, t); });
   add_work(work, vis);
 }
 
@@ -2110,7 +2141,7 @@ void front_compute(mf_ctx* c, Front& f, const int32_t* seeds, int64_t ns, cudaSt
   MF_CUDA(cudaMemsetAsync(f.uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), st));
   MF_CUDA(cudaMemsetAsync(f.cnt.p + 1, 0, sizeof(int64_t), st));
   row_offsets_into(c, seeds, ns, f.lb_offs, f.ws, st);
-  MF_K(k_lb_hop1_bound<<<lb_grid(c, k_lb_hop1_bound), kTB, 0, st>>>(g, seeds, f.lb_offs.p, ns, hbits, f.uacc.p,
+  MF_K(k_lb_hop1_bound<<<lb_grid(c, k_lb_hop1_bound), kTB, 0, st>>>(g, c->deg.p, seeds, f.lb_offs.p, ns, hbits, f.uacc.p,
                                                                     c->work.p + 2 * kStHop1));
   if (ns > 0) MF_K(k_seed_bits<<<grid_for(ns), kTB, 0, st>>>(seeds, ns, sbits));
   const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
