@@ -68,16 +68,24 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="skip the served and batched legs")
     ap.add_argument("--no-exact", action="store_true", help="skip the exact-MIS leg")
-    ap.add_argument("--served-graphs", type=int, default=64)
-    ap.add_argument("--graphs-nmax", type=int, default=200000,
-                    help="largest vertex count of the served/batched graph set (the batched configuration "
-                         "goes to 1,000,000 with 256 graphs)")
-    ap.add_argument("--served-requests", type=int, default=300)
-    ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrivals per second")
+    ap.add_argument("--batched-graphs", type=int, default=256, help="graphs of the batched form")
+    ap.add_argument("--served-graphs", type=int, default=1000, help="resident graphs of the serving form")
+    ap.add_argument("--graphs-nmax", type=int, default=1000000,
+                    help="largest vertex count of the served/batched graph sets (log-uniform from 1,000)")
+    ap.add_argument("--served-requests", type=int, default=1000, help="requests per arrival rate")
+    ap.add_argument("--served-rates", default="2000,10000,50000", help="Poisson arrival rates per second")
     ap.add_argument("--served-workers", type=int, default=8)
     ap.add_argument("--served-budget", type=float, default=0.6, help="HBM budget as a fraction of the footprint")
     ap.add_argument("--served-cta-limit", type=int, default=512,
                     help="largest request the served form's continuous batching gives to the persistent kernel")
+    ap.add_argument("--no-large", action="store_true", help="skip the 64-bit-layout leg (R-MAT scale 26)")
+    ap.add_argument("--large-only", action="store_true", help="run only the 64-bit-layout leg and print its JSON")
+    ap.add_argument("--large-scale", type=int, default=26)
+    ap.add_argument("--large-edge-factor", type=int, default=20)
+    ap.add_argument("--large-batch", type=int, default=1000000, help="toggles per batch of the large leg")
+    ap.add_argument("--large-seconds", type=float, default=60.0,
+                    help="device-time budget of the large leg's timed sample")
+    ap.add_argument("--large-dir", default=None, help="folder for the large .egr file (default: the system temp)")
     ap.add_argument("--served-only", action="store_true", help="run only the served leg and print its JSON")
     ap.add_argument("--batched-only", action="store_true",
                     help="run only the batched-form leg and print its JSON (profiling runs)")
@@ -215,49 +223,186 @@ def cpu_greedy(nindex, nlist, batches, flags):
 
 
 def run_reference(args, rank):
+    """The reference arm: the reference path restated on the CPU (the oracle,
+    OpenMP over all host cores) on the same batches, state carried from step
+    to step.  One oracle holds the graph and the membership for the whole
+    run.  Each step times the leading lines of its batch through the whole
+    path (overlay apply, split, neighbourhoods, clustering, repair) in
+    doubling chunks until the per-step budget is spent, then applies the
+    batch's remaining lines to the overlay only (untimed), so that the next
+    step starts from the graph the full batch leaves.  The membership evolves
+    through the timed lines only.  `value` is the timed lines over the time
+    spent on them; `ms_per_step` is that time per step (what the run really
+    spent), and each step's timed lines are listed."""
     if rank != 0:
         return
     import torch
     device = "cuda:%d" % int(os.environ.get("LOCAL_RANK", "0")) if torch.cuda.is_available() else "cpu"
     n, nindex, nlist, stream = make_workload(args, device)
     import oracle as O
-    orc0 = O.Oracle.from_csr(nindex, nlist)
+    orc0 = O.Oracle.from_csr(nindex, nlist)          # flags against the base graph
+    orc = O.Oracle.from_csr(nindex, nlist)           # the evolving state
+    orc.set_mis(O.greedy_mis(nindex, nlist))
     cores = os.cpu_count()
-    rates, lat = [], []
-    steps = args.warmup + args.steps
     budget = max(2.0, args.cpu_seconds / 2)
-    for i in range(steps):
+    timed_lines, timed_s, per_step = 0, 0.0, []
+    for i in range(args.warmup + args.steps):
         u, v = stream.next_batch(args.batch)
         ins = orc0.flag_updates(u, v)
-        rate, lines, spent = cpu_sample(n, nindex, nlist, (u, v), ins, budget)
+        done, spent, chunk = 0, 0.0, 16
+        while done < u.size and spent < budget:
+            k = min(chunk, u.size - done)
+            t = time.perf_counter()
+            orc.apply_batch(u[done:done + k], v[done:done + k], ins[done:done + k])
+            spent += time.perf_counter() - t
+            done += k
+            chunk *= 2
+        if done < u.size:
+            orc.apply_overlay(u[done:], v[done:], ins[done:])
         if i >= args.warmup:
-            rates.append(rate)
-            lat.append(spent / lines * args.batch * 1e3)
-    value = float(np.mean(rates))
+            timed_lines += done
+            timed_s += spent
+            per_step.append(done)
+    orc.close()
+    orc0.close()
+    value = timed_lines / timed_s
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.batch / value * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": timed_s / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded R-MAT + toggle stream)", "config": workload_config(args),
+        "step": "a bounded sample of one batch: its leading lines through the whole path, ~%.0f s each, "
+                "on the state every earlier batch left (graph: all lines; membership: the timed lines)" % budget,
+        "lines_timed_per_step": per_step, "sampled_fraction": timed_lines / float(args.steps * args.batch),
+        "extrapolated": False,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "oracle (reference path restated, OpenMP %d threads) on the leading lines "
-                                   "of each batch from the initial state, ~%.0f s per step" % (cores, budget)},
+                         "sample": "oracle (reference path restated, OpenMP %d threads): %d lines over %d steps "
+                                   "(%.1f s), the leading lines of each batch on the evolving state"
+                                   % (cores, timed_lines, args.steps, timed_s)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
+# ---- the 64-bit layout at scale ---------------------------------------------------------
+
+def run_large(args, local):
+    """R-MAT scale 26 (67,108,864 vertices), 20 undirected samples per vertex,
+    a,b,c,d = .57/.19/.19/.05, symmetrised and de-duplicated: more than 2^31
+    directed entries, so the .egr file takes the int64-sentinel layout.  The
+    graph is written to disk and opened through mf_open_egr (chunked pinned
+    reads, asynchronous copies).  Batches hold 1,000,000 toggles, 50/50
+    deletes and inserts, both endpoints proportional to current degree
+    (deletes: uniform over the edges; inserts: endpoints drawn by degree,
+    pairs not adjacent in the base graph).  Under the reference's split rule
+    a batch with hub endpoints cuts into thousands of sub-batches, so the
+    leg times a bounded sample: consecutive prefixes of the first batch
+    (1,000 lines, then doubling), each applied as a batch, until the budget
+    of device time is spent; then one more prefix in exact-MIS mode, after
+    which the membership is checked for independence and maximality on the
+    whole graph."""
+    import torch
+    from misfit_gb300 import native
+    from misfit_gb300 import workloads as W
+    import tempfile
+    dev = "cuda:%d" % local
+    out = {"workload": "R-MAT scale %d, %d samples/vertex, abcd .57/.19/.19/.05, seed %d; batches of %d toggles, "
+                       "50/50, endpoints proportional to degree" % (args.large_scale, args.large_edge_factor,
+                                                                     args.seed, args.large_batch)}
+    t = time.perf_counter()
+    n, (nindex, nlist) = W.rmat_graph_torch(args.large_scale, args.large_edge_factor, args.seed, device=dev)
+    torch.cuda.empty_cache()
+    out["generate_s"] = time.perf_counter() - t
+    out["vertices"] = int(n)
+    out["directed_entries"] = int(nlist.size)
+    out["beyond_2_31"] = bool(nlist.size > 0x7FFFFFFF)
+    folder = args.large_dir or tempfile.gettempdir()
+    path = os.path.join(folder, "misfit_rmat%d_%d.egr" % (args.large_scale, os.getpid()))
+    g = None
+    try:
+        t = time.perf_counter()
+        W.write_egr(path, n, nindex, nlist)
+        out["write_s"] = time.perf_counter() - t
+        out["file_bytes"] = os.path.getsize(path)
+        with open(path, "rb") as f:
+            out["layout"] = "int64-sentinel" if struct_unpack_second_int(f.read(8)) == -1 else "int32"
+        t = time.perf_counter()
+        g = native.Graph.open_egr(path, gpu=local)
+        out["ingest_s"] = time.perf_counter() - t
+        out["ingest_gbs"] = out["file_bytes"] / out["ingest_s"] / 1e9
+        t = time.perf_counter()
+        mis0 = g.greedy_mis()
+        g.set_mis(mis0)
+        out["greedy_seed_s"] = time.perf_counter() - t
+
+        def adjacent(a, b):
+            f = g.flag_updates(a.to(torch.int32).cpu().numpy(), b.to(torch.int32).cpu().numpy())
+            return torch.from_numpy(f == 0).to(a.device)
+
+        toggles = W.DeviceToggles(nindex, nlist, args.seed + 1, device=dev, adjacent=adjacent)
+        del nlist
+        u, v, ins = toggles.next_batch(args.large_batch, endpoints="preferential")
+        del toggles
+        torch.cuda.empty_cache()
+        g.profile(2)
+        g.profile_reset()
+        done, dev_ms, sub, chunk, samples = 0, 0.0, 0, 1000, []
+        while done < u.size and dev_ms < args.large_seconds * 1e3:
+            k = min(chunk, u.size - done)
+            g.apply_batch(u[done:done + k], v[done:done + k], ins[done:done + k])
+            st = g.stats()
+            dev_ms += st["device_ms"]
+            sub += st["sub_batches"]
+            samples.append({"lines": k, "device_ms": round(st["device_ms"], 3), "sub_batches": st["sub_batches"]})
+            done += k
+            chunk *= 2
+        prof = g.profile_read()
+        g.profile(False)
+        rate = done / (dev_ms / 1e3)
+        out.update({"value": rate, "unit": UNIT, "lines_timed": done, "device_ms": dev_ms,
+                    "sub_batches": sub, "sub_batches_per_line": sub / max(done, 1), "samples": samples,
+                    "projected_s_per_batch": args.large_batch / rate,
+                    "timing": "library CUDA events per applied prefix (host-buffer batches)"})
+        ms, calls, nbytes = prof["push_hop"]
+        peak, peak_kind = measured_peaks()
+        if ms > 0:
+            ach = nbytes / (ms / 1e3) / 1e9
+            out["roofline"] = {"bound": "hbm", "kernel": "k_lb_push_hop", "achieved": ach, "peak": peak,
+                               "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind, "launches": int(calls)}
+        # exact-MIS mode on one more prefix, then the checks on the whole graph
+        k = min(max(1000, done // 4), u.size - done)
+        if k > 0:
+            g.set_exact(True)
+            g.apply_batch(u[done:done + k], v[done:done + k], ins[done:done + k])
+            viol, unc = g.check_mis()
+            g.set_exact(False)
+            out["exact_check"] = {"lines": int(k), "device_ms": g.stats()["device_ms"],
+                                  "violations": int(viol), "uncovered": int(unc)}
+    finally:
+        if g is not None:
+            g.close()
+        if os.path.exists(path):
+            os.remove(path)
+    return out
+
+
+def struct_unpack_second_int(head):
+    import struct
+    return struct.unpack("<ii", head)[1]
+
+
 # ---- served and batched forms (many graphs on one GPU) ------------------------------
 
-def graph_set(count, nmin, nmax, seed):
+def graph_set(count, nmin, nmax, seed, device="cuda"):
     """2-D random geometric graphs with log-uniform vertex counts in [nmin,
-    nmax] and mean degree uniform in 4..32, one seed per graph."""
+    nmax] and mean degree uniform in 4..32, one seed per graph, built on the
+    GPU (workloads.rgg_graph_torch)."""
     from misfit_gb300 import workloads as W
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
         n = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
-        nindex, nlist = W.rgg_graph(n, float(rng.uniform(4, 32)), seed * 1000 + k)
+        nindex, nlist = W.rgg_graph_torch(n, float(rng.uniform(4, 32)), seed * 1000 + k, device=device)
         out.append((n, nindex, nlist))
     return out
 
@@ -328,61 +473,165 @@ def pooled(graphs, mis0, reqs, workers, budget_frac, batching=None):
     return updates / span, lat, out, st
 
 
-def run_served(args, graphs, mis0, batching=None):
-    """Serving form at reduced scale: graphs drawn as in the batched form,
-    requests arriving as a Poisson stream, each one batch of log-uniform
-    10..20,000 toggles to a graph chosen Zipf(1.1), endpoints uniform,
-    preferential or low-degree (1/3 each).  Compared with the plain
-    sequential loop on the same requests."""
+SIZE_BUCKETS = ((10, 100), (101, 1000), (1001, 10000), (10001, 20000))
+
+
+def latency_summary(lat, sizes):
+    lat = np.asarray(lat, dtype=np.float64)
+    sizes = np.asarray(sizes)
+    out = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "by_size": {}}
+    for lo, hi in SIZE_BUCKETS:
+        sel = (sizes >= lo) & (sizes <= hi)
+        if sel.any():
+            out["by_size"]["%d-%d" % (lo, hi)] = {"requests": int(sel.sum()),
+                                                 "p50_ms": float(np.percentile(lat[sel], 50)),
+                                                 "p99_ms": float(np.percentile(lat[sel], 99))}
+    return out
+
+
+def run_served(args, graphs, mis0, batching, device):
+    """Serving form: resident graphs drawn as in the batched form; for each
+    Poisson arrival rate of the sweep, `served_requests` requests, each one
+    batch of log-uniform 10..20,000 toggles to a graph chosen Zipf(1.1),
+    endpoints uniform, preferential or low-degree (1/3 each), drawn on the
+    GPU against the graph's base CSR.  The rates run one after another on
+    the same graphs, in the pool (worker threads, HBM budget 60% of the
+    graphs' footprint, so graphs are evicted to pinned host memory and
+    restored), in the pool with continuous batching of the small requests,
+    and in the plain sequential loop (one dedicated context per graph, each
+    request applied at its arrival or when the previous one ends).  Latency
+    is arrival to completion; every graph's final membership must be the
+    same in all three."""
+    from misfit_gb300 import native
     from misfit_gb300 import workloads as W
+    rates = [float(x) for x in args.served_rates.split(",")]
     rng = np.random.default_rng(11)
-    streams = [W.ToggleStream(n, ni, nl, 500 + k) for k, (n, ni, nl) in enumerate(graphs)]
     zipf = np.arange(1, len(graphs) + 1, dtype=np.float64) ** -1.1
     zipf /= zipf.sum()
     modes = ["uniform", "preferential", "low_degree"]
-    reqs, t = [], 0.0
-    for _ in range(args.served_requests):
-        t += float(rng.exponential(1.0 / args.served_rate))
-        gid = int(rng.choice(len(graphs), p=zipf))
-        size = int(round(np.exp(rng.uniform(np.log(10), np.log(20000)))))
-        u, v, ins = streams[gid].next_batch(size, endpoints=modes[int(rng.integers(3))], with_flags=True)
-        reqs.append((t, gid, u, v, ins))
-    p_rate, p_lat, p_mis = plain_loop(graphs, mis0, reqs)
-    s_rate, s_lat, s_mis, st = pooled(graphs, mis0, reqs, args.served_workers, args.served_budget)
-    same = all(np.array_equal(a, b) for a, b in zip(p_mis, s_mis))
-    cb = None
-    if batching is not None:
-        # serving is latency-bound: the dispatcher takes only the small
-        # requests (one CTA each finishes in a few ms), the workers the rest
-        from misfit_gb300 import native
-        lat_opts = native.batched_opts(block=batching.block, ctas_per_sm=batching.ctas_per_sm,
-                                       max_cta_updates=min(int(args.served_cta_limit), batching.max_cta_updates))
-        c_rate, c_lat, c_mis, cst = pooled(graphs, mis0, reqs, args.served_workers, args.served_budget, lat_opts)
-        cb = {"value": c_rate, "unit": UNIT, "p50_ms": float(np.percentile(c_lat, 50)),
-              "p99_ms": float(np.percentile(c_lat, 99)), "steps": cst["batched_steps"],
-              "requests_in_steps": cst["batched_requests"], "evictions": cst["evictions"],
-              "restores": cst["restores"],
-              "settings": {k: getattr(lat_opts, k) for k, _ in lat_opts._fields_},
-              "identical_to_plain_loop": bool(all(np.array_equal(a, b) for a, b in zip(p_mis, c_mis)))}
+    plan = []
+    for ri, rate in enumerate(rates):
+        t = 0.0
+        for _ in range(args.served_requests):
+            t += float(rng.exponential(1.0 / rate))
+            gid = int(rng.choice(len(graphs), p=zipf))
+            size = int(round(np.exp(rng.uniform(np.log(10), np.log(20000)))))
+            plan.append((ri, t, gid, size, modes[int(rng.integers(3))]))
+    t0 = time.perf_counter()
+    by_gid = {}
+    for idx, r in enumerate(plan):
+        by_gid.setdefault(r[2], []).append(idx)
+    batch_of = [None] * len(plan)
+    for gid, idxs in by_gid.items():
+        n, ni, nl = graphs[gid]
+        dt = W.DeviceToggles(ni, nl, 500 + gid, device=device)
+        for idx in idxs:
+            batch_of[idx] = dt.next_batch(plan[idx][3], endpoints=plan[idx][4])
+        del dt
+    gen_s = time.perf_counter() - t0
+    per_rate = [[(plan[i][1], plan[i][2]) + batch_of[i] for i in range(len(plan)) if plan[i][0] == ri]
+                for ri in range(len(rates))]
+
+    p_res = plain_sweep(graphs, mis0, per_rate)
+    s_res = pool_sweep(graphs, mis0, per_rate, args.served_workers, args.served_budget)
+    lat_opts = native.batched_opts(block=batching.block, ctas_per_sm=batching.ctas_per_sm,
+                                   max_cta_updates=min(int(args.served_cta_limit), batching.max_cta_updates))
+    c_res = pool_sweep(graphs, mis0, per_rate, args.served_workers, args.served_budget, lat_opts)
+    same = all(np.array_equal(a, b) for a, b in zip(p_res["mis"], s_res["mis"]))
+    same_c = all(np.array_equal(a, b) for a, b in zip(p_res["mis"], c_res["mis"]))
+    sweep = []
+    for ri, rate in enumerate(rates):
+        sizes = [int(r[2].size) for r in per_rate[ri]]
+        updates = int(sum(sizes))
+        sweep.append({
+            "rate_per_s": rate, "requests": len(sizes), "updates": updates,
+            "pool": {"value": updates / s_res["span"][ri], "unit": UNIT,
+                     **latency_summary(s_res["lat"][ri], sizes)},
+            "pool_continuous_batching": {"value": updates / c_res["span"][ri], "unit": UNIT,
+                                         **latency_summary(c_res["lat"][ri], sizes)},
+            "plain_loop": {"value": updates / p_res["span"][ri], "unit": UNIT,
+                           **latency_summary(p_res["lat"][ri], sizes)},
+            "pool_vs_plain": (updates / s_res["span"][ri]) / (updates / p_res["span"][ri]),
+        })
+    st = s_res["stats"]
     return {
-        "workload": "%d RGGs (n log-uniform 1e3..%.0e, mean degree 4..32); %d requests, Poisson %.0f/s, "
-                    "batches log-uniform 10..20000 toggles, graph Zipf(1.1), endpoints uniform/preferential/"
-                    "low-degree" % (len(graphs), args.graphs_nmax, len(reqs), args.served_rate),
-        "value": s_rate, "unit": UNIT, "p50_ms": float(np.percentile(s_lat, 50)),
-        "p99_ms": float(np.percentile(s_lat, 99)), "workers": args.served_workers,
-        "hbm_budget_fraction": args.served_budget, "evictions": st["evictions"], "restores": st["restores"],
-        "scratch_trims": st["trims"], "over_budget_admissions": st["over_budget"],
+        "workload": "%d RGGs (n log-uniform 1e3..%.0e, mean degree 4..32, built on the GPU); per rate %d "
+                    "requests, Poisson arrivals, batches log-uniform 10..20000 toggles, graph Zipf(1.1), endpoints "
+                    "uniform/preferential/low-degree" % (len(graphs), args.graphs_nmax, args.served_requests),
+        "sweep": sweep, "value": sweep[0]["pool"]["value"], "unit": UNIT,
+        "p50_ms": sweep[0]["pool"]["p50_ms"], "p99_ms": sweep[0]["pool"]["p99_ms"],
+        "p99_target_ms": 5.0, "workers": args.served_workers, "hbm_budget_fraction": args.served_budget,
         "footprint_bytes": st["footprint_bytes"], "peak_resident_bytes": st["peak_resident_bytes"],
-        "plain_loop": {"value": p_rate, "unit": UNIT, "p50_ms": float(np.percentile(p_lat, 50)),
-                       "p99_ms": float(np.percentile(p_lat, 99))},
-        "identical_to_plain_loop": bool(same), "timing": "host wall clock, host buffers in and out",
-        "continuous_batching": cb,
+        "evictions": st["evictions"], "restores": st["restores"], "scratch_trims": st["trims"],
+        "continuous_batching": {"steps": c_res["stats"]["batched_steps"],
+                                "requests_in_steps": c_res["stats"]["batched_requests"],
+                                "settings": {k: getattr(lat_opts, k) for k, _ in lat_opts._fields_}},
+        "identical_to_plain_loop": bool(same), "continuous_batching_identical_to_plain_loop": bool(same_c),
+        "request_generation_s": gen_s,
+        "timing": "host wall clock from each request's arrival to its completion; host buffers in",
     }
 
 
-def run_batched(args, graphs, mis0):
-    """Batched form at reduced scale: independent graphs, one batch each
-    (log-uniform 10..50,000 toggles, low-degree and uniform endpoints 50/50),
+def plain_sweep(graphs, mis0, per_rate):
+    """The plain sequential loop over the rates' requests (dedicated contexts,
+    state carried from rate to rate)."""
+    from misfit_gb300 import native
+    ctxs = []
+    for (n, nindex, nlist), m in zip(graphs, mis0):
+        g = native.Graph.from_csr(nindex, nlist)
+        g.set_mis(m)
+        ctxs.append(g)
+    lats, spans = [], []
+    for reqs in per_rate:
+        lat = []
+        t0 = time.perf_counter()
+        for t, gid, u, v, ins in reqs:
+            wait = t - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            ctxs[gid].apply_batch(u, v, ins)
+            lat.append((time.perf_counter() - t0 - t) * 1e3)
+        spans.append(time.perf_counter() - t0)
+        lats.append(lat)
+    out = [c.get_mis() for c in ctxs]
+    for c in ctxs:
+        c.close()
+    return {"lat": lats, "span": spans, "mis": out}
+
+
+def pool_sweep(graphs, mis0, per_rate, workers, budget_frac, batching=None):
+    """The same requests through one serving pool, rate after rate."""
+    from misfit_gb300 import native
+    pool = native.Pool(1 << 40, workers=workers)
+    if batching is not None:
+        pool.set_batching(batching)
+    gids = [pool.add_graph(nindex, nlist, m) for (n, nindex, nlist), m in zip(graphs, mis0)]
+    footprint = pool.stats()["resident_bytes"]
+    pool.set_budget(max(1, int(footprint * budget_frac)))
+    lats, spans = [], []
+    for reqs in per_rate:
+        rids = []
+        t0 = time.perf_counter()
+        for t, gid, u, v, ins in reqs:
+            wait = t - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            rids.append(pool.submit(gids[gid], u, v, ins))
+        lat = [pool.wait(r) for r in rids]
+        spans.append(time.perf_counter() - t0)
+        lats.append(lat)
+    out = [pool.get_mis(g) for g in gids]
+    st = pool.stats()
+    st["footprint_bytes"] = footprint
+    pool.close()
+    return {"lat": lats, "span": spans, "mis": out, "stats": st}
+
+
+def run_batched(args, graphs, mis0, device):
+    """Batched form: independent graphs, one batch each (log-uniform
+    10..50,000 toggles, low-degree and uniform endpoints 50/50, drawn on the
+    GPU against each graph's base CSR),
     all applied in one mf_apply_batches step -- the batches one CTA can carry
     in one persistent kernel driven by a device work queue and launched as a
     CUDA graph, the rest through the multi-launch path meanwhile -- with the
@@ -394,10 +643,9 @@ def run_batched(args, graphs, mis0):
     rng = np.random.default_rng(12)
     reqs = []
     for k, (n, ni, nl) in enumerate(graphs):
-        ts = W.ToggleStream(n, ni, nl, 900 + k)
         size = int(round(np.exp(rng.uniform(np.log(10), np.log(50000)))))
         mode = "low_degree" if k % 2 == 0 else "uniform"
-        u, v, ins = ts.next_batch(size, endpoints=mode, with_flags=True)
+        u, v, ins = W.DeviceToggles(ni, nl, 900 + k, device=device).next_batch(size, endpoints=mode)
         reqs.append((0.0, k, u, v, ins))
     batches = [(u, v, ins) for _, _, u, v, ins in reqs]
     updates = sum(int(b[0].size) for b in batches)
@@ -451,31 +699,34 @@ def main():
     torch.cuda.set_device(local)
     from misfit_gb300 import build, native
     build.build()
+    dev = "cuda:%d" % local
     if args.profile_step:
         from misfit_gb300 import autotune
         from misfit_gb300 import workloads as W
-        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
+        graphs = graph_set(args.batched_graphs, 1000, args.graphs_nmax, 12, dev)
         mis0 = initial_mis(graphs)
         rng = np.random.default_rng(12)
         batches = []
         for k, (n, ni, nl) in enumerate(graphs):
             size = min(8192, int(round(np.exp(rng.uniform(np.log(10), np.log(50000))))))
-            u, v, ins = W.ToggleStream(n, ni, nl, 900 + k).next_batch(size, with_flags=True)
-            batches.append((u, v, ins))
+            batches.append(W.DeviceToggles(ni, nl, 900 + k, device=dev).next_batch(size))
         opts = native.batched_opts(max_cta_updates=1 << 20, use_graph=0)
         sec, _, st = autotune.run_step(graphs, mis0, batches, opts)
         print(json.dumps({"graphs": len(graphs), "updates": int(sum(b[0].size for b in batches)),
                           "step_ms": sec * 1e3, **st}))
         return
     if args.served_only:
-        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
-        print(json.dumps(run_served(args, graphs, initial_mis(graphs), native.batched_opts())))
+        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11, dev)
+        print(json.dumps(run_served(args, graphs, initial_mis(graphs), native.batched_opts(), dev)))
         return
     if args.batched_only:
-        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
-        res, _ = run_batched(args, graphs, initial_mis(graphs))
+        graphs = graph_set(args.batched_graphs, 1000, args.graphs_nmax, 12, dev)
+        res, _ = run_batched(args, graphs, initial_mis(graphs), dev)
         res["gpu_launches_total"] = int(native.load_library().mf_kernel_launches())
         print(json.dumps(res))
+        return
+    if args.large_only:
+        print(json.dumps(run_large(args, local)))
         return
     n, nindex, nlist, stream = make_workload(args, "cuda:%d" % local)
     g = native.Graph.from_csr(nindex, nlist, gpu=local)
@@ -483,13 +734,13 @@ def main():
     # warm-up, timed, e2e, one untimed batch with every stage timed, then the
     # exact-MIS leg (one warm-up and `steps` timed batches)
     exact_steps = 0 if args.no_exact else 1 + args.steps
-    total = args.warmup + args.steps + (0 if args.no_e2e else args.steps) + 1 + exact_steps
+    total = args.warmup + args.steps + (0 if args.no_e2e else args.steps) + 2 + exact_steps
     batches = [stream.next_batch(args.batch) for _ in range(total)]
     flags = [g.flag_updates(u, v) for u, v in batches]  # against the base graph, before any batch
 
-    dev = []
+    dev_inputs = []
     for (u, v), ins in zip(batches[: args.warmup + args.steps], flags):
-        dev.append((torch.from_numpy(u).cuda(), torch.from_numpy(v).cuda(), torch.from_numpy(ins).cuda()))
+        dev_inputs.append((torch.from_numpy(u).cuda(), torch.from_numpy(v).cuda(), torch.from_numpy(ins).cuda()))
     torch.cuda.synchronize()
 
     def dist_barrier():
@@ -502,7 +753,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     for i in range(args.warmup):
-        du, dv, di = dev[i]
+        du, dv, di = dev_inputs[i]
         g.apply_batch_device(du.data_ptr(), dv.data_ptr(), di.data_ptr(), du.numel())
 
     # ---- timed: inputs resident in HBM
@@ -516,7 +767,7 @@ def main():
     t0 = time.perf_counter()
     lat = []
     for i in range(args.warmup, args.warmup + args.steps):
-        du, dv, di = dev[i]
+        du, dv, di = dev_inputs[i]
         g.apply_batch_device(du.data_ptr(), dv.data_ptr(), di.data_ptr(), du.numel())
         lat.append(g.stats()["device_ms"])
     torch.cuda.synchronize()
@@ -559,6 +810,16 @@ def main():
     g.profile(False)
     nxt += 1
 
+    # ---- algorithmic bytes of one batch (the per-batch roofline): one more
+    # untimed batch with the library's accounting on (every sub-batch then
+    # computes its exact packed size; results are unchanged)
+    g.profile(4)
+    u, v = batches[nxt]
+    g.apply_batch(u, v, flags[nxt])
+    acct = g.stats()
+    g.profile(False)
+    nxt += 1
+
     # ---- exact-MIS mode on the same context: the fix-up after every batch
     exact = None
     if exact_steps:
@@ -594,6 +855,28 @@ def main():
             "traffic_note": "DRAM bytes per pushed element from an ncu capture of the R-MAT scale-20 case, "
                             "times this workload's elements per launch"}
 
+    # per-batch roofline: the algorithmic bytes of a whole batch, summed over
+    # the reference's sub-batches, against the timed batches' mean time:
+    #   B = sum_SB [ 32*|E_SB| + sum_{r in S u H} (2*w_idx + 4*deg(r)) + 8*A_SB + 8*rows_SB ]
+    # (edge record in + overlay write; each mapped row's offsets and entries
+    # read once; state read + cluster-id write per packed element; final state
+    # read + write per mapped row), w_idx = 4 for the int32 .egr layout
+    rows = int(acct["seeds"] + acct["candidates"])
+    w_idx = 4
+    bbytes = (32.0 * args.batch + (2 * w_idx + 8) * rows + 4.0 * acct["row_degree_total"]
+              + 8.0 * acct["packed_total"])
+    batch_ms = dev_ms / args.steps
+    roof["batch"] = {
+        "bytes": bbytes, "packed_total": int(acct["packed_total"]), "rows": rows,
+        "row_degree_total": int(acct["row_degree_total"]), "sub_batches": int(acct["sub_batches"]),
+        "batch_ms": batch_ms, "achieved": bbytes / (batch_ms / 1e3) / 1e9,
+        "frac": bbytes / (batch_ms / 1e3) / 1e9 / peak,
+        "formula": "B = 32*|E| + (2*w_idx + 8)*rows + 4*sum deg(rows) + 8*packed, w_idx 4; counted on one "
+                   "untimed batch of the same stream (library accounting), timed against the timed batches' "
+                   "mean device time",
+    }
+    roof["batch_frac"] = roof["batch"]["frac"]
+
     line = {
         "metric": METRIC, "value_is": VALUE_IS, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -620,11 +903,39 @@ def main():
         except Exception as e:  # a baseline must not cost the line
             line["cpu_greedy_recompute"] = {"error": str(e)}
     g.close()
+    del dev_inputs
+    torch.cuda.empty_cache()
+    # the configuration legs; a leg that fails records its error instead of
+    # costing the line
+    def leg(name, fn):
+        t = time.perf_counter()
+        try:
+            res = fn()
+        except Exception as e:  # noqa: BLE001
+            import traceback
+            res = {"error": "%s: %s" % (type(e).__name__, e), "trace": traceback.format_exc()[-1500:]}
+        if isinstance(res, dict):
+            res["leg_wall_s"] = time.perf_counter() - t
+        line[name] = res
+        torch.cuda.empty_cache()
+        return res
+
+    if rank == 0 and not args.no_large:
+        leg("large_int64", lambda: run_large(args, local))
     if rank == 0 and not args.no_served:
-        graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11)
-        mis0 = initial_mis(graphs)
-        line["batched"], tuned = run_batched(args, graphs, mis0)
-        line["served"] = run_served(args, graphs, mis0, tuned)
+        tuned_box = {}
+
+        def batched_leg():
+            graphs = graph_set(args.batched_graphs, 1000, args.graphs_nmax, 12, dev)
+            res, tuned_box["opts"] = run_batched(args, graphs, initial_mis(graphs), dev)
+            return res
+
+        def served_leg():
+            graphs = graph_set(args.served_graphs, 1000, args.graphs_nmax, 11, dev)
+            return run_served(args, graphs, initial_mis(graphs), tuned_box.get("opts") or native.batched_opts(), dev)
+
+        leg("batched", batched_leg)
+        leg("served", served_leg)
     if rank == 0:
         print(json.dumps(line), flush=True)
     dist_barrier()

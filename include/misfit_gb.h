@@ -57,6 +57,12 @@ typedef struct mf_batch_stats {
   int64_t max_csr;          /* MAX_CSR_ELEMENTS after the batch */
   int64_t repair_rounds;    /* speculative repair rounds, summed */
   double device_ms;         /* device time of the batch (CUDA events) */
+  /* With profiler bit 4 (mf_profile_enable): the exact packed volume of the
+   * batch, summed over sub-batches (every seed's 2-hop list length plus every
+   * candidate row's length, the elements the reference packs), and the sum
+   * of the degrees of the mapped rows.  -1 otherwise. */
+  int64_t packed_total;
+  int64_t row_degree_total;
 } mf_batch_stats;
 
 /* ---- lifetime -------------------------------------------------------- */
@@ -173,6 +179,24 @@ int mf_sync(mf_ctx* ctx);
 
 int mf_last_batch_stats(mf_ctx* ctx, mf_batch_stats* out);
 
+/* Load-balancing settings of one context.  They decide how the work of a
+ * sub-batch is spread over kernels and threads, never what it computes:
+ * every setting gives the same results (misfit_gb300/autotune.py searches
+ * them).  No reference counterpart (the reference's kernels have none).  */
+typedef struct mf_tuning {
+  int64_t pull_long;      /* rows longer than this take the warp-per-row pass of the
+                             candidates' cluster-id pull instead of one thread (default 2048) */
+  int64_t heavy_min;      /* least row length of a heavy vertex, whose neighbourhood bitmap the
+                             exact 2-hop sizes cache (default 2048; the threshold used is
+                             max(heavy_min, n/256)) */
+  int64_t big_threshold;  /* hop-2 volume above which the insertion rule's search for the first
+                             eligible vertex goes to the grid-wide kernel (default 256) */
+  int64_t first_bound;    /* row positions the warp level of the first-cluster-id search covers
+                             before long rows go to the chunk level (default 256, at least 8) */
+} mf_tuning;
+int mf_get_tuning(mf_ctx* ctx, mf_tuning* out);
+int mf_set_tuning(mf_ctx* ctx, const mf_tuning* in);
+
 /* ---- graph queries ----------------------------------------------------- */
 
 /* Row of x in overlay order (base minus tombstones, then added neighbours in
@@ -240,7 +264,11 @@ const char* mf_stage_name(int stage);
 /* on = 1: every later batch records CUDA events around each stage on the
  * context's stream; times accumulate until mf_profile_reset.  on = 2: only
  * the k_lb_push_hop launches are timed (the "push_hop" stage), which costs
- * four event records per sub-batch instead of about fifty.  on = 0: off. */
+ * four event records per sub-batch instead of about fifty.  on = 0: off.
+ * Adding 4 (on = 4, 5, 6) also counts each batch's algorithmic work
+ * (mf_batch_stats.packed_total / row_degree_total): every sub-batch then
+ * computes its exact 2-hop sizes, which costs device time, so a batch timed
+ * for throughput should run without it.  Results are unchanged. */
 int mf_profile_enable(mf_ctx* ctx, int on);
 int mf_profile_reset(mf_ctx* ctx);
 /* Accumulated device milliseconds, occurrences and algorithmic bytes per

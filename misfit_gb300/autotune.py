@@ -13,6 +13,14 @@ schedule of independent graphs, never a result); a disagreement raises.
 Results are cached in a JSON file keyed by the GPU name and a shape bucket
 of the workload (graph count, log2 of the median vertex count and of the
 median batch size), so later runs with a similar mix skip the search.
+
+tune_plain does the same for the per-batch path (mf_apply_batch): its four
+load-balancing thresholds (mf_tuning: the candidate pull's long-row cut,
+the heavy-vertex row length of the exact sizes, the hop-2 volume that
+defers the insertion rule's search to the grid-wide kernel, and the warp
+level of the first-cluster-id search) are searched one after another on
+the caller's batches, each candidate on a fresh context, every candidate
+required to give the same memberships.
 """
 import json
 import os
@@ -119,3 +127,65 @@ def tune_batched(graphs, mis0, batches, use_cache=True):
         except OSError:
             pass
     return native.batched_opts(**chosen), {"cached": False, "key": key, **entry}
+
+
+# The library's defaults of mf_tuning (a GPU test checks that a new context
+# reports these), and the candidate values, searched one at a time.
+DEFAULT_TUNING = {"pull_long": 2048, "heavy_min": 2048, "big_threshold": 256, "first_bound": 256}
+PLAIN_KNOBS = (
+    ("big_threshold", (64, 256, 1024, 4096)),
+    ("first_bound", (64, 256, 1024)),
+    ("pull_long", (512, 2048, 8192)),
+    ("heavy_min", (1024, 2048, 8192)),
+)
+
+
+def run_plain(nindex, nlist, mis0, batches, tuning):
+    """A fresh context with `tuning`, the batches applied in order.  Returns
+    (device seconds summed over the batches, final membership)."""
+    g = native.Graph.from_csr(nindex, nlist)
+    try:
+        g.set_tuning(**tuning)
+        g.set_mis(mis0)
+        ms = 0.0
+        for u, v, ins in batches:
+            g.apply_batch(u, v, ins)
+            ms += g.stats()["device_ms"]
+        return ms / 1e3, g.get_mis()
+    finally:
+        g.close()
+
+
+def tune_plain(nindex, nlist, mis0, batches, use_cache=True):
+    """Coordinate search of the per-batch path's thresholds on `batches`
+    (a list of (u, v, ins)).  Returns (tuning dict, report)."""
+    path = cache_path()
+    key = "plain|%s|n2^%d|m2^%d" % (_gpu_name(), int(np.log2(max(1, np.asarray(nindex).size - 1))),
+                                    int(np.log2(max(1, np.median([np.asarray(b[0]).size for b in batches])))))
+    cache = _load(path) if use_cache else {}
+    if key in cache:
+        return dict(cache[key]["tuning"]), {"cached": True, "key": key, **cache[key]}
+    best = dict(DEFAULT_TUNING)
+    trials = []
+    ref = None
+    run_plain(nindex, nlist, mis0, batches[:1], best)   # warm-up
+    for name, values in PLAIN_KNOBS:
+        scores = {}
+        for val in values:
+            cand = dict(best, **{name: val})
+            sec, mis = run_plain(nindex, nlist, mis0, batches, cand)
+            if ref is None:
+                ref = mis
+            elif not np.array_equal(ref, mis):
+                raise RuntimeError("per-batch results differ between settings %s" % cand)
+            trials.append({"tuning": cand, "seconds": sec})
+            scores[val] = sec
+        best[name] = min(scores, key=scores.get)
+    entry = {"tuning": best, "trials": trials}
+    if use_cache:
+        cache[key] = entry
+        try:
+            _store(path, cache)
+        except OSError:
+            pass
+    return dict(best), {"cached": False, "key": key, **entry}

@@ -161,6 +161,7 @@ mf_ctx* new_ctx(int gpu) {
   c->device = gpu;
   try {
     mf::noalloc_refresh(gpu);
+    if (const char* e = std::getenv("MISFIT_GB_BIG_THRESHOLD")) c->tune.big_threshold = std::max<long long>(0, std::atoll(e));
     MF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     mf::g_alloc_stream = c->stream;
     // keep freed stream-ordered memory in this process's pool for reuse
@@ -201,6 +202,8 @@ void run_batch(mf_ctx* c, int64_t m) {
   cudaStream_t s = c->stream;
   c->stats = mf_batch_stats{};
   c->stats.updates = m;
+  c->stats.packed_total = -1;
+  c->stats.row_degree_total = -1;
   c->traces.clear();
   c->work.reserve(2 * mf::kStCount + 8);
   c->touched_total = 0;
@@ -755,6 +758,25 @@ int mf_sync(mf_ctx* c) {
   return st;
 }
 
+int mf_get_tuning(mf_ctx* c, mf_tuning* out) {
+  return guarded([&] {
+    need(c && out, MF_EINVAL, "null argument");
+    *out = c->tune;
+  });
+}
+
+int mf_set_tuning(mf_ctx* c, const mf_tuning* in) {
+  return guarded([&] {
+    need(c && in, MF_EINVAL, "null argument");
+    need(in->pull_long >= 32 && in->heavy_min >= 64 && in->big_threshold >= 0 && in->first_bound >= 8 &&
+             in->first_bound <= ((int64_t)1 << 20),
+         MF_EINVAL, "tuning out of range (pull_long >= 32, heavy_min >= 64, big_threshold >= 0, "
+                    "8 <= first_bound <= 2^20)");
+    bind(c);
+    c->tune = *in;
+  });
+}
+
 int mf_last_batch_stats(mf_ctx* c, mf_batch_stats* out) {
   return guarded([&] {
     need(c && out, MF_EINVAL, "null argument");
@@ -1021,7 +1043,7 @@ const char* mf_stage_name(int stage) {
 
 int mf_profile_enable(mf_ctx* c, int on) {
   return guarded([&] {
-    need(c != nullptr && on >= 0 && on <= 2, MF_EINVAL, "bad arguments");
+    need(c != nullptr && on >= 0 && on <= 6 && (on & 3) != 3, MF_EINVAL, "bad arguments");
     c->profile = on;
   });
 }

@@ -236,6 +236,8 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
     mf_ctx* c = ctxs[i];
     if (m[i] == 0) {
       c->stats = mf_batch_stats{};
+      c->stats.packed_total = -1;
+      c->stats.row_degree_total = -1;
       c->stats.max_csr = c->max_csr;
       continue;
     }
@@ -432,6 +434,8 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
       c->max_csr = out[cta::kOutMaxCsr];
       c->cta_epoch = (uint32_t)out[cta::kOutEpoch];
       c->stats = mf_batch_stats{};
+      c->stats.packed_total = -1;
+      c->stats.row_degree_total = -1;
       c->stats.updates = m[i];
       c->stats.sub_batches = out[cta::kOutSubBatches];
       c->stats.seeds = out[cta::kOutSeeds];

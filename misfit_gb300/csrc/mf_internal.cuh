@@ -618,6 +618,9 @@ struct mf_ctx {
   // counts the ones not yet collected
   mf::AsyncQueue* aq = nullptr;
   bool pending = false;
+  // load-balancing settings (mf_set_tuning); they move work between kernels,
+  // never a result
+  mf_tuning tune = mf_tuning{2048, 2048, 256, 256};
 
   mf::GraphView view() const {
     return mf::GraphView{n, nindex.p, nlist.p, live.p, dead.p, aoff.p, aadj.p};
@@ -715,7 +718,7 @@ struct StageScope {
   size_t first = 0;
   bool on;
   StageScope(mf_ctx* ctx, int st)
-      : c(ctx), stage(st), on(ctx->profile == 1 || (ctx->profile == 2 && st == kStPushHop)) {
+      : c(ctx), stage(st), on((ctx->profile & 3) == 1 || ((ctx->profile & 3) == 2 && st == kStPushHop)) {
     if (!on) return;
     if (c->ev_used + 2 > c->ev_pool.size()) {
       for (int k = 0; k < 64; ++k) {

@@ -237,7 +237,8 @@ __global__ void __launch_bounds__(kLbThreads) k_lb_hop1_bound(GraphView g, const
   int64_t cur = -1;
   unsigned long long acc = 0;
   const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
-    atomicOr(hbits + (y >> 5), 1u << (y & 31));
+    const uint32_t bit = 1u << (y & 31);
+    if (!(hbits[y >> 5] & bit)) atomicOr(hbits + (y >> 5), bit);
     if (i != cur) {
       if (cur >= 0 && acc) atomicAdd(uacc + cur, acc);
       cur = i;
@@ -678,6 +679,25 @@ __global__ void k_cand_lens(GraphView g, const int32_t* cands, int64_t nct, int6
 // (src/misfit/misfit.cu:565-568): whenever a row's end offset reaches the
 // limit, the limit becomes 1.5x that end offset.  io[0] = limit in/out,
 // io[1] = packed total out.
+// Algorithmic accounting of one sub-batch (profiler bit 4): the packed
+// volume (sum of the exact row lengths) and the degrees of the mapped rows.
+__global__ void k_acct(const int64_t* lens, int64_t rows, const int32_t* seeds, int64_t ns, const int32_t* cands,
+                       const int32_t* deg, unsigned long long* acc) {
+  unsigned long long a = 0, d = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+    a += (unsigned long long)lens[i];
+    d += (unsigned long long)deg[i < ns ? seeds[i] : cands[i - ns]];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    d += __shfl_down_sync(0xffffffffu, d, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (a) atomicAdd(acc, a);
+    if (d) atomicAdd(acc + 1, d);
+  }
+}
+
 __global__ void k_growth(const int64_t* pex, int64_t rows, int64_t* io) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   int64_t cur = io[0];
@@ -701,12 +721,11 @@ __global__ void k_growth(const int64_t* pex, int64_t rows, int64_t* io) {
 
 // ---- first-hit row searches --------------------------------------------------------
 // First position j of row(x) (in order) whose element y satisfies a predicate,
-// for every x of a list.  A warp scans the first kFirstBound positions; rows
+// for every x of a list.  A warp scans the first `bound` positions; rows
 // still unresolved are finished by a load-balanced pass that keeps the
 // minimum hit position per row (atomicMin), so hub rows are spread over the
 // GPU while short rows stop at their first hit.
 
-constexpr int64_t kFirstBound = 256;
 constexpr unsigned long long kNoPos = ~0ull;
 
 struct HasCid {   // the element already carries a cluster id
@@ -718,7 +737,7 @@ struct HasCid {   // the element already carries a cluster id
 // Three levels, none of which needs the host to know a count:
 //   1. one thread per row probes the first kProbe positions;
 //   2. rows still open go to a queue; a fixed grid of warps scans positions
-//      kProbe .. kFirstBound of each;
+//      kProbe .. bound of each (a tuning setting, 256 by default);
 //   3. rows still open get chunks of kFirstChunk positions from one packed
 //      64-bit counter ((rows << 40) | chunks), so that the chunk bases grow
 //      with the row slots; a fixed grid of warps takes chunks, finds the row
@@ -763,9 +782,10 @@ __device__ __forceinline__ int64_t cq_slot(const ChunkQueue& q, int64_t rows, in
 
 // Warp-cooperative: first position k in [k0, k1) of row(x) (nb base
 // positions, then the added entries) whose element is live and satisfies
-// pred, or -1.  Four 32-position windows are loaded before any is tested,
-// so each lane has four element loads (then four predicate loads) in
-// flight; the answer is the first window's lowest hit.
+// pred, or -1.  Steps of one, two, then four 32-position windows: the
+// windows of a step are loaded before any is tested, so each lane has up to
+// four element loads (then four predicate loads) in flight; the answer is
+// the lowest hit of the first window that has one.
 template <class P>
 __device__ __forceinline__ int64_t warp_first_range(const GraphView& g, int32_t x, int64_t nb, int64_t k0, int64_t k1,
                                                     P pred) {
@@ -773,7 +793,8 @@ __device__ __forceinline__ int64_t warp_first_range(const GraphView& g, int32_t 
   const int64_t b0 = g.nindex[x];
   const int64_t a0 = g.aoff[x];
   const bool filt = g.dead[x] != 0;
-  for (int64_t base = k0; base < k1; base += 128) {
+  int nwin = 1;   // windows per step: 1, 2, then 4 (a hit is often early)
+  for (int64_t base = k0; base < k1; base += 32 * nwin, nwin = nwin < 4 ? 2 * nwin : 4) {
     int32_t y[4];
     bool live[4];
 #pragma unroll
@@ -781,7 +802,7 @@ __device__ __forceinline__ int64_t warp_first_range(const GraphView& g, int32_t 
       const int64_t k = base + 32 * q + lane;
       y[q] = -1;
       live[q] = false;
-      if (k < k1) {
+      if (q < nwin && k < k1) {
         if (k < nb) {
           y[q] = __ldg(g.nlist + b0 + k);
           live[q] = !filt || live_at(g.live, b0 + k);
@@ -808,6 +829,7 @@ struct FirstQueues {
   int32_t* mid_v;
   unsigned long long* mid_count;
   ChunkQueue rest;
+  int64_t bound;    // positions the warp level covers (kProbe .. bound); a tuning setting
 };
 
 template <class P>
@@ -846,12 +868,12 @@ __global__ void k_first_warp(GraphView g, P pred, unsigned long long* firstpos, 
     const int32_t x = q.mid_v[w];
     const int64_t nb = g.nindex[x + 1] - g.nindex[x];
     const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
-    const int64_t lim = np < kFirstBound ? np : kFirstBound;
+    const int64_t lim = np < q.bound ? np : q.bound;
     const int64_t hit = warp_first_range(g, x, nb, kProbe, lim, pred);
     if (hit >= 0) {
       if (lane == 0) firstpos[i] = (unsigned long long)hit;
-    } else if (np > kFirstBound && lane == 0) {
-      cq_push(q.rest, i, x, (np - kFirstBound + kFirstChunk - 1) / kFirstChunk);
+    } else if (np > q.bound && lane == 0) {
+      cq_push(q.rest, i, x, (np - q.bound + kFirstChunk - 1) / kFirstChunk);
     }
   }
 }
@@ -866,7 +888,7 @@ __global__ void k_first_chunks(GraphView g, P pred, unsigned long long* firstpos
     const int64_t slot = cq_slot(q.rest, rows, c);
     const int32_t i = q.rest.idx[slot];
     const int32_t x = q.rest.v[slot];
-    const int64_t p0 = kFirstBound + (c - q.rest.base[slot]) * kFirstChunk;
+    const int64_t p0 = q.bound + (c - q.rest.base[slot]) * kFirstChunk;
     // skip when an earlier position already hit; one lane reads, so that the
     // whole warp takes the same branch while other warps lower the value
     unsigned long long fp = 0;
@@ -986,6 +1008,16 @@ __global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid) {
   if (i < rows && rowcid[i] == -1) rowcid[i] = (int32_t)pos[i];
 }
 
+// The pushes are reductions whose results are not read back, so they issue
+// as fire-and-forget RED operations.  Within one launch a tag word only
+// grows, so a plain read that already shows the pushed tag (or a larger one)
+// proves the push cannot change it and it is skipped: rows of R-MAT
+// sub-batches share their hub neighbours, and without the filter every
+// hop-1 row's push to a hub serialises on that one address.
+__device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag) {
+  if (wval[y] < tag) atomicMax(wval + y, tag);
+}
+
 // Phase 1: bval[y] = max tag of the non-skipped seed rows with y in {s} u row(s).
 __global__ void k_seed_self(const int32_t* seeds, int64_t ns, const int32_t* rowcid, uint32_t epoch, uint32_t* bval) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -995,14 +1027,12 @@ __global__ void k_seed_self(const int32_t* seeds, int64_t ns, const int32_t* row
 __global__ void k_lb_push_seed(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t epoch,
                                uint32_t* bval, unsigned long long* work) {
   const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
-    atomicMax(bval + y, (epoch << kRowBits) | (uint32_t)i);
+    push_w(bval, y, (epoch << kRowBits) | (uint32_t)i);
   });
   add_work(work, vis);
 }
 
-// The pushes are reductions whose results are not read back, so they issue
-// as fire-and-forget RED operations.
-__device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag) { atomicMax(wval + y, tag); }
+
 
 // Phase 2: wval[y] = max over x with y in {x} u row(x) of bval[x] (the 2-hop
 // reach of the seed rows), and the candidate rows' own tags over row(c).
@@ -1039,9 +1069,9 @@ __global__ void k_lb_push_cand(GraphView g, const int32_t* cands, const int64_t*
 // candidate neighbour: the added part of row(y) is scanned, then the base
 // part from its end until the first such neighbour.  That tag dominates every
 // seed-row tag; without one, the pushed seed-row tag (wval) decides.
-// One thread per vertex; rows longer than kPullLong positions go to a list
-// that k_pull_cand_long finishes with one warp per row.
-constexpr int64_t kPullLong = 2048;
+// One thread per vertex; rows longer than a.pull_long positions (a tuning
+// setting, 2048 by default) go to a list that k_pull_cand_long finishes with
+// one warp per row.
 
 struct PullArgs {
   GraphView g;
@@ -1055,6 +1085,7 @@ struct PullArgs {
   int32_t* longv;                 // rows left for the warp pass
   unsigned long long* nlong;
   unsigned long long* work;
+  int64_t pull_long;              // rows longer than this go to the warp pass
 };
 
 __device__ __forceinline__ bool pull_nonskip(const PullArgs& a, int32_t c) {
@@ -1086,7 +1117,7 @@ __global__ void k_pull_cand(PullArgs a) {
     const int32_t y = (int32_t)yi;
     const int64_t b = g.nindex[y], e = g.nindex[y + 1];
     const int64_t ab = g.aoff[y], ae = g.aoff[y + 1];
-    if ((e - b) + (ae - ab) > kPullLong) {
+    if ((e - b) + (ae - ab) > a.pull_long) {
       a.longv[atomicAdd(a.nlong, 1ull)] = y;
     } else {
       int32_t best = -1;
@@ -1409,7 +1440,6 @@ __global__ void __launch_bounds__(1024) k_repair_sequential(RepairArgs a) {
 // the sequential kernel.
 
 constexpr int kMaxRounds = 48;
-constexpr int64_t kBigThreshold = 256;    // hop-2 volume above which the grid-wide search runs
 
 struct View {
   const uint8_t* m;     // bit 0: committed membership; bit 1: pending writes exist
@@ -2215,7 +2245,7 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
     MF_CUDA(cudaMemsetAsync(c->heavy_slot.p, 0xFF, sizeof(int32_t) * (size_t)std::max<int32_t>(n, 1), s));
     c->heavy_used = 0;
   }
-  const int64_t thr = std::max<int64_t>(2048, words / 8);
+  const int64_t thr = std::max<int64_t>(c->tune.heavy_min, words / 8);
   // collect the heavy members of the seeds' closed neighbourhoods not cached yet
   h[30] = c->heavy_used;
   MF_CUDA(cudaMemcpyAsync(c->counters.p + 30, h + 30, sizeof(int64_t), cudaMemcpyHostToDevice, s));
@@ -2329,7 +2359,8 @@ void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, 
   c->rq_v.reserve(cap);
   unsigned long long* ucnt = reinterpret_cast<unsigned long long*>(c->counters.p);
   MF_CUDA(cudaMemsetAsync(ucnt + 48, 0, sizeof(unsigned long long) * 2, s));
-  const FirstQueues q{c->un_idx.p, c->un_v.p, ucnt + 48, ChunkQueue{c->rq_idx.p, c->rq_v.p, c->un_cnt.p, ucnt + 49}};
+  const FirstQueues q{c->un_idx.p, c->un_v.p, ucnt + 48, ChunkQueue{c->rq_idx.p, c->rq_v.p, c->un_cnt.p, ucnt + 49},
+                      std::max<int64_t>(c->tune.first_bound, kProbe)};
   const GraphView g = c->view();
   MF_K(k_first_probe<<<lb_grid(c, k_first_probe<P>), kTB, 0, s>>>(g, list, dcnt, pred, c->fpos.p, q));
   MF_K(k_first_warp<<<lb_grid(c, k_first_warp<P>), kTB, 0, s>>>(g, pred, c->fpos.p, q));
@@ -2358,14 +2389,6 @@ void next_epoch(mf_ctx* c) {
   ++c->epoch;
 }
 
-
-int64_t big_threshold() {
-  static const int64_t v = [] {
-    const char* e = std::getenv("MISFIT_GB_BIG_THRESHOLD");
-    return e ? std::max<int64_t>(0, std::atoll(e)) : kBigThreshold;
-  }();
-  return v;
-}
 
 bool sequential_repair_forced() {
   static const bool forced = [] {
@@ -2430,7 +2453,7 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     MF_CUDA(cudaMemsetAsync(c->counters.p + 24, 0, sizeof(int64_t) * 6, s));  // deferrals, prefix use, queue, done
     SpecArgs a{g, c->bu.p, c->bv.p, c->bins.p, p, order, p0, nproc, ns, c->v2i.p,
                View{c->mis.p, c->rp_keys.p, c->rp_vals.p, nview}, c->rp_n0.p, c->rp_n1.p,
-               big_threshold(), ucnt + 24, c->big_pos.p, c->big_r.p, c->big_off.p, c->big_nr.p,
+               c->tune.big_threshold, ucnt + 24, c->big_pos.p, c->big_r.p, c->big_off.p, c->big_nr.p,
                c->big_pre.p, ucnt + 25, c->big_pre.cap};
     rsc.emplace(c, kStRepair);
     MF_K(k_spec_eval<<<warps_grid(pending), kTB, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26,
@@ -2525,6 +2548,7 @@ void process_batch(mf_ctx* c, int64_t m) {
   unsigned long long* ucnt = reinterpret_cast<unsigned long long*>(cnt);
   int64_t* h = c->h_counters;
 
+  if (c->profile & 4) MF_CUDA(cudaMemsetAsync(cnt + 56, 0, sizeof(int64_t) * 2, s));
   // previous occurrence of every endpoint slot (for "not seen in this sub-batch")
   const int sbits = bits_for(std::max<int64_t>(2 * m - 1, 1));
   const int nbits = bits_for(std::max<int32_t>(n - 1, 1));
@@ -2676,6 +2700,17 @@ void process_batch(mf_ctx* c, int64_t m) {
         c->stats.exact_sizes += 1;
       }
     }
+    if (c->profile & 4) {
+      // the algorithmic accounting needs every row's exact length: the
+      // seeds' exact 2-hop sizes unless the growth check computed them
+      if (packed < 0) {
+        exact_sizes(c, ns, ep, false);
+        if (nct > 0) MF_K(k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns));
+      }
+      if (rows > 0)
+        MF_K(k_acct<<<(unsigned)std::min<int64_t>((rows + kTB - 1) / kTB, 1024), kTB, 0, s>>>(
+            c->rowlens.p, rows, c->seeds.p, ns, c->cands.p, c->deg.p, ucnt + 56));
+    }
     MF_CUDA(cudaGetLastError());
 
     // ---- the next sub-batch: re-plan after a growth of the limit, then its
@@ -2762,7 +2797,7 @@ void process_batch(mf_ctx* c, int64_t m) {
       if (nct > 0)
         MF_K(k_cand_bits<<<grid_for(nct), kTB, 0, s>>>(c->cands.p, nct, ns, c->rowcid.p, c->ncbits.p));
       const PullArgs pa{g,  c->v2i.p, c->rowcid.p, c->ncbits.p, ns, c->wval.p, ep, c->cid.p, c->pull_long.p,
-                        ucnt + 36, wk_extra + 2};
+                        ucnt + 36, wk_extra + 2, c->tune.pull_long};
       MF_K(k_pull_cand<<<grid_for(n), kTB, 0, s>>>(pa));
       MF_K(k_pull_cand_long<<<lb_grid(c, k_pull_cand_long), kTB, 0, s>>>(pa));
     } else {
@@ -2830,6 +2865,12 @@ void process_batch(mf_ctx* c, int64_t m) {
   }
   if (front_on_b) MF_CUDA(cudaStreamSynchronize(c->stream_b));
   c->stats.max_csr = c->max_csr;
+  if (c->profile & 4) {
+    MF_CUDA(cudaMemcpyAsync(h + 56, cnt + 56, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
+    MF_CUDA(cudaStreamSynchronize(s));
+    c->stats.packed_total = h[56];
+    c->stats.row_degree_total = h[57];
+  }
 }
 
 }  // namespace mf

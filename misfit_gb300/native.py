@@ -18,7 +18,7 @@ EXPORTS = [
     "mf_version", "mf_status_string", "mf_last_error", "mf_open_egr", "mf_open_csr", "mf_close",
     "mf_num_nodes", "mf_num_base_entries", "mf_set_mis", "mf_get_mis", "mf_mis_size", "mf_greedy_mis",
     "mf_flag_updates", "mf_flag_updates_noalloc", "mf_apply_batch", "mf_apply_batch_device", "mf_apply_batch_async", "mf_collect", "mf_sync",
-    "mf_last_batch_stats", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
+    "mf_last_batch_stats", "mf_get_tuning", "mf_set_tuning", "mf_get_row", "mf_get_degrees", "mf_is_adjacent", "mf_get_max_csr",
     "mf_set_max_csr", "mf_get_cluster_ids", "mf_check_mis", "mf_set_exact", "mf_compact", "mf_read_mis_file",
     "mf_write_mis_file", "mf_read_batch_file", "mf_parse_batch_file", "mf_list_batch_files", "mf_free", "mf_trace_enable",
     "mf_trace_count", "mf_trace_get", "mf_stage_name", "mf_profile_enable", "mf_profile_reset",
@@ -34,8 +34,16 @@ class BatchStats(C.Structure):
         ("updates", C.c_int64), ("sub_batches", C.c_int64), ("seeds", C.c_int64),
         ("candidates", C.c_int64), ("clusters", C.c_int64), ("processed_edges", C.c_int64),
         ("exact_sizes", C.c_int64), ("max_csr", C.c_int64), ("repair_rounds", C.c_int64),
-        ("device_ms", C.c_double),
+        ("device_ms", C.c_double), ("packed_total", C.c_int64), ("row_degree_total", C.c_int64),
     ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("pull_long", C.c_int64), ("heavy_min", C.c_int64), ("big_threshold", C.c_int64),
+                ("first_bound", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -114,6 +122,8 @@ def _lib():
         "mf_collect": (C.c_int, [_P, C.c_void_p]),
         "mf_sync": (C.c_int, [_P]),
         "mf_last_batch_stats": (C.c_int, [_P, C.POINTER(BatchStats)]),
+        "mf_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+        "mf_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
         "mf_get_row": (C.c_int, [_P, C.c_int32, _I32P, C.c_int64, _I64P]),
         "mf_get_degrees": (C.c_int, [_P, _I32P, C.c_int64]),
         "mf_is_adjacent": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int)]),
@@ -290,6 +300,19 @@ class Graph:
         finally:
             self._queued = []
 
+    def tuning(self):
+        t = Tuning()
+        _check(_lib().mf_get_tuning(self._h, C.byref(t)), "mf_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        """Load-balancing settings (pull_long, heavy_min, big_threshold,
+        first_bound); unnamed ones keep their values.  Results never change."""
+        cur = self.tuning()
+        cur.update(kw)
+        t = Tuning(**cur)
+        _check(_lib().mf_set_tuning(self._h, C.byref(t)), "mf_set_tuning")
+
     def stats(self):
         st = BatchStats()
         _check(_lib().mf_last_batch_stats(self._h, C.byref(st)), "mf_last_batch_stats")
@@ -357,7 +380,9 @@ class Graph:
         _check(_lib().mf_compact(self._h, os.fsencode(path), 1 if rebase else 0), "mf_compact")
 
     def profile(self, on=True):
-        """True/1: all stages; 2: the k_lb_push_hop launches only; False/0: off."""
+        """True/1: all stages; 2: the k_lb_push_hop launches only; False/0: off;
+        adding 4 also counts each batch's algorithmic work (stats packed_total,
+        row_degree_total), at the cost of exact 2-hop sizes in every sub-batch."""
         level = 1 if on is True else (0 if on is False else int(on))
         _check(_lib().mf_profile_enable(self._h, level), "mf_profile_enable")
 

@@ -22,7 +22,7 @@ import numpy as np
 
 __all__ = [
     "read_egr", "write_egr", "csr_from_pairs", "er_graph", "rmat_graph", "rmat_graph_torch", "rgg_graph",
-    "ToggleStream", "write_batch_file", "write_batch_folder", "read_batch_file",
+    "rgg_graph_torch", "ToggleStream", "DeviceToggles", "write_batch_file", "write_batch_folder", "read_batch_file",
     "write_mis_file", "read_mis_file", "undirected_pairs",
 ]
 
@@ -309,7 +309,10 @@ class ToggleStream:
 def rmat_graph_torch(scale, edge_factor, seed, device="cuda", abcd=(0.57, 0.19, 0.19, 0.05)):
     """R-MAT as rmat_graph, generated on a CUDA device with torch (Philox
     stream seeded by ``seed``); returns host numpy arrays (n, (nindex, nlist)).
-    Used for the large benchmark graphs, which numpy builds too slowly."""
+    Used for the large benchmark graphs, which numpy builds too slowly.  The
+    keys are de-duplicated and sorted per range of source vertices (at most
+    2^30 keys per sort), so that graphs beyond 2^31 directed entries build
+    without one giant sort; the result is the same as one global sort."""
     import torch
 
     a, b, c, _ = abcd
@@ -317,7 +320,9 @@ def rmat_graph_torch(scale, edge_factor, seed, device="cuda", abcd=(0.57, 0.19, 
     total = n * edge_factor
     gen = torch.Generator(device=device)
     gen.manual_seed(seed)
-    keys = []
+    nbuck = max(1, -(-2 * total // (1 << 30)))
+    bounds = [(n * k) // nbuck for k in range(nbuck + 1)]
+    buckets = [[] for _ in range(nbuck)]
     chunk = 1 << 25
     done = 0
     while done < total:
@@ -331,18 +336,207 @@ def rmat_graph_torch(scale, edge_factor, seed, device="cuda", abcd=(0.57, 0.19, 
         keep = u != v
         lo = torch.minimum(u[keep], v[keep])
         hi = torch.maximum(u[keep], v[keep])
-        keys.append(torch.unique(lo * n + hi))
+        key = torch.unique(lo * n + hi)
+        for k in range(nbuck):
+            sel = key[(key >= bounds[k] * n) & (key < bounds[k + 1] * n)]
+            if sel.numel():
+                buckets[k].append(sel)
         done += cnt
-    key = torch.unique(torch.cat(keys))
-    del keys
-    lo, hi = key // n, key % n
-    both = torch.sort(torch.cat([lo * n + hi, hi * n + lo])).values
-    src = both // n
-    dst = (both % n).to(torch.int32)
-    deg = torch.bincount(src, minlength=n)
+    # unique undirected keys, lo < hi, per bucket of lo
+    ukeys = []
+    for k in range(nbuck):
+        ukeys.append(torch.unique(torch.cat(buckets[k])) if buckets[k] else
+                     torch.zeros(0, dtype=torch.int64, device=device))
+        buckets[k] = None
+    # both directions, sorted per bucket of the source vertex
+    deg = torch.zeros(n, dtype=torch.int64, device=device)
+    for uk in ukeys:
+        deg += torch.bincount(uk // n, minlength=n) + torch.bincount(uk % n, minlength=n)
     nindex = torch.zeros(n + 1, dtype=torch.int64, device=device)
     nindex[1:] = torch.cumsum(deg, 0)
-    return n, (nindex.cpu().numpy(), dst.cpu().numpy())
+    nlist = np.empty(int(nindex[-1].item()), dtype=np.int32)
+    for k in range(nbuck):
+        lo_b, hi_b = bounds[k] * n, bounds[k + 1] * n
+        parts = [ukeys[k]]                                 # (lo, hi) with lo in the bucket
+        for uk in ukeys:                                   # (hi, lo) with hi in the bucket
+            h = uk % n
+            m = (h >= bounds[k]) & (h < bounds[k + 1])
+            if m.any():
+                parts.append(h[m] * n + uk[m] // n)
+        both = torch.sort(torch.cat(parts)).values
+        del parts
+        if both.numel():
+            assert int(both[0].item()) >= lo_b and int(both[-1].item()) < hi_b
+            start = int(nindex[bounds[k]].item())
+            nlist[start:start + both.numel()] = (both % n).to(torch.int32).cpu().numpy()
+        del both
+    del ukeys
+    return n, (nindex.cpu().numpy(), nlist)
+
+
+def rgg_graph_torch(n, mean_degree, seed, device="cuda"):
+    """2-D random geometric graph as rgg_graph (points uniform in the unit
+    square, radius set for the mean degree with the same boundary
+    correction), generated on a CUDA device with torch from its own seeded
+    stream: the same distribution as rgg_graph, not the same graph.  Returns
+    host numpy arrays (nindex int64, nlist int32), rows sorted ascending."""
+    import torch
+
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    pts = torch.rand((n, 2), generator=gen, device=device, dtype=torch.float64)
+    r = np.sqrt(mean_degree / (n * np.pi))
+    for _ in range(3):
+        r = np.sqrt(mean_degree / (n * np.pi * max(1e-9, 1 - 8 * r / (3 * np.pi))))
+    cells = max(1, int(1.0 / r))
+    cx = (pts[:, 0] * cells).long().clamp_(max=cells - 1)
+    cy = (pts[:, 1] * cells).long().clamp_(max=cells - 1)
+    cell = cx * cells + cy
+    order = torch.argsort(cell)
+    starts = torch.searchsorted(cell[order], torch.arange(cells * cells + 1, device=device))
+    r2 = r * r
+    us, vs = [], []
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            ncx, ncy = cx + dx, cy + dy
+            idx = ((ncx >= 0) & (ncx < cells) & (ncy >= 0) & (ncy < cells)).nonzero().squeeze(1)
+            nc = ncx[idx] * cells + ncy[idx]
+            lo = starts[nc]
+            cnt = starts[nc + 1] - lo
+            tot = int(cnt.sum().item())
+            if tot == 0:
+                continue
+            rep = torch.repeat_interleave(idx, cnt)
+            off = torch.arange(tot, device=device) - torch.repeat_interleave(torch.cumsum(cnt, 0) - cnt, cnt)
+            cand = order[torch.repeat_interleave(lo, cnt) + off]
+            d = pts[rep] - pts[cand]
+            sel = ((d * d).sum(dim=1) <= r2) & (rep < cand)
+            us.append(rep[sel])
+            vs.append(cand[sel])
+    u = torch.cat(us) if us else torch.zeros(0, dtype=torch.int64, device=device)
+    v = torch.cat(vs) if vs else torch.zeros(0, dtype=torch.int64, device=device)
+    both = torch.sort(torch.cat([u * n + v, v * n + u])).values
+    src = both // n
+    nindex = torch.zeros(n + 1, dtype=torch.int64, device=device)
+    nindex[1:] = torch.cumsum(torch.bincount(src, minlength=n), 0)
+    return nindex.cpu().numpy(), (both % n).to(torch.int32).cpu().numpy()
+
+
+class DeviceToggles:
+    """Batches of toggles drawn on a CUDA device against a graph's base CSR,
+    for graphs too large (or too many) for ToggleStream's host arrays.
+
+    A batch holds ``round(size*delete_frac)`` deletes of distinct base edges
+    and the rest inserts of distinct non-adjacent pairs (u != v), shuffled,
+    each line in a random direction.  ``endpoints``:
+      * ``uniform``: deletes uniform over the edges, insert endpoints uniform;
+      * ``preferential``: endpoints proportional to degree -- deletes uniform
+        over the edges (each endpoint of a uniform edge is degree-
+        proportional), insert endpoints drawn independently by degree;
+      * ``low_degree``: proportional to 1/max(degree, 1) -- a delete keeps a
+        uniform edge with probability w(u)*w(v), insert endpoints by weight.
+    Draws are against the base graph: a graph that takes many batches sees
+    deletes of edges an earlier batch may have deleted already (no-ops for
+    the overlay), as a client working from a stale copy would send them.
+    ``adjacent(a, b)`` (torch int64 tensors -> bool tensor) tests base
+    adjacency; by default a sorted key array of the base entries is built
+    on the device."""
+
+    def __init__(self, nindex, nlist, seed, device="cuda", adjacent=None):
+        import torch
+
+        self.torch = torch
+        self.dev = device
+        self.nindex = torch.as_tensor(np.asarray(nindex, np.int64), device=device)
+        self.n = int(self.nindex.numel() - 1)
+        self.nlist = torch.as_tensor(np.asarray(nlist, np.int32), device=device)
+        self.E = int(self.nlist.numel())
+        self.deg = (self.nindex[1:] - self.nindex[:-1]).to(torch.float64)
+        self.gen = torch.Generator(device=device)
+        self.gen.manual_seed(seed)
+        if adjacent is None:
+            src = torch.repeat_interleave(torch.arange(self.n, device=device),
+                                          (self.nindex[1:] - self.nindex[:-1]))
+            self.keys = src * self.n + self.nlist.to(torch.int64)   # ascending: sorted rows
+            adjacent = self._adjacent_keys
+        self.adjacent = adjacent
+        self._cdf = {}
+
+    def _adjacent_keys(self, a, b):
+        torch = self.torch
+        k = a * self.n + b
+        if self.E == 0:
+            return torch.zeros(k.shape, dtype=torch.bool, device=self.dev)
+        pos = torch.searchsorted(self.keys, k).clamp_(max=self.E - 1)
+        return self.keys[pos] == k
+
+    def _weights(self, mode):
+        if mode == "preferential":
+            return self.deg + 1e-12
+        return 1.0 / self.deg.clamp(min=1.0)
+
+    def _vertices(self, mode, size):
+        torch = self.torch
+        if mode == "uniform":
+            return torch.randint(0, self.n, (size,), generator=self.gen, device=self.dev)
+        if mode not in self._cdf:
+            self._cdf[mode] = torch.cumsum(self._weights(mode), 0)
+        cdf = self._cdf[mode]
+        x = torch.rand(size, generator=self.gen, device=self.dev, dtype=torch.float64) * cdf[-1]
+        return torch.searchsorted(cdf, x).clamp_(max=self.n - 1)
+
+    def _edges(self, mode, count):
+        torch = self.torch
+        got = torch.zeros(0, dtype=torch.int64, device=self.dev)
+        if count <= 0 or self.E == 0:
+            return got
+        w = None if mode in ("uniform", "preferential") else self._weights(mode)
+        while got.numel() < count:
+            need = count - got.numel()
+            draws = 4 * need + 64 if w is None else 64 * need + 1024
+            pos = torch.randint(0, self.E, (draws,), generator=self.gen, device=self.dev)
+            a = torch.searchsorted(self.nindex, pos, right=True) - 1
+            b = self.nlist[pos].to(torch.int64)
+            if w is not None:
+                keep = torch.rand(draws, generator=self.gen, device=self.dev, dtype=torch.float64) < w[a] * w[b]
+                a, b = a[keep], b[keep]
+            k = torch.minimum(a, b) * self.n + torch.maximum(a, b)
+            got = torch.unique(torch.cat([got, k]))
+            if got.numel() > count:
+                got = got[torch.randperm(got.numel(), generator=self.gen, device=self.dev)[:count]]
+        return got
+
+    def next_batch(self, size, delete_frac=0.5, endpoints="uniform"):
+        """(u, v, ins) host numpy arrays (int32, int32, uint8); ins is 1 for
+        an insert (non-adjacent in the base graph) and 0 for a delete."""
+        torch = self.torch
+        n = self.n
+        nd = min(int(round(size * delete_frac)), self.E // 2)
+        ni = size - nd
+        dkeys = self._edges(endpoints, nd)
+        ikeys = torch.zeros(0, dtype=torch.int64, device=self.dev)
+        tries = 0
+        while ikeys.numel() < ni and tries < 64:
+            tries += 1
+            need = ni - ikeys.numel()
+            a = self._vertices(endpoints, 2 * need + 16)
+            b = self._vertices(endpoints, 2 * need + 16)
+            ok = a != b
+            lo, hi = torch.minimum(a[ok], b[ok]), torch.maximum(a[ok], b[ok])
+            keep = ~self.adjacent(lo, hi)
+            ikeys = torch.unique(torch.cat([ikeys, lo[keep] * n + hi[keep]]))
+            if ikeys.numel() > ni:
+                ikeys = ikeys[torch.randperm(ikeys.numel(), generator=self.gen, device=self.dev)[:ni]]
+        keys = torch.cat([dkeys, ikeys])
+        ins = torch.cat([torch.zeros(dkeys.numel(), dtype=torch.uint8, device=self.dev),
+                         torch.ones(ikeys.numel(), dtype=torch.uint8, device=self.dev)])
+        perm = torch.randperm(keys.numel(), generator=self.gen, device=self.dev)
+        keys, ins = keys[perm], ins[perm]
+        lo, hi = keys // n, keys % n
+        flip = torch.rand(keys.numel(), generator=self.gen, device=self.dev) < 0.5
+        u = torch.where(flip, hi, lo).to(torch.int32)
+        v = torch.where(flip, lo, hi).to(torch.int32)
+        return u.cpu().numpy(), v.cpu().numpy(), ins.cpu().numpy()
 
 
 def write_batch_file(path, u, v):

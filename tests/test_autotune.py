@@ -75,3 +75,34 @@ def test_shape_key_buckets():
     k2 = autotune.shape_key([(2000, None, None)] * 4, b)     # same power-of-two bucket
     k3 = autotune.shape_key([(9000, None, None)] * 4, b)
     assert k1 == k2 and k1 != k3
+
+
+def test_plain_search_keeps_fastest_refuses_disagreement_and_caches(monkeypatch, tmp_path):
+    """tune_plain: one threshold at a time from the defaults, the fastest
+    value kept, a setting with a different membership refused, the winner
+    cached by GPU and shape."""
+    monkeypatch.setenv(autotune.CACHE_ENV, str(tmp_path / "cache.json"))
+    monkeypatch.setattr(autotune, "_gpu_name", lambda: "test-gpu")
+    want = {"pull_long": 8192, "heavy_min": 1024, "big_threshold": 1024, "first_bound": 64}
+    calls = []
+
+    def fake_plain(nindex, nlist, mis0, batches, tuning):
+        calls.append(dict(tuning))
+        sec = sum(abs(np.log2(tuning[k]) - np.log2(v)) for k, v in want.items())
+        return sec, np.zeros(4, np.uint8)
+
+    monkeypatch.setattr(autotune, "run_plain", fake_plain)
+    nindex = np.zeros(1025, np.int64)
+    batches = [(np.zeros(100, np.int32), None, None)]
+    best, rep = autotune.tune_plain(nindex, None, None, batches)
+    assert best == want and not rep["cached"]
+    assert len(calls) == 1 + sum(len(v) for _, v in autotune.PLAIN_KNOBS)
+    best2, rep2 = autotune.tune_plain(nindex, None, None, batches)
+    assert rep2["cached"] and best2 == want and len(calls) == 1 + sum(len(v) for _, v in autotune.PLAIN_KNOBS)
+
+    def bad_plain(nindex, nlist, mis0, batches, tuning):
+        return 1.0, np.full(4, 1 if tuning["pull_long"] == 8192 else 0, np.uint8)
+
+    monkeypatch.setattr(autotune, "run_plain", bad_plain)
+    with pytest.raises(RuntimeError):
+        autotune.tune_plain(nindex, None, None, batches, use_cache=False)

@@ -34,3 +34,18 @@ def test_reference_arm_two_ranks_gloo():
     assert d["impl"] == "reference" and d["n_gpus"] == 2
     assert d["value"] > 0 and d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_evolving_state_single_rank():
+    """The reference arm carries its state across steps and reports what it
+    actually timed: the lines of each step, the time spent on them."""
+    pytest.importorskip("torch")
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--scale", "10",
+           "--batch", "300", "--steps", "2", "--warmup", "1", "--cpu-seconds", "30"]
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS="2")
+    out = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][0])
+    assert d["lines_timed_per_step"] == [300, 300]     # a small batch fits the budget whole
+    assert d["sampled_fraction"] == 1.0 and d["extrapolated"] is False
+    assert abs(d["value"] - 600 / (d["ms_per_step"] * 2 / 1e3)) < 1e-6 * d["value"]

@@ -393,3 +393,35 @@ def test_exact_mode_matches_oracle(gpu_lib, kind):
     finally:
         gr.close()
         orc.close()
+
+
+def test_tuning_settings_change_no_result(gpu_lib):
+    """mf_set_tuning moves work between kernels, never a result: an R-MAT
+    stream with cut sub-batches gives the same memberships and cluster ids
+    under extreme settings as under the defaults; bad settings are refused."""
+    from misfit_gb300 import autotune
+    n, ni, nl, bs = _stream("rmat", 21, 3, 600, endpoints="preferential")
+    mis0 = O.greedy_mis(ni, nl)
+    orc = O.Oracle.from_csr(ni, nl)
+    flags = [orc.flag_updates(u, v) for u, v in bs]
+    results = []
+    for tune in ({}, {"pull_long": 32, "heavy_min": 64, "big_threshold": 0, "first_bound": 8},
+                 {"pull_long": 1 << 20, "heavy_min": 1 << 30, "big_threshold": 1 << 40, "first_bound": 1 << 20}):
+        g = native.Graph.from_csr(ni, nl)
+        if not tune:
+            assert g.tuning() == autotune.DEFAULT_TUNING
+        g.max_csr = 30000
+        g.set_tuning(**tune)
+        g.set_mis(mis0)
+        out = []
+        for (u, v), ins in zip(bs, flags):
+            g.apply_batch(u, v, ins)
+            out.append((g.get_mis(), g.cluster_ids()))
+        results.append(out)
+        for bad in ({"pull_long": 1}, {"first_bound": 4}, {"big_threshold": -1}):
+            with pytest.raises(native.MisfitError):
+                g.set_tuning(**bad)
+        g.close()
+    for other in results[1:]:
+        for (m0, c0), (m1, c1) in zip(results[0], other):
+            assert np.array_equal(m0, m1) and np.array_equal(c0, c1)
