@@ -193,6 +193,9 @@ typedef struct mf_tuning {
                              eligible vertex goes to the grid-wide kernel (default 256) */
   int64_t first_bound;    /* row positions the warp level of the first-cluster-id search covers
                              before long rows go to the chunk level (default 256, at least 8) */
+  int64_t cand_push;      /* 0: on graphs with symmetric sorted rows, the candidate rows' cluster ids
+                             are pulled by every vertex (default); 1: always pushed from the
+                             candidate rows, then finalised per vertex */
 } mf_tuning;
 int mf_get_tuning(mf_ctx* ctx, mf_tuning* out);
 int mf_set_tuning(mf_ctx* ctx, const mf_tuning* in);
@@ -258,7 +261,7 @@ void mf_free(void* p);
 /* ---- profiling ----------------------------------------------------------- */
 
 /* Number of stages the profiler distinguishes. */
-#define MF_NUM_STAGES 13
+#define MF_NUM_STAGES 15
 /* Name of stage i (0 <= i < MF_NUM_STAGES), NULL otherwise. */
 const char* mf_stage_name(int stage);
 /* on = 1: every later batch records CUDA events around each stage on the

@@ -14,11 +14,12 @@ Results are cached in a JSON file keyed by the GPU name and a shape bucket
 of the workload (graph count, log2 of the median vertex count and of the
 median batch size), so later runs with a similar mix skip the search.
 
-tune_plain does the same for the per-batch path (mf_apply_batch): its four
-load-balancing thresholds (mf_tuning: the candidate pull's long-row cut,
-the heavy-vertex row length of the exact sizes, the hop-2 volume that
-defers the insertion rule's search to the grid-wide kernel, and the warp
-level of the first-cluster-id search) are searched one after another on
+tune_plain does the same for the per-batch path (mf_apply_batch): its
+load-balancing settings (mf_tuning: pull or push for the candidate rows'
+cluster ids, the candidate pull's long-row cut, the heavy-vertex row length
+of the exact sizes, the hop-2 volume that defers the insertion rule's
+search to the grid-wide kernel, and the warp level of the
+first-cluster-id search) are searched one after another on
 the caller's batches, each candidate on a fresh context, every candidate
 required to give the same memberships.
 """
@@ -131,8 +132,9 @@ def tune_batched(graphs, mis0, batches, use_cache=True):
 
 # The library's defaults of mf_tuning (a GPU test checks that a new context
 # reports these), and the candidate values, searched one at a time.
-DEFAULT_TUNING = {"pull_long": 2048, "heavy_min": 2048, "big_threshold": 256, "first_bound": 256}
+DEFAULT_TUNING = {"pull_long": 2048, "heavy_min": 2048, "big_threshold": 256, "first_bound": 256, "cand_push": 0}
 PLAIN_KNOBS = (
+    ("cand_push", (0, 1)),
     ("big_threshold", (64, 256, 1024, 4096)),
     ("first_bound", (64, 256, 1024)),
     ("pull_long", (512, 2048, 8192)),

@@ -87,7 +87,7 @@ void ktime_end(const char* launch_text, double t0) {
 
 const char* const kStageNames[kStCount] = {"overlay", "split",  "seeds", "hop1",  "sizes", "cluster_read",
                                            "cluster_write", "assign", "repair", "clear", "exact", "repair_big",
-                                           "push_hop"};
+                                           "push_hop", "cluster_read_need", "pull"};
 
 void set_error(const std::string& msg) { g_error = msg; }
 
@@ -769,9 +769,9 @@ int mf_set_tuning(mf_ctx* c, const mf_tuning* in) {
   return guarded([&] {
     need(c && in, MF_EINVAL, "null argument");
     need(in->pull_long >= 32 && in->heavy_min >= 64 && in->big_threshold >= 0 && in->first_bound >= 8 &&
-             in->first_bound <= ((int64_t)1 << 20),
+             in->first_bound <= ((int64_t)1 << 20) && (in->cand_push == 0 || in->cand_push == 1),
          MF_EINVAL, "tuning out of range (pull_long >= 32, heavy_min >= 64, big_threshold >= 0, "
-                    "8 <= first_bound <= 2^20)");
+                    "8 <= first_bound <= 2^20, cand_push 0 or 1)");
     bind(c);
     c->tune = *in;
   });

@@ -96,6 +96,8 @@ enum Stage : int {
   kStExact,         // exact 2-hop sizes (heavy bitmaps) and limit growth
   kStRepairBig,     // MIS repair: grid-wide hop-2 searches
   kStPushHop,       // the k_lb_push_hop launches alone (part of the clustering write)
+  kStFirstNeed,     // clustering read, seeds without an id in their own row (the hop-2 part)
+  kStPull,          // clustering write, the candidate rows' ids (pull or push + finalize)
   kStCount
 };
 extern const char* const kStageNames[kStCount];
@@ -458,7 +460,10 @@ struct Scratch {
   DBuf<int64_t> hist_scan;
   DBuf<uint64_t> keys_alt;
   DBuf<uint32_t> vals_alt;
+  DBuf<unsigned long long> scan_status;   // look-back scan: 3 words per tile, tagged with scan_seq
+  unsigned long long scan_seq = 0;
   void release() {
+    scan_status.release();
     block_sums.release();
     block_sums2.release();
     hist.release();
@@ -607,6 +612,7 @@ struct mf_ctx {
   mf::DBuf<unsigned long long> work;   // 2 * kStCount entries
   double stage_bytes[mf::kStCount] = {};
   mf::DBuf<int64_t> lb_offs;           // row-position prefix for lb_rows
+  mf::DBuf<uint32_t> cidbits;          // bit y <=> cid[y] != -1, during the clustering read
   int64_t touched_total = 0;
   int64_t dbg_first[5] = {};           // debug: first-hit calls, rows, warp-level rows, chunk rows, chunks
 
@@ -620,7 +626,7 @@ struct mf_ctx {
   bool pending = false;
   // load-balancing settings (mf_set_tuning); they move work between kernels,
   // never a result
-  mf_tuning tune = mf_tuning{2048, 2048, 256, 256};
+  mf_tuning tune = mf_tuning{2048, 2048, 256, 256, 0};
 
   mf::GraphView view() const {
     return mf::GraphView{n, nindex.p, nlist.p, live.p, dead.p, aoff.p, aadj.p};
@@ -646,17 +652,17 @@ void for_each_buffer(mf_ctx* c, F&& f) {
   f(c->un_idx); f(c->un_v); f(c->need); f(c->needv); f(c->live_i); f(c->live_v); f(c->nlist_need);
   f(c->live); f(c->bval); f(c->wval); f(c->vals); f(c->app_vals); f(c->rp_vals); f(c->rp_vals2);
   f(c->bitmaps); f(c->heavy_bits); f(c->dense_bits); f(c->ncbits); f(c->n2stamp);
-  f(c->n2bstamp); f(c->nmark);
+  f(c->n2bstamp); f(c->nmark); f(c->cidbits);
   f(c->mis); f(c->bins); f(c->u8a); f(c->akill); f(c->creates); f(c->rp_u8); f(c->plan_flags);
   f(c->xst); f(c->xleave); f(c->cta_vert); f(c->cta_ws);
   f(c->keys); f(c->app_keys); f(c->rp_keys); f(c->rp_keys2);
   f(c->big_best); f(c->fpos); f(c->work);
   f(c->ws.block_sums); f(c->ws.block_sums2); f(c->ws.hist); f(c->ws.hist_scan); f(c->ws.keys_alt);
-  f(c->ws.vals_alt);
+  f(c->ws.vals_alt); f(c->ws.scan_status);
   for (auto& fr : c->front) {
     f(fr.bits); f(fr.bits_sums); f(fr.uacc); f(fr.hlist); f(fr.cands); f(fr.lb_offs); f(fr.cnt);
     f(fr.ws.block_sums); f(fr.ws.block_sums2); f(fr.ws.hist); f(fr.ws.hist_scan); f(fr.ws.keys_alt);
-    f(fr.ws.vals_alt);
+    f(fr.ws.vals_alt); f(fr.ws.scan_status);
   }
 }
 

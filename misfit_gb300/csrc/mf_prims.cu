@@ -1,8 +1,9 @@
 // mf_prims.cu -- device scans and a stable LSD radix sort.
 //
-// Scans: three passes (tile reduce, scan of tile sums in one block, tile
-// rescan).  Tiles are 256 threads x 8 items, loaded striped for coalescing
-// and scanned per thread out of shared memory.
+// Scans: one launch.  Small inputs in one block; larger ones with the
+// single-pass decoupled look-back scan (k_scan_lookback).  Tiles are 256
+// threads x 8 items, loaded striped for coalescing and scanned per thread out
+// of shared memory.
 // Radix sort: 8-bit digits, per-tile digit histograms, a scan over the
 // digit-major histogram and a stable scatter that ranks items inside a tile
 // with __match_any_sync.  Stability is what the callers rely on: equal keys
@@ -66,73 +67,6 @@ __device__ __forceinline__ int64_t block_exclusive(int64_t v, int64_t* smem_warp
   return r;
 }
 
-template <typename L>
-__global__ void k_tile_reduce(L load, int64_t n, int64_t* sums) {
-  __shared__ int64_t sw[33];
-  const int64_t base = (int64_t)blockIdx.x * kTile;
-  int64_t acc = 0;
-  for (int k = 0; k < kItems; ++k) {
-    const int64_t i = base + (int64_t)k * kThreads + threadIdx.x;
-    if (i < n) acc += load(i);
-  }
-  const int64_t t = block_sum(acc, sw);
-  if (threadIdx.x == 0) sums[blockIdx.x] = t;
-}
-
-// Single block: exclusive scan of sums[0..nb) in place, total to sums[nb].
-__global__ void k_scan_sums(int64_t* sums, int64_t nb) {
-  __shared__ int64_t sw[33];
-  int64_t carry = 0;
-  for (int64_t base = 0; base < nb; base += kTile) {
-    int64_t v[kItems];
-    int64_t local = 0;
-    for (int k = 0; k < kItems; ++k) {
-      const int64_t i = base + (int64_t)threadIdx.x * kItems + k;
-      v[k] = i < nb ? sums[i] : 0;
-      local += v[k];
-    }
-    int64_t tot;
-    int64_t pre = block_exclusive(local, sw, &tot) + carry;
-    for (int k = 0; k < kItems; ++k) {
-      const int64_t i = base + (int64_t)threadIdx.x * kItems + k;
-      if (i < nb) sums[i] = pre;
-      pre += v[k];
-    }
-    carry += tot;
-  }
-  if (threadIdx.x == 0) sums[nb] = carry;
-}
-
-template <typename L>
-__global__ void k_tile_scan(L load, int64_t n, const int64_t* offs, int64_t* out) {
-  __shared__ int64_t tile[kTile];
-  __shared__ int64_t sw[33];
-  const int64_t base = (int64_t)blockIdx.x * kTile;
-  for (int k = 0; k < kItems; ++k) {
-    const int idx = k * kThreads + threadIdx.x;
-    const int64_t i = base + idx;
-    tile[idx] = i < n ? load(i) : 0;
-  }
-  __syncthreads();
-  int64_t local = 0;
-  for (int k = 0; k < kItems; ++k) local += tile[threadIdx.x * kItems + k];
-  int64_t tot;
-  int64_t pre = block_exclusive(local, sw, &tot) + offs[blockIdx.x];
-  for (int k = 0; k < kItems; ++k) {
-    const int idx = threadIdx.x * kItems + k;
-    const int64_t v = tile[idx];
-    tile[idx] = pre;
-    pre += v;
-  }
-  __syncthreads();
-  for (int k = 0; k < kItems; ++k) {
-    const int idx = k * kThreads + threadIdx.x;
-    const int64_t i = base + idx;
-    if (i < n) out[i] = tile[idx];
-  }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = offs[gridDim.x];
-}
-
 // One block scans the whole (small) input tile by tile with a carry.
 template <typename L>
 __global__ void k_scan_single(L load, int64_t n, int64_t* out) {
@@ -158,7 +92,101 @@ __global__ void k_scan_single(L load, int64_t n, int64_t* out) {
   if (threadIdx.x == 0) out[n] = carry;
 }
 
-constexpr int64_t kSingleScanMax = 65536;
+// Single-pass scan with decoupled look-back (Merrill and Garland, "Single-pass
+// Parallel Prefix Scan with Decoupled Look-back", 2016): one launch, one
+// tile of kTile items per block.  Tile t publishes its aggregate, then looks
+// back over its predecessors, adding aggregates until it meets an inclusive
+// prefix, and publishes its own inclusive prefix.  Each tile has three
+// status words: aggregate, inclusive prefix, and a tag (seq << 2 | flag,
+// flag 1 = aggregate ready, 2 = inclusive ready), the value slots written
+// before the tag.  `seq` is new for every call, so the words are never reset
+// (a stale tag never matches).  Blocks are dispatched in index order, so a
+// tile's predecessors are running or done; still, a wait on one gives up
+// after kLookbackSpin reads, and the tile then sums its predecessors' inputs
+// itself, so the result is right and the wait ends either way.
+constexpr int64_t kLookbackSpin = (int64_t)1 << 22;
+
+template <typename L>
+__global__ void __launch_bounds__(kThreads) k_scan_lookback(L load, int64_t n, int64_t* out,
+                                                            unsigned long long* st, unsigned long long seq) {
+  __shared__ int64_t tile[kTile];
+  __shared__ int64_t sw[33];
+  __shared__ int64_t s_excl;
+  __shared__ int s_fallback;
+  const int64_t t = blockIdx.x;
+  const int64_t base = t * kTile;
+  for (int k = 0; k < kItems; ++k) {
+    const int idx = k * kThreads + threadIdx.x;
+    const int64_t i = base + idx;
+    tile[idx] = i < n ? load(i) : 0;
+  }
+  __syncthreads();
+  int64_t local = 0;
+  for (int k = 0; k < kItems; ++k) local += tile[threadIdx.x * kItems + k];
+  int64_t tot;
+  int64_t pre = block_exclusive(local, sw, &tot);
+  unsigned long long* my = st + 3 * t;
+  if (threadIdx.x == 0) {
+    int64_t excl = 0;
+    int fb = 0;
+    if (t > 0) {
+      *(volatile unsigned long long*)(my + 0) = (unsigned long long)tot;
+      __threadfence();
+      atomicExch(my + 2, (seq << 2) | 1ull);
+      for (int64_t q = t - 1; q >= 0;) {
+        unsigned long long tag = 0;
+        int64_t spins = 0;
+        do {
+          tag = *(volatile const unsigned long long*)(st + 3 * q + 2);
+        } while ((tag >> 2) != seq && ++spins < kLookbackSpin);
+        if ((tag >> 2) != seq) {
+          fb = 1;
+          break;
+        }
+        __threadfence();
+        if ((tag & 3ull) == 2ull) {
+          excl += (int64_t)*(volatile const unsigned long long*)(st + 3 * q + 1);
+          break;
+        }
+        excl += (int64_t)*(volatile const unsigned long long*)(st + 3 * q + 0);
+        --q;
+      }
+    }
+    s_excl = excl;
+    s_fallback = fb;
+  }
+  __syncthreads();
+  if (s_fallback) {
+    int64_t acc = 0;
+    for (int64_t i = threadIdx.x; i < base; i += blockDim.x) acc += load(i);
+    const int64_t sum = block_sum(acc, sw);
+    if (threadIdx.x == 0) s_excl = sum;
+    __syncthreads();
+  }
+  const int64_t excl = s_excl;
+  if (threadIdx.x == 0) {
+    *(volatile unsigned long long*)(my + 1) = (unsigned long long)(excl + tot);
+    __threadfence();
+    atomicExch(my + 2, (seq << 2) | 2ull);
+  }
+  pre += excl;
+  for (int k = 0; k < kItems; ++k) {
+    const int idx = threadIdx.x * kItems + k;
+    const int64_t v = tile[idx];
+    tile[idx] = pre;
+    pre += v;
+  }
+  __syncthreads();
+  for (int k = 0; k < kItems; ++k) {
+    const int idx = k * kThreads + threadIdx.x;
+    const int64_t i = base + idx;
+    if (i < n) out[i] = tile[idx];
+  }
+  if (t == (int64_t)gridDim.x - 1 && threadIdx.x == 0) out[n] = excl + tot;
+}
+
+// Inputs up to two tiles go to one block; larger ones to the look-back scan.
+constexpr int64_t kSingleScanMax = 2 * kTile;
 
 template <typename L>
 void scan_exclusive(L load, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s) {
@@ -172,10 +200,13 @@ void scan_exclusive(L load, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s
     return;
   }
   const int64_t nb = (n + kTile - 1) / kTile;
-  ws.block_sums.reserve(nb + 1);
-  MF_K(k_tile_reduce<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p));
-  MF_K(k_scan_sums<<<1, kThreads, 0, s>>>(ws.block_sums.p, nb));
-  MF_K(k_tile_scan<<<(unsigned)nb, kThreads, 0, s>>>(load, n, ws.block_sums.p, out));
+  if (ws.scan_status.cap < 3 * nb) {
+    ws.scan_status.reserve(3 * nb);
+    // fresh memory may hold anything: no tag may match a later sequence number
+    MF_CUDA(cudaMemsetAsync(ws.scan_status.p, 0, sizeof(unsigned long long) * (size_t)ws.scan_status.cap, s));
+  }
+  const unsigned long long seq = ++ws.scan_seq;
+  MF_K(k_scan_lookback<<<(unsigned)nb, kThreads, 0, s>>>(load, n, out, ws.scan_status.p, seq));
   MF_CUDA(cudaGetLastError());
 }
 

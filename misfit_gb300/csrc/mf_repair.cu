@@ -728,10 +728,21 @@ __global__ void k_growth(const int64_t* pex, int64_t rows, int64_t* io) {
 
 constexpr unsigned long long kNoPos = ~0ull;
 
-struct HasCid {   // the element already carries a cluster id
-  const int32_t* cid;
-  __device__ __forceinline__ bool operator()(int32_t y) const { return cid[y] != -1; }
+// The element already carries a cluster id, tested on a bitmap (bit y set
+// <=> cid[y] != -1) built before the clustering read, while the ids do not
+// change: the first-hit searches read 1 bit per element from an array 32x
+// smaller than the ids, which stays in L1, instead of a 4-byte id from L2.
+struct HasCidBit {
+  const uint32_t* bits;
+  __device__ __forceinline__ bool operator()(int32_t y) const { return (__ldg(bits + (y >> 5)) >> (y & 31)) & 1u; }
 };
+
+__global__ void k_cid_bits(const int32_t* cid, int32_t n, uint32_t* bits) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool set = i < n && cid[i] != -1;
+  const unsigned m = __ballot_sync(0xffffffffu, set);
+  if ((threadIdx.x & 31) == 0 && i < ((int64_t)n + 31)) bits[i >> 5] = m;
+}
 
 // ---- first-hit searches with device-side counts ---------------------------------
 // Three levels, none of which needs the host to know a count:
@@ -1768,7 +1779,13 @@ __global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_
       // search (each step samples 32 prefix entries and keeps the interval
       // around the boundary, so a hub row of 10^6 entries takes 4 steps)
       int live = 0;
-      if (lane == 0) live = (unsigned long long)p0 < best[i] ? 1 : 0;  // an earlier chunk may have answered
+      if (lane == 0) {
+        live = (unsigned long long)p0 < best[i] ? 1 : 0;  // an earlier chunk may have answered
+        // chunks are handed out in increasing position order, so once edge i
+        // has an answer before this chunk, no later chunk of edge i can beat
+        // it: move the queue head to the next edge's first chunk
+        if (!live) atomicMax(queue, (unsigned long long)chunk_pre[i + 1]);
+      }
       live = __shfl_sync(0xffffffffu, live, 0);
       int64_t lo = 0, hi = nr;  // pre[lo] <= p0 < pre[hi]
       while (live && hi - lo > 1) {
@@ -1843,7 +1860,10 @@ __global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0 && s_best != ~0ull) atomicMin(best + i, s_best);
+    if (threadIdx.x == 0 && s_best != ~0ull) {
+      atomicMin(best + i, s_best);
+      atomicMax(queue, (unsigned long long)chunk_pre[i + 1]);   // edge i's later chunks cannot win
+    }
     __syncthreads();
   }
 }
@@ -2753,12 +2773,16 @@ void process_batch(mf_ctx* c, int64_t m) {
     const ChunkQueue mq{c->mq_idx.p, c->mq_v.p, c->mq_base.p, ucnt + 50};
     MF_K(k_row_skip<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->rowcid.p,
                                                     c->creates.p, c->live_i.p, c->live_v.p, ucnt + 33));
-    first_hits(c, c->live_v.p, ucnt + 33, rows, HasCid{c->cid.p});
+    c->cidbits.reserve(((int64_t)n + 31) / 32 + 1);
+    MF_K(k_cid_bits<<<grid_for(((int64_t)n + 31) / 32 * 32), kTB, 0, s>>>(c->cid.p, n, c->cidbits.p));
+    const HasCidBit has_cid{c->cidbits.p};
+    first_hits(c, c->live_v.p, ucnt + 33, rows, has_cid);
     MF_K(k_live_decide<<<lb_grid(c, k_live_decide), kTB, 0, s>>>(g, c->live_i.p, c->live_v.p, ucnt + 33, ns,
                                                                  c->fpos.p, c->cid.p, c->rowcid.p, c->creates.p,
                                                                  c->seeds.p, c->need.p, c->needv.p, ucnt + 34, mq));
+    sc.emplace(c, kStFirstNeed);
     MF_K(k_mark_need<<<lb_grid(c, k_mark_need), kTB, 0, s>>>(g, mq, ep, c->nmark.p, c->nlist_need.p, ucnt + 35));
-    first_hits(c, c->nlist_need.p, ucnt + 35, n, HasCid{c->cid.p});
+    first_hits(c, c->nlist_need.p, ucnt + 35, n, has_cid);
     MF_K(k_f1_finish<<<lb_grid(c, k_f1_finish), kTB, 0, s>>>(g, c->nlist_need.p, ucnt + 35, c->fpos.p, c->cid.p,
                                                              c->f1.p));
     first_hits(c, c->needv.p, ucnt + 34, ns, HasF1{c->f1.p});
@@ -2788,7 +2812,8 @@ void process_batch(mf_ctx* c, int64_t m) {
                                                                  c->wval.p, wk_extra + 1));
     sc.emplace(c, kStPush);
     if (debug_launches()) debug_push_hop(c, wk_extra + 1, dbg1);
-    if (c->symmetric && c->rows_sorted) {
+    sc.emplace(c, kStPull);
+    if (c->symmetric && c->rows_sorted && c->tune.cand_push == 0) {
       c->pull_long.reserve(std::max<int32_t>(n, 1));
       const int64_t nwords = ((int64_t)n + 31) / 32;
       c->ncbits.reserve(std::max<int64_t>(nwords, 1));

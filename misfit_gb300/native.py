@@ -43,7 +43,7 @@ class BatchStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("pull_long", C.c_int64), ("heavy_min", C.c_int64), ("big_threshold", C.c_int64),
-                ("first_bound", C.c_int64)]
+                ("first_bound", C.c_int64), ("cand_push", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -83,12 +83,12 @@ def test_plain_search_keeps_fastest_refuses_disagreement_and_caches(monkeypatch,
     cached by GPU and shape."""
     monkeypatch.setenv(autotune.CACHE_ENV, str(tmp_path / "cache.json"))
     monkeypatch.setattr(autotune, "_gpu_name", lambda: "test-gpu")
-    want = {"pull_long": 8192, "heavy_min": 1024, "big_threshold": 1024, "first_bound": 64}
+    want = {"pull_long": 8192, "heavy_min": 1024, "big_threshold": 1024, "first_bound": 64, "cand_push": 1}
     calls = []
 
     def fake_plain(nindex, nlist, mis0, batches, tuning):
         calls.append(dict(tuning))
-        sec = sum(abs(np.log2(tuning[k]) - np.log2(v)) for k, v in want.items())
+        sec = sum(abs(np.log2(tuning[k] + 1) - np.log2(v + 1)) for k, v in want.items())
         return sec, np.zeros(4, np.uint8)
 
     monkeypatch.setattr(autotune, "run_plain", fake_plain)
