@@ -20,7 +20,8 @@ LIB = os.path.join(LIB_DIR, "libmisfit_gb.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["mf_prims.cu", "mf_overlay.cu", "mf_repair.cu", "mf_api.cu", "mf_pool.cu", "mf_parse.cu", "mf_batched.cu"]
 CLI_SOURCE = "misfit_main.cpp"
-HEADERS = [os.path.join(CSRC, "mf_internal.cuh"), os.path.join(CSRC, "mf_cta.cuh"), os.path.join(ROOT, "include", "misfit_gb.h")]
+HEADERS = [os.path.join(CSRC, "mf_internal.cuh"), os.path.join(CSRC, "mf_cta.cuh"), os.path.join(CSRC, "mf_scan.cuh"),
+           os.path.join(ROOT, "include", "misfit_gb.h")]
 
 
 def nvcc():

@@ -249,9 +249,18 @@ __device__ __forceinline__ void warp_row_each(const GraphView& g, int32_t x, F f
 // shared-memory probes (none when the whole 32-position window lies in one
 // row) and the element loads of four windows are issued before any is used.
 // Kernels that call it run blocks of kLbThreads threads.
+// Compile-time knobs of the traversal (defaults are the measured best):
+// windows loaded before any is used, and the minimum resident blocks per SM
+// the traversal kernels are compiled for (1: no register cap).
+#ifndef MF_LB_UNROLL
+#define MF_LB_UNROLL 4
+#endif
+#ifndef MF_LB_MIN_BLOCKS
+#define MF_LB_MIN_BLOCKS 1
+#endif
 constexpr int kLbThreads = 256;
 constexpr int kLbWarps = kLbThreads / 32;
-constexpr int kLbUnroll = 4;
+constexpr int kLbUnroll = MF_LB_UNROLL;
 
 struct LbStage {
   int64_t end[32];    // end position (exclusive) of staged row k

@@ -28,6 +28,7 @@
 #include <unordered_map>
 
 #include "mf_internal.cuh"
+#include "mf_scan.cuh"
 
 namespace mf {
 
@@ -190,27 +191,36 @@ __global__ void k_seed_rows(const int32_t* seeds_all, int64_t ns, int32_t* seeds
 // Row-position counts for lb_rows; rows that must not be visited count 0.
 enum CountKind : int { kCntAll = 0, kCntSeedRows, kCntCandRows, kCntSeedPushers, kCntHopPushers };
 
-__global__ void k_row_counts(GraphView g, const int32_t* list, int64_t cnt, int kind, const int32_t* rowcid,
-                             int64_t ns, const uint32_t* bval, uint32_t epoch, const int32_t* v2i, int64_t* out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cnt) return;
-  const int32_t x = list[i];
-  bool use = true;
-  if (kind == kCntSeedRows) {
-    use = rowcid[i] != kSkip;
-  } else if (kind == kCntCandRows) {
-    use = rowcid[ns + i] != kSkip;
-  } else if (kind == kCntSeedPushers) {
-    use = (bval[x] >> kRowBits) == epoch;
-  } else if (kind == kCntHopPushers) {
-    use = (bval[x] >> kRowBits) == epoch;
-    const int32_t vi = v2i[x];
-    // seeds push in their own pass; a candidate row that writes its own tag
-    // over row(x) dominates bval[x] there (candidate tags are the larger)
-    if (vi >= 0 && ((int64_t)vi < ns || rowcid[vi] != kSkip)) use = false;
+// The count of row i is computed inside the scan's tile load (RowCounts is
+// the scan's loader), so the prefix needs one launch and no count array.
+struct RowCounts {
+  GraphView g;
+  const int32_t* list;
+  int kind;
+  const int32_t* rowcid;
+  int64_t ns;
+  const uint32_t* bval;
+  uint32_t epoch;
+  const int32_t* v2i;
+  __device__ __forceinline__ int64_t operator()(int64_t i) const {
+    const int32_t x = list[i];
+    bool use = true;
+    if (kind == kCntSeedRows) {
+      use = rowcid[i] != kSkip;
+    } else if (kind == kCntCandRows) {
+      use = rowcid[ns + i] != kSkip;
+    } else if (kind == kCntSeedPushers) {
+      use = (bval[x] >> kRowBits) == epoch;
+    } else if (kind == kCntHopPushers) {
+      use = (bval[x] >> kRowBits) == epoch;
+      const int32_t vi = v2i[x];
+      // seeds push in their own pass; a candidate row that writes its own tag
+      // over row(x) dominates bval[x] there (candidate tags are the larger)
+      if (vi >= 0 && ((int64_t)vi < ns || rowcid[vi] != kSkip)) use = false;
+    }
+    return use ? row_positions(g, x) : 0;
   }
-  out[i] = use ? row_positions(g, x) : 0;
-}
+};
 
 __device__ __forceinline__ void add_work(unsigned long long* work, int64_t visited) {
   for (int o = 16; o > 0; o >>= 1) visited += __shfl_down_sync(0xffffffffu, visited, o);
@@ -231,7 +241,7 @@ constexpr int kBitsWords = kBitsThreads * kBitsPerThread;       // words per blo
 // the sum of len(h) over row(s) for the packed-size upper bound (uacc).
 // deg[y] (DeltaOverlay::degree) is at least the overlay row length of y (a
 // tombstone removes at least one base entry), so the sums stay upper bounds.
-__global__ void __launch_bounds__(kLbThreads) k_lb_hop1_bound(GraphView g, const int32_t* deg, const int32_t* seeds,
+__global__ void __launch_bounds__(kLbThreads, MF_LB_MIN_BLOCKS) k_lb_hop1_bound(GraphView g, const int32_t* deg, const int32_t* seeds,
                                                               const int64_t* offs, int64_t ns, uint32_t* hbits,
                                                               unsigned long long* uacc, unsigned long long* work) {
   int64_t cur = -1;
@@ -1055,7 +1065,7 @@ __global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, co
   if ((t >> kRowBits) == epoch) push_w(wval, x, t);
 }
 
-__global__ void __launch_bounds__(kLbThreads) k_lb_push_hop(GraphView g, const int32_t* list, const int64_t* offs,
+__global__ void __launch_bounds__(kLbThreads, MF_LB_MIN_BLOCKS) k_lb_push_hop(GraphView g, const int32_t* list, const int64_t* offs,
                                                             int64_t cnt, uint32_t epoch, const uint32_t* bval,
                                                             uint32_t* wval, unsigned long long* work) {
   // the row's tag is staged once per row with the row's metadata
@@ -2139,23 +2149,16 @@ unsigned lb_grid(mf_ctx* c, K kernel) {
 // Row-position prefix of list[0..cnt) for lb_rows into c->lb_offs.
 void row_offsets(mf_ctx* c, const int32_t* list, int64_t cnt, int kind, int64_t ns, uint32_t epoch) {
   cudaStream_t s = c->stream;
-  c->lb_offs.reserve(2 * cnt + 2);
-  int64_t* counts = c->lb_offs.p + cnt + 1;
-  if (cnt > 0)
-    MF_K(k_row_counts<<<grid_for(cnt), kTB, 0, s>>>(c->view(), list, cnt, kind, c->rowcid.p, ns, c->bval.p, epoch,
-                                                   c->v2i.p, counts));
-  scan_exclusive_i64(counts, c->lb_offs.p, cnt, c->ws, s);
+  c->lb_offs.reserve(cnt + 1);
+  scan_exclusive_with(RowCounts{c->view(), list, kind, c->rowcid.p, ns, c->bval.p, epoch, c->v2i.p}, c->lb_offs.p, cnt,
+                      c->ws, s);
 }
 
 // row_offsets into caller-given buffers on a given stream (the fronts).
 void row_offsets_into(mf_ctx* c, const int32_t* list, int64_t cnt, DBuf<int64_t>& offs, Scratch& ws,
                       cudaStream_t s) {
-  offs.reserve(2 * cnt + 2);
-  int64_t* counts = offs.p + cnt + 1;
-  if (cnt > 0)
-    MF_K(k_row_counts<<<grid_for(cnt), kTB, 0, s>>>(c->view(), list, cnt, kCntAll, c->rowcid.p, 0, c->bval.p, 0,
-                                                   c->v2i.p, counts));
-  scan_exclusive_i64(counts, offs.p, cnt, ws, s);
+  offs.reserve(cnt + 1);
+  scan_exclusive_with(RowCounts{c->view(), list, kCntAll, c->rowcid.p, 0, c->bval.p, 0, c->v2i.p}, offs.p, cnt, ws, s);
 }
 
 // Buffers of both fronts at their largest sizes for a batch of m updates, so
