@@ -190,7 +190,7 @@ typedef struct mf_tuning {
                              exact 2-hop sizes cache (default 2048; the threshold used is
                              max(heavy_min, n/256)) */
   int64_t big_threshold;  /* hop-2 volume above which the insertion rule's search for the first
-                             eligible vertex goes to the grid-wide kernel (default 256) */
+                             eligible vertex goes to the grid-wide kernel (default 64) */
   int64_t first_bound;    /* row positions the warp level of the first-cluster-id search covers
                              before long rows go to the chunk level (default 256, at least 8) */
   int64_t cand_push;      /* 0: on graphs with symmetric sorted rows, the candidate rows' cluster ids
@@ -375,6 +375,8 @@ typedef struct mf_batched_opts {
   int64_t max_cta_updates;    /* batches of at most this many lines take the kernel (default 8192) */
   int32_t max_cta_vertices;   /* ... on graphs of at most this many vertices (default 2^20) */
   int use_graph;              /* 1: capture the step as a CUDA graph (default), 0: plain launches */
+  int path_threads;           /* host threads driving the batches above the kernel's limits, each
+                                 graph on its own stream (1..64, default 8) */
 } mf_batched_opts;
 
 typedef struct mf_batched_stats {

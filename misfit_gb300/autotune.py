@@ -1,9 +1,9 @@
 """Autotuner of the batched form (mf_apply_batches).
 
-The batched step has four knobs (mf_batched_opts): the persistent kernel's
-block size, its CTAs per SM, and the two limits that decide which batches it
-carries (lines per batch, vertices per graph) -- everything above them takes
-the multi-launch path concurrently.  Which setting is fastest depends on the
+The batched step's knobs (mf_batched_opts): the persistent kernel's block
+size, its CTAs per SM, the two limits that decide which batches it carries
+(lines per batch, vertices per graph) -- everything above them takes the
+multi-launch path concurrently -- and the host threads of that path.  Which setting is fastest depends on the
 GPU and on the mix of graph and batch sizes, so the tuner measures: it runs
 the caller's step once per candidate setting, each time on fresh contexts
 from the same initial state, and keeps the fastest.  Every candidate must
@@ -34,9 +34,11 @@ from . import native
 CACHE_ENV = "MISFIT_GB_AUTOTUNE_CACHE"
 
 # Coordinate search: the batch-size limit first (it moves the most work),
-# then block size and CTAs per SM at the best limit.
+# then block size and CTAs per SM at the best limit, then the host threads
+# of the multi-launch path.
 LIMITS = (2048, 4096, 8192, 16384, 32768)
 SHAPES = ((512, 2), (256, 4), (1024, 1), (256, 2))
+PATH_THREADS = (4, 8, 16)
 
 
 def cache_path():
@@ -119,7 +121,10 @@ def tune_batched(graphs, mis0, batches, use_cache=True):
     run_step(graphs, mis0, batches, native.batched_opts())   # warm-up: library, allocations
     best_limit = min(LIMITS, key=lambda lim: trial(max_cta_updates=lim))
     best_shape = min(SHAPES, key=lambda s: trial(max_cta_updates=best_limit, block=s[0], ctas_per_sm=s[1]))
-    chosen = {"max_cta_updates": best_limit, "block": best_shape[0], "ctas_per_sm": best_shape[1]}
+    best_threads = min(PATH_THREADS, key=lambda t: trial(max_cta_updates=best_limit, block=best_shape[0],
+                                                         ctas_per_sm=best_shape[1], path_threads=t))
+    chosen = {"max_cta_updates": best_limit, "block": best_shape[0], "ctas_per_sm": best_shape[1],
+              "path_threads": best_threads}
     entry = {"opts": chosen, "trials": trials}
     if use_cache:
         cache[key] = entry
@@ -132,7 +137,7 @@ def tune_batched(graphs, mis0, batches, use_cache=True):
 
 # The library's defaults of mf_tuning (a GPU test checks that a new context
 # reports these), and the candidate values, searched one at a time.
-DEFAULT_TUNING = {"pull_long": 2048, "heavy_min": 2048, "big_threshold": 256, "first_bound": 256, "cand_push": 0}
+DEFAULT_TUNING = {"pull_long": 2048, "heavy_min": 2048, "big_threshold": 64, "first_bound": 256, "cand_push": 0}
 PLAIN_KNOBS = (
     ("cand_push", (0, 1)),
     ("big_threshold", (64, 256, 1024, 4096)),

@@ -145,6 +145,7 @@ mf_batched_opts default_opts() {
   o.max_cta_updates = 8192;
   o.max_cta_vertices = 1 << 20;
   o.use_graph = 1;
+  o.path_threads = 8;
   return o;
 }
 
@@ -157,11 +158,10 @@ double host_ms() {
 // host threads, each graph on its own stream, largest first.  Returns the
 // first failure's status (its message in *error).
 int run_path_items(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* const* v, const uint8_t* const* ins,
-                   const int64_t* m, std::vector<int64_t> items, std::string* error) {
+                   const int64_t* m, std::vector<int64_t> items, int threads, std::string* error) {
   if (items.empty()) return MF_OK;
   std::sort(items.begin(), items.end(), [&](int64_t a, int64_t b) { return m[a] > m[b]; });
-  constexpr size_t kMaxThreads = 8;
-  const size_t nt = std::min(kMaxThreads, items.size());
+  const size_t nt = std::min((size_t)std::max(threads, 1), items.size());
   std::mutex mu;
   size_t next = 0;
   int status = MF_OK;
@@ -203,6 +203,7 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
   need(o.ctas_per_sm >= 1 && o.ctas_per_sm <= 32, MF_EINVAL, "ctas_per_sm must be in [1, 32]");
   need(o.max_cta_updates >= 0 && o.max_cta_updates <= cta::kMaxBatchEdges, MF_EINVAL,
        "max_cta_updates must be in [0, 1048576]");
+  need(o.path_threads >= 1 && o.path_threads <= 64, MF_EINVAL, "path_threads must be in [1, 64]");
   mf_batched_stats stats{};
   if (count == 0) {
     if (st) *st = stats;
@@ -404,7 +405,7 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
 
     // the batches above the kernel's limits, on their own streams meanwhile
     std::string path_error;
-    const int path_status = run_path_items(ctxs, u, v, ins, m, path_items, &path_error);
+    const int path_status = run_path_items(ctxs, u, v, ins, m, path_items, o.path_threads, &path_error);
     MF_CUDA(cudaSetDevice(device));
     const cudaError_t se = cudaStreamSynchronize(E.s);
     if (exec) cudaGraphExecDestroy(exec);
@@ -457,7 +458,7 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
     if (path_status != MF_OK) MF_FAIL(path_status, path_error);
   } else {
     std::string path_error;
-    const int r = run_path_items(ctxs, u, v, ins, m, path_items, &path_error);
+    const int r = run_path_items(ctxs, u, v, ins, m, path_items, o.path_threads, &path_error);
     if (r != MF_OK) MF_FAIL(r, path_error);
   }
   stats.wall_ms = host_ms() - t_start;

@@ -635,7 +635,7 @@ struct mf_ctx {
   bool pending = false;
   // load-balancing settings (mf_set_tuning); they move work between kernels,
   // never a result
-  mf_tuning tune = mf_tuning{2048, 2048, 256, 256, 0};
+  mf_tuning tune = mf_tuning{2048, 2048, 64, 256, 0};
 
   mf::GraphView view() const {
     return mf::GraphView{n, nindex.p, nlist.p, live.p, dead.p, aoff.p, aadj.p};

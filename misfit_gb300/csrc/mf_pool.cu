@@ -638,7 +638,8 @@ int mf_pool_set_batching(mf_pool* p, const mf_batched_opts* opts) {
     if (opts) {
       o = *opts;
       need_arg(o.block >= 64 && o.block <= 1024 && o.block % 32 == 0 && o.ctas_per_sm >= 1 && o.ctas_per_sm <= 32 &&
-                   o.max_cta_updates >= 0 && o.max_cta_updates <= mf::kMaxBatchEdges,
+                   o.max_cta_updates >= 0 && o.max_cta_updates <= mf::kMaxBatchEdges && o.path_threads >= 1 &&
+                   o.path_threads <= 64,
                "bad batched options");
     }
     std::lock_guard<std::mutex> lk(p->mu);

@@ -64,7 +64,7 @@ class PoolStats(C.Structure):
 class BatchedOpts(C.Structure):
     _fields_ = [
         ("block", C.c_int), ("ctas_per_sm", C.c_int), ("max_cta_updates", C.c_int64),
-        ("max_cta_vertices", C.c_int32), ("use_graph", C.c_int),
+        ("max_cta_vertices", C.c_int32), ("use_graph", C.c_int), ("path_threads", C.c_int),
     ]
 
 

@@ -14,11 +14,11 @@ class _Opts:
     """Stands in for native.BatchedOpts (no library needed)."""
 
     _fields_ = [("block", None), ("ctas_per_sm", None), ("max_cta_updates", None), ("max_cta_vertices", None),
-                ("use_graph", None)]
+                ("use_graph", None), ("path_threads", None)]
 
     def __init__(self, **kw):
         self.block, self.ctas_per_sm, self.max_cta_updates = 512, 2, 8192
-        self.max_cta_vertices, self.use_graph = 1 << 20, 1
+        self.max_cta_vertices, self.use_graph, self.path_threads = 1 << 20, 1, 8
         for k, v in kw.items():
             setattr(self, k, v)
 
@@ -42,17 +42,19 @@ def _setup(monkeypatch, tmp_path, cost, results=None):
 
 def test_search_keeps_fastest_and_caches(monkeypatch, tmp_path):
     def cost(o):
-        return abs(o.max_cta_updates - 32768) / 1e6 + abs(o.block - 256) / 1e5 + abs(o.ctas_per_sm - 4) / 1e4
+        return (abs(o.max_cta_updates - 32768) / 1e6 + abs(o.block - 256) / 1e5 + abs(o.ctas_per_sm - 4) / 1e4
+                + abs(o.path_threads - 16) / 1e3)
 
     graphs, batches, calls = _setup(monkeypatch, tmp_path, cost)
     opts, rep = autotune.tune_batched(graphs, None, batches)
-    assert (opts.max_cta_updates, opts.block, opts.ctas_per_sm) == (32768, 256, 4)
+    assert (opts.max_cta_updates, opts.block, opts.ctas_per_sm, opts.path_threads) == (32768, 256, 4, 16)
     assert not rep["cached"]
     n_trials = len(calls)
-    assert n_trials == 1 + len(autotune.LIMITS) + len(autotune.SHAPES)   # warm-up + coordinate search
+    # warm-up + coordinate search
+    assert n_trials == 1 + len(autotune.LIMITS) + len(autotune.SHAPES) + len(autotune.PATH_THREADS)
     data = json.load(open(tmp_path / "cache.json"))
     assert list(data) == [autotune.shape_key(graphs, batches)]
-    assert data[rep["key"]]["opts"] == {"max_cta_updates": 32768, "block": 256, "ctas_per_sm": 4}
+    assert data[rep["key"]]["opts"] == {"max_cta_updates": 32768, "block": 256, "ctas_per_sm": 4, "path_threads": 16}
     # the second call with the same shape is served from the cache
     opts2, rep2 = autotune.tune_batched(graphs, None, batches)
     assert rep2["cached"] and len(calls) == n_trials
