@@ -295,12 +295,13 @@ def run_large(args, local):
     deletes and inserts, both endpoints proportional to current degree
     (deletes: uniform over the edges; inserts: endpoints drawn by degree,
     pairs not adjacent in the base graph).  Under the reference's split rule
-    a batch with hub endpoints cuts into thousands of sub-batches, so the
-    leg times a bounded sample: consecutive prefixes of the first batch
-    (1,000 lines, then doubling), each applied as a batch, until the budget
-    of device time is spent; then one more prefix in exact-MIS mode, after
-    which the membership is checked for independence and maximality on the
-    whole graph."""
+    a batch with hub endpoints packs 2-hop lists of tens of millions of
+    entries per seed, so the leg times a bounded sample: consecutive
+    prefixes of the first batch (25 lines, then doubling), each applied as a
+    batch, while the next prefix's expected device time fits the budget;
+    then one more 25-line prefix in exact-MIS mode, after which the
+    membership is checked for independence and maximality on the whole
+    graph."""
     import torch
     from misfit_gb300 import native
     from misfit_gb300 import workloads as W
@@ -344,16 +345,23 @@ def run_large(args, local):
         u, v, ins = toggles.next_batch(args.large_batch, endpoints="preferential")
         del toggles
         torch.cuda.empty_cache()
-        g.profile(2)
+        g.profile(1)
         g.profile_reset()
-        done, dev_ms, sub, chunk, samples = 0, 0.0, 0, 1000, []
-        while done < u.size and dev_ms < args.large_seconds * 1e3:
+        budget_ms = args.large_seconds * 1e3
+        done, dev_ms, sub, chunk, samples = 0, 0.0, 0, 25, []
+        while done < u.size:
             k = min(chunk, u.size - done)
+            if samples:
+                # the next prefix's expected time from the last one's per-line time
+                last = samples[-1]
+                if dev_ms + last["device_ms"] / last["lines"] * k > budget_ms:
+                    break
             g.apply_batch(u[done:done + k], v[done:done + k], ins[done:done + k])
             st = g.stats()
             dev_ms += st["device_ms"]
             sub += st["sub_batches"]
-            samples.append({"lines": k, "device_ms": round(st["device_ms"], 3), "sub_batches": st["sub_batches"]})
+            samples.append({"lines": k, "device_ms": round(st["device_ms"], 3), "sub_batches": st["sub_batches"],
+                            "max_csr": st["max_csr"]})
             done += k
             chunk *= 2
         prof = g.profile_read()
@@ -362,7 +370,9 @@ def run_large(args, local):
         out.update({"value": rate, "unit": UNIT, "lines_timed": done, "device_ms": dev_ms,
                     "sub_batches": sub, "sub_batches_per_line": sub / max(done, 1), "samples": samples,
                     "projected_s_per_batch": args.large_batch / rate,
-                    "timing": "library CUDA events per applied prefix (host-buffer batches)"})
+                    "stage_ms": {s: round(x[0], 1) for s, x in prof.items() if x[0] > 0},
+                    "timing": "library CUDA events per applied prefix (host-buffer batches); prefixes of 25 "
+                              "lines, doubling, while the next one's expected device time fits the budget"})
         ms, calls, nbytes = prof["push_hop"]
         peak, peak_kind = measured_peaks()
         if ms > 0:
@@ -370,7 +380,7 @@ def run_large(args, local):
             out["roofline"] = {"bound": "hbm", "kernel": "k_lb_push_hop", "achieved": ach, "peak": peak,
                                "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind, "launches": int(calls)}
         # exact-MIS mode on one more prefix, then the checks on the whole graph
-        k = min(max(1000, done // 4), u.size - done)
+        k = min(25, u.size - done)
         if k > 0:
             g.set_exact(True)
             g.apply_batch(u[done:done + k], v[done:done + k], ins[done:done + k])

@@ -59,6 +59,14 @@ double ktime_now() {
 }
 }  // namespace
 
+bool pdl_on() {
+  static const bool on = [] {
+    const char* e = std::getenv("MISFIT_GB_PDL");
+    return !(e != nullptr && std::strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 bool ktime_on() {
   static const bool on = [] {
     const char* e = std::getenv("MISFIT_GB_KTIME");

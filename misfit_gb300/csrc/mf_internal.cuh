@@ -17,6 +17,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -80,6 +81,37 @@ void ktime_end(const char* launch_text, double t0);
     ::mf::note_launch();                                       \
     if (kt_) ::mf::ktime_end(#__VA_ARGS__, t_);                \
   } while (0)
+
+// ---- programmatic dependent launch -----------------------------------------
+// The kernels of a sub-batch form one long chain on the context's stream.
+// Launched with launch_pdl, a kernel's CTAs may be scheduled while its
+// predecessor's last CTAs still run; they stop at pdl_wait() (PTX
+// griddepcontrol.wait), which returns once every prerequisite grid has
+// completed and its memory writes are visible.  So a kernel launched this way
+// must call pdl_wait() before it touches anything its predecessor writes; the
+// kernels that do call it first.  In a kernel launched the ordinary way it
+// returns at once.  MISFIT_GB_PDL=0 turns the attribute off.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel of the chain be scheduled once every CTA of this one
+// has executed it (its CTAs then wait in pdl_wait for this grid to finish).
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+bool pdl_on();
+
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_on() ? 1 : 0;
+  MF_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
 
 // Stages timed by the optional profiler (mf_profile_enable).
 enum Stage : int {

@@ -179,6 +179,8 @@ __global__ void k_plan_seed_ends(const int64_t* cuts, const unsigned long long* 
 
 // Seeds of one sub-batch into their rows: seeds[i], v2i[seeds[i]] = i.
 __global__ void k_seed_rows(const int32_t* seeds_all, int64_t ns, int32_t* seeds, int32_t* v2i) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ns) return;
   const int32_t x = seeds_all[i];
@@ -244,6 +246,8 @@ constexpr int kBitsWords = kBitsThreads * kBitsPerThread;       // words per blo
 __global__ void __launch_bounds__(kLbThreads, MF_LB_MIN_BLOCKS) k_lb_hop1_bound(GraphView g, const int32_t* deg, const int32_t* seeds,
                                                               const int64_t* offs, int64_t ns, uint32_t* hbits,
                                                               unsigned long long* uacc, unsigned long long* work) {
+  pdl_wait();
+  pdl_trigger();
   int64_t cur = -1;
   unsigned long long acc = 0;
   const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
@@ -261,6 +265,8 @@ __global__ void __launch_bounds__(kLbThreads, MF_LB_MIN_BLOCKS) k_lb_hop1_bound(
 }
 
 __global__ void k_seed_bits(const int32_t* seeds, int64_t ns, uint32_t* sbits) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < ns) atomicOr(sbits + (seeds[i] >> 5), 1u << (seeds[i] & 31));
 }
@@ -303,6 +309,8 @@ __device__ __forceinline__ int64_t bits_block_scan(int64_t x, int64_t* s_warp, i
 
 __global__ void __launch_bounds__(kBitsThreads) k_bits_reduce(const uint32_t* hbits, const uint32_t* sbits,
                                                               int64_t words, int64_t* block_sums) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ int64_t s_warp[kBitsThreads / 32 + 1];
   const int64_t w0 = (int64_t)blockIdx.x * kBitsWords + (int64_t)threadIdx.x * kBitsPerThread;
   int64_t total = 0;
@@ -314,6 +322,8 @@ __global__ void __launch_bounds__(kBitsThreads) k_bits_reduce(const uint32_t* hb
 // the grand total goes to *total.
 __global__ void __launch_bounds__(kBitsThreads) k_bits_scan_sums(int64_t* block_sums, int64_t nblocks,
                                                                  int64_t* total) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ int64_t s_warp[kBitsThreads / 32 + 1];
   int64_t carry = 0;
   for (int64_t b0 = 0; b0 < nblocks; b0 += kBitsThreads) {
@@ -331,6 +341,8 @@ __global__ void __launch_bounds__(kBitsThreads) k_bits_compact(const uint32_t* h
                                                                int64_t words, const int64_t* block_offs, int64_t cap,
                                                                int64_t ns, int32_t* hlist, int32_t* cands,
                                                                int32_t* v2i) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ int64_t s_warp[kBitsThreads / 32 + 1];
   const int64_t w0 = (int64_t)blockIdx.x * kBitsWords + (int64_t)threadIdx.x * kBitsPerThread;
   int64_t total = 0;
@@ -360,6 +372,8 @@ __global__ void __launch_bounds__(kBitsThreads) k_bits_compact(const uint32_t* h
 // Row map of the candidates (rows ns .. ns + nct - 1), once the previous
 // sub-batch has cleared its rows.
 __global__ void k_cand_v2i(const int32_t* cands, int64_t nct, int64_t ns, int32_t* v2i) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nct) v2i[cands[i]] = (int32_t)(ns + i);
 }
@@ -376,6 +390,8 @@ __global__ void k_bound_finish(GraphView g, const int32_t* seeds, int64_t ns, co
                                const int64_t* hop_counts, int64_t capc, const unsigned long long* uacc,
                                const int64_t* n2cache, const uint32_t* n2stamp, const int64_t* n2bound,
                                const uint32_t* n2bstamp, uint32_t stamp, unsigned long long* out) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t nct = min((int64_t)(*hop_counts & 0xffffffffll), capc);
   const int64_t rows = ns + nct;
   unsigned long long b = 0;
@@ -748,6 +764,8 @@ struct HasCidBit {
 };
 
 __global__ void k_cid_bits(const int32_t* cid, int32_t n, uint32_t* bits) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool set = i < n && cid[i] != -1;
   const unsigned m = __ballot_sync(0xffffffffu, set);
@@ -856,6 +874,8 @@ struct FirstQueues {
 template <class P>
 __global__ void k_first_probe(GraphView g, const int32_t* list, const unsigned long long* dcnt, P pred,
                               unsigned long long* firstpos, FirstQueues q) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t cnt = (int64_t)*dcnt;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t x = list[i];
@@ -881,6 +901,8 @@ __global__ void k_first_probe(GraphView g, const int32_t* list, const unsigned l
 
 template <class P>
 __global__ void k_first_warp(GraphView g, P pred, unsigned long long* firstpos, FirstQueues q) {
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x & 31;
   const int64_t nmid = (int64_t)*q.mid_count;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -901,6 +923,8 @@ __global__ void k_first_warp(GraphView g, P pred, unsigned long long* firstpos, 
 
 template <class P>
 __global__ void k_first_chunks(GraphView g, P pred, unsigned long long* firstpos, FirstQueues q) {
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x & 31;
   const unsigned long long pk = *q.rest.packed;
   const int64_t rows = (int64_t)(pk >> kChunkShift), chunks = (int64_t)(pk & kChunkMask);
@@ -930,6 +954,8 @@ __global__ void k_first_chunks(GraphView g, P pred, unsigned long long* firstpos
 __global__ void k_row_skip(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, const int32_t* cid,
                            int32_t* rowcid, uint8_t* creates, int32_t* live_i, int32_t* live_v,
                            unsigned long long* nlive) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ns + nct) return;
   const int32_t x = i < ns ? seeds[i] : cands[i - ns];
@@ -949,6 +975,8 @@ __global__ void k_live_decide(GraphView g, const int32_t* live_i, const int32_t*
                               const unsigned long long* dcnt, int64_t ns, const unsigned long long* firstpos,
                               const int32_t* cid, int32_t* rowcid, uint8_t* creates, const int32_t* seeds,
                               int32_t* need, int32_t* needv, unsigned long long* nneed, ChunkQueue mq) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t cnt = (int64_t)*dcnt;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t i = live_i[k];
@@ -978,6 +1006,8 @@ __global__ void k_live_decide(GraphView g, const int32_t* live_i, const int32_t*
 // with an id.  f1 is computed for the neighbours of the seeds that need it.
 __global__ void k_mark_need(GraphView g, ChunkQueue mq, uint32_t epoch, uint32_t* nmark, int32_t* list,
                             unsigned long long* count) {
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x & 31;
   const unsigned long long pk = *mq.packed;
   const int64_t rows = (int64_t)(pk >> kChunkShift), chunks = (int64_t)(pk & kChunkMask);
@@ -997,6 +1027,8 @@ __global__ void k_mark_need(GraphView g, ChunkQueue mq, uint32_t epoch, uint32_t
 
 __global__ void k_f1_finish(GraphView g, const int32_t* list, const unsigned long long* dcnt,
                             const unsigned long long* firstpos, const int32_t* cid, int32_t* f1) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t cnt = (int64_t)*dcnt;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t x = list[i];
@@ -1013,6 +1045,8 @@ struct HasF1 {    // the element's own row holds an element with a cluster id
 __global__ void k_need_decide(GraphView g, const int32_t* need, const int32_t* needv, const unsigned long long* dcnt,
                               const unsigned long long* firstpos, const int32_t* f1, int32_t* rowcid,
                               uint8_t* creates) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t cnt = (int64_t)*dcnt;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x) {
     const unsigned long long fp = firstpos[k];
@@ -1025,6 +1059,8 @@ __global__ void k_need_decide(GraphView g, const int32_t* need, const int32_t* n
 }
 
 __global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid) {
+  pdl_wait();
+  pdl_trigger();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < rows && rowcid[i] == -1) rowcid[i] = (int32_t)pos[i];
 }
@@ -1041,12 +1077,16 @@ __device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag) 
 
 // Phase 1: bval[y] = max tag of the non-skipped seed rows with y in {s} u row(s).
 __global__ void k_seed_self(const int32_t* seeds, int64_t ns, const int32_t* rowcid, uint32_t epoch, uint32_t* bval) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < ns && rowcid[i] != kSkip) atomicMax(bval + seeds[i], (epoch << kRowBits) | (uint32_t)i);
 }
 
 __global__ void k_lb_push_seed(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t epoch,
                                uint32_t* bval, unsigned long long* work) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t vis = lb_rows(g, seeds, offs, ns, [&](int64_t i, int32_t, int32_t y) {
     push_w(bval, y, (epoch << kRowBits) | (uint32_t)i);
   });
@@ -1058,6 +1098,8 @@ __global__ void k_lb_push_seed(GraphView g, const int32_t* seeds, const int64_t*
 // Phase 2: wval[y] = max over x with y in {x} u row(x) of bval[x] (the 2-hop
 // reach of the seed rows), and the candidate rows' own tags over row(c).
 __global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, const uint32_t* bval, uint32_t* wval) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cnt) return;
   const int32_t x = list[i];
@@ -1068,6 +1110,8 @@ __global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, co
 __global__ void __launch_bounds__(kLbThreads, MF_LB_MIN_BLOCKS) k_lb_push_hop(GraphView g, const int32_t* list, const int64_t* offs,
                                                             int64_t cnt, uint32_t epoch, const uint32_t* bval,
                                                             uint32_t* wval, unsigned long long* work) {
+  pdl_wait();
+  pdl_trigger();
   // the row's tag is staged once per row with the row's metadata
   const int64_t vis = lb_rows_aux(
       g, list, offs, cnt, [&](int64_t, int32_t x) { return bval[x]; },
@@ -1077,6 +1121,8 @@ __global__ void __launch_bounds__(kLbThreads, MF_LB_MIN_BLOCKS) k_lb_push_hop(Gr
 
 __global__ void k_lb_push_cand(GraphView g, const int32_t* cands, const int64_t* offs, int64_t nct, int64_t ns,
                                uint32_t epoch, uint32_t* wval, unsigned long long* work) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t vis = lb_rows(g, cands, offs, nct, [&](int64_t i, int32_t, int32_t y) {
     push_w(wval, y, (epoch << kRowBits) | (uint32_t)(ns + i));
   });
@@ -1115,6 +1161,8 @@ __device__ __forceinline__ bool pull_nonskip(const PullArgs& a, int32_t c) {
 
 // Bits of the non-skipped candidates (rows ns .. ns+nct-1) for the pull pass.
 __global__ void k_cand_bits(const int32_t* cands, int64_t nct, int64_t ns, const int32_t* rowcid, uint32_t* bits) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nct || rowcid[ns + i] == kSkip) return;
   const int32_t c = cands[i];
@@ -1131,6 +1179,8 @@ __device__ __forceinline__ void pull_finish(const PullArgs& a, int32_t y, int32_
 }
 
 __global__ void k_pull_cand(PullArgs a) {
+  pdl_wait();
+  pdl_trigger();
   const GraphView& g = a.g;
   const int64_t yi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t visited = 0;
@@ -1170,6 +1220,8 @@ __global__ void k_pull_cand(PullArgs a) {
 // first of them (lowest lane) that is live and non-skipped is the answer,
 // and a prefix shorter than 32 lanes ends the walk.
 __global__ void k_pull_cand_long(PullArgs a) {
+  pdl_wait();
+  pdl_trigger();
   const GraphView& g = a.g;
   const int lane = threadIdx.x & 31;
   const int64_t nl = (int64_t)*a.nlong;
@@ -1211,6 +1263,8 @@ __global__ void k_pull_cand_long(PullArgs a) {
 
 // cid[y] = id of the row that wrote y last, for every y tagged this epoch.
 __global__ void k_finalize_all(const uint32_t* wval, int32_t n, uint32_t epoch, const int32_t* rowcid, int32_t* cid) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t x0 = q * 4;
   if (x0 >= n) return;
@@ -1234,6 +1288,8 @@ __global__ void k_finalize_all(const uint32_t* wval, int32_t n, uint32_t epoch, 
 // at or beyond min(cluster_count, MAX_BATCH_SIZE) are dropped.
 __global__ void k_assign(const int32_t* u, const int32_t* v, int64_t p, int64_t len, const int32_t* cid,
                          const int64_t* ccp, uint64_t* keys, uint32_t* vals, unsigned long long* count) {
+  pdl_wait();
+  pdl_trigger();
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= len) return;
   const int64_t limit = min(*ccp, kMaxBatchEdges);
@@ -1707,6 +1763,8 @@ __device__ void big_prep_block(const SpecArgs& a, int64_t* chunk_pre, unsigned l
 // records before it counts itself done.
 __global__ void k_spec_eval(SpecArgs a, int64_t* chunk_pre, unsigned long long* best, unsigned long long* queue,
                             unsigned int* done) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t wi = warp_id();
   if (wi < a.cnt - a.p0) {
     const int lane = threadIdx.x & 31;
@@ -1757,6 +1815,8 @@ __global__ void k_spec_eval(SpecArgs a, int64_t* chunk_pre, unsigned long long* 
 // smallest eligible position.
 __global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_t* chunk_pre,
                                                         unsigned long long* best, unsigned long long* queue) {
+  pdl_wait();
+  pdl_trigger();
   const GraphView& g = a.g;
   const int64_t nbig = (int64_t)*a.big_count;
   const int64_t total = chunk_pre[nbig];
@@ -1900,6 +1960,8 @@ __device__ void big_finalize_one(const SpecArgs& a, const unsigned long long* be
 }
 
 __global__ void k_big_finalize(SpecArgs a, const unsigned long long* best) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < (int64_t)*a.big_count) big_finalize_one(a, best, i);
 }
@@ -2012,6 +2074,8 @@ __global__ void __launch_bounds__(kRoundThreads) k_spec_round(const int32_t* n0,
                                                               int64_t nview_old, uint8_t* m,
                                                               unsigned long long* out, SpecArgs sa,
                                                               const unsigned long long* best) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ uint64_t s_keys[kRoundWrites];
   __shared__ uint32_t s_vals[kRoundWrites];
   __shared__ int s_warp[33];
@@ -2113,6 +2177,8 @@ __global__ void __launch_bounds__(kRoundThreads) k_spec_round(const int32_t* n0,
 
 __global__ void k_clear(const int32_t* seeds, int64_t ns, const int32_t* cands, int64_t nct, int32_t* cid,
                         int32_t* v2i) {
+  pdl_wait();
+  pdl_trigger();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ns + nct) return;
   const int32_t x = i < ns ? seeds[i] : cands[i - ns];
@@ -2194,15 +2260,15 @@ void front_compute(mf_ctx* c, Front& f, const int32_t* seeds, int64_t ns, cudaSt
   MF_CUDA(cudaMemsetAsync(f.uacc.p, 0, sizeof(unsigned long long) * (size_t)std::max<int64_t>(ns, 1), st));
   MF_CUDA(cudaMemsetAsync(f.cnt.p + 1, 0, sizeof(int64_t), st));
   row_offsets_into(c, seeds, ns, f.lb_offs, f.ws, st);
-  MF_K(k_lb_hop1_bound<<<lb_grid(c, k_lb_hop1_bound), kTB, 0, st>>>(g, c->deg.p, seeds, f.lb_offs.p, ns, hbits, f.uacc.p,
+  MF_K(launch_pdl(k_lb_hop1_bound, lb_grid(c, k_lb_hop1_bound), kTB, 0, st, g, c->deg.p, seeds, f.lb_offs.p, ns, hbits, f.uacc.p,
                                                                     c->work.p + 2 * kStHop1));
-  if (ns > 0) MF_K(k_seed_bits<<<grid_for(ns), kTB, 0, st>>>(seeds, ns, sbits));
+  if (ns > 0) MF_K(launch_pdl(k_seed_bits, grid_for(ns), kTB, 0, st, seeds, ns, sbits));
   const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
-  MF_K(k_bits_reduce<<<(unsigned)bblocks, kBitsThreads, 0, st>>>(hbits, sbits, words, f.bits_sums.p));
-  MF_K(k_bits_scan_sums<<<1, kBitsThreads, 0, st>>>(f.bits_sums.p, bblocks, f.cnt.p));
-  MF_K(k_bits_compact<<<(unsigned)bblocks, kBitsThreads, 0, st>>>(hbits, sbits, words, f.bits_sums.p, capc, ns,
+  MF_K(launch_pdl(k_bits_reduce, (unsigned)bblocks, kBitsThreads, 0, st, hbits, sbits, words, f.bits_sums.p));
+  MF_K(launch_pdl(k_bits_scan_sums, 1, kBitsThreads, 0, st, f.bits_sums.p, bblocks, f.cnt.p));
+  MF_K(launch_pdl(k_bits_compact, (unsigned)bblocks, kBitsThreads, 0, st, hbits, sbits, words, f.bits_sums.p, capc, ns,
                                                                   f.hlist.p, f.cands.p, nullptr));
-  MF_K(k_bound_finish<<<lb_grid(c, k_bound_finish), kTB, 0, st>>>(
+  MF_K(launch_pdl(k_bound_finish, lb_grid(c, k_bound_finish), kTB, 0, st, 
       g, seeds, ns, f.cands.p, f.cnt.p, capc, f.uacc.p, c->n2cache.p, c->n2stamp.p, c->n2bound.p, c->n2bstamp.p,
       c->n2batch, reinterpret_cast<unsigned long long*>(f.cnt.p + 1)));
 }
@@ -2385,9 +2451,9 @@ void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, 
   const FirstQueues q{c->un_idx.p, c->un_v.p, ucnt + 48, ChunkQueue{c->rq_idx.p, c->rq_v.p, c->un_cnt.p, ucnt + 49},
                       std::max<int64_t>(c->tune.first_bound, kProbe)};
   const GraphView g = c->view();
-  MF_K(k_first_probe<<<lb_grid(c, k_first_probe<P>), kTB, 0, s>>>(g, list, dcnt, pred, c->fpos.p, q));
-  MF_K(k_first_warp<<<lb_grid(c, k_first_warp<P>), kTB, 0, s>>>(g, pred, c->fpos.p, q));
-  MF_K(k_first_chunks<<<lb_grid(c, k_first_chunks<P>), kTB, 0, s>>>(g, pred, c->fpos.p, q));
+  MF_K(launch_pdl(k_first_probe<P>, lb_grid(c, k_first_probe<P>), kTB, 0, s, g, list, dcnt, pred, c->fpos.p, q));
+  MF_K(launch_pdl(k_first_warp<P>, lb_grid(c, k_first_warp<P>), kTB, 0, s, g, pred, c->fpos.p, q));
+  MF_K(launch_pdl(k_first_chunks<P>, lb_grid(c, k_first_chunks<P>), kTB, 0, s, g, pred, c->fpos.p, q));
   if (debug_counters()) {
     unsigned long long v[3] = {0, 0, 0};
     MF_CUDA(cudaStreamSynchronize(s));
@@ -2479,15 +2545,15 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
                c->tune.big_threshold, ucnt + 24, c->big_pos.p, c->big_r.p, c->big_off.p, c->big_nr.p,
                c->big_pre.p, ucnt + 25, c->big_pre.cap};
     rsc.emplace(c, kStRepair);
-    MF_K(k_spec_eval<<<warps_grid(pending), kTB, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26,
+    MF_K(launch_pdl(k_spec_eval, warps_grid(pending), kTB, 0, s, a, c->big_chunks.p, c->big_best.p, ucnt + 26,
                                                           reinterpret_cast<unsigned int*>(ucnt + 29)));
     rsc.emplace(c, kStRepairBig);
-    MF_K(k_big_scan<<<(unsigned)c->big_grid, kBigChunk, 0, s>>>(a, c->big_chunks.p, c->big_best.p, ucnt + 26));
+    MF_K(launch_pdl(k_big_scan, (unsigned)c->big_grid, kBigChunk, 0, s, a, c->big_chunks.p, c->big_best.p, ucnt + 26));
     rsc.emplace(c, kStRepair);
     if (pending <= kRoundCap) {
       // small round: one CTA finalizes the grid-wide searches and finishes
       // the round, one host round trip
-      MF_K(k_spec_round<<<1, kRoundThreads, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0, nproc, c->bins.p,
+      MF_K(launch_pdl(k_spec_round, 1, kRoundThreads, 0, s, c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0, nproc, c->bins.p,
                                                     p, order, c->rp_keys.p, c->rp_vals.p, nview, c->mis.p, ucnt + 20,
                                                     a, c->big_best.p));
       MF_CUDA(cudaMemcpyAsync(h + 20, c->counters.p + 20, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
@@ -2509,7 +2575,7 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
       p0 = f + 1;
       continue;
     }
-    MF_K(k_big_finalize<<<grid_for(pending), kTB, 0, s>>>(a, c->big_best.p));
+    MF_K(launch_pdl(k_big_finalize, grid_for(pending), kTB, 0, s, a, c->big_best.p));
     h[20] = (int64_t)nproc;
     MF_CUDA(cudaMemcpyAsync(c->counters.p + 20, h + 20, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     MF_K(k_spec_first_change<<<grid_for(pending), kTB, 0, s>>>(c->rp_n0.p, c->rp_n1.p, c->rp_w0.p, c->rp_w1.p, p0,
@@ -2671,7 +2737,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     // ---- seeds (first appearance) of this sub-batch into their rows
     sc.emplace(c, kStSeeds);
     if (ns > 0)
-      MF_K(k_seed_rows<<<grid_for(ns), kTB, 0, s>>>(c->seeds_all.p + seed_base, ns, c->seeds.p, c->v2i.p));
+      MF_K(launch_pdl(k_seed_rows, grid_for(ns), kTB, 0, s, c->seeds_all.p + seed_base, ns, c->seeds.p, c->v2i.p));
     const int64_t max_before = c->max_csr;
 
     // ---- hop-1 set and size bound: this sub-batch's front (computed on the
@@ -2697,7 +2763,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     const int64_t capc = std::max<int64_t>(0, kMaxRows - ns);
     const int64_t nct = std::min<int64_t>(h[3], capc);
     const int64_t rows = ns + nct;
-    if (nct > 0) MF_K(k_cand_v2i<<<grid_for(nct), kTB, 0, s>>>(c->cands.p, nct, ns, c->v2i.p));
+    if (nct > 0) MF_K(launch_pdl(k_cand_v2i, grid_for(nct), kTB, 0, s, c->cands.p, nct, ns, c->v2i.p));
     int64_t packed = -1;
     const bool exact = h[4] >= c->max_csr;
     if (exact) {
@@ -2774,44 +2840,44 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t) * 3, s));   // live rows, need seeds, their neighbours
     MF_CUDA(cudaMemsetAsync(cnt + 50, 0, sizeof(int64_t), s));       // chunk queue of the need seeds' rows
     const ChunkQueue mq{c->mq_idx.p, c->mq_v.p, c->mq_base.p, ucnt + 50};
-    MF_K(k_row_skip<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->rowcid.p,
+    MF_K(launch_pdl(k_row_skip, grid_for(rows), kTB, 0, s, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->rowcid.p,
                                                     c->creates.p, c->live_i.p, c->live_v.p, ucnt + 33));
     c->cidbits.reserve(((int64_t)n + 31) / 32 + 1);
-    MF_K(k_cid_bits<<<grid_for(((int64_t)n + 31) / 32 * 32), kTB, 0, s>>>(c->cid.p, n, c->cidbits.p));
+    MF_K(launch_pdl(k_cid_bits, grid_for(((int64_t)n + 31) / 32 * 32), kTB, 0, s, c->cid.p, n, c->cidbits.p));
     const HasCidBit has_cid{c->cidbits.p};
     first_hits(c, c->live_v.p, ucnt + 33, rows, has_cid);
-    MF_K(k_live_decide<<<lb_grid(c, k_live_decide), kTB, 0, s>>>(g, c->live_i.p, c->live_v.p, ucnt + 33, ns,
+    MF_K(launch_pdl(k_live_decide, lb_grid(c, k_live_decide), kTB, 0, s, g, c->live_i.p, c->live_v.p, ucnt + 33, ns,
                                                                  c->fpos.p, c->cid.p, c->rowcid.p, c->creates.p,
                                                                  c->seeds.p, c->need.p, c->needv.p, ucnt + 34, mq));
     sc.emplace(c, kStFirstNeed);
-    MF_K(k_mark_need<<<lb_grid(c, k_mark_need), kTB, 0, s>>>(g, mq, ep, c->nmark.p, c->nlist_need.p, ucnt + 35));
+    MF_K(launch_pdl(k_mark_need, lb_grid(c, k_mark_need), kTB, 0, s, g, mq, ep, c->nmark.p, c->nlist_need.p, ucnt + 35));
     first_hits(c, c->nlist_need.p, ucnt + 35, n, has_cid);
-    MF_K(k_f1_finish<<<lb_grid(c, k_f1_finish), kTB, 0, s>>>(g, c->nlist_need.p, ucnt + 35, c->fpos.p, c->cid.p,
+    MF_K(launch_pdl(k_f1_finish, lb_grid(c, k_f1_finish), kTB, 0, s, g, c->nlist_need.p, ucnt + 35, c->fpos.p, c->cid.p,
                                                              c->f1.p));
     first_hits(c, c->needv.p, ucnt + 34, ns, HasF1{c->f1.p});
-    MF_K(k_need_decide<<<lb_grid(c, k_need_decide), kTB, 0, s>>>(g, c->need.p, c->needv.p, ucnt + 34, c->fpos.p,
+    MF_K(launch_pdl(k_need_decide, lb_grid(c, k_need_decide), kTB, 0, s, g, c->need.p, c->needv.p, ucnt + 34, c->fpos.p,
                                                                  c->f1.p, c->rowcid.p, c->creates.p));
     scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
-    MF_K(k_new_ids<<<grid_for(rows), kTB, 0, s>>>(rows, c->i64b.p, c->rowcid.p));
+    MF_K(launch_pdl(k_new_ids, grid_for(rows), kTB, 0, s, rows, c->i64b.p, c->rowcid.p));
     MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     sc.emplace(c, kStPush);
     unsigned long long* wk_extra = c->work.p + 2 * kStCount;   // [0] seed, [1] hop, [2] candidate pushes
-    MF_K(k_seed_self<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
+    MF_K(launch_pdl(k_seed_self, grid_for(ns), kTB, 0, s, c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedRows, ns, ep);
-    MF_K(k_lb_push_seed<<<lb_grid(c, k_lb_push_seed), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk_extra + 0));
-    MF_K(k_self_push<<<grid_for(ns), kTB, 0, s>>>(c->seeds.p, ns, ep, c->bval.p, c->wval.p));
-    MF_K(k_self_push<<<grid_for(nh), kTB, 0, s>>>(c->hlist.p, nh, ep, c->bval.p, c->wval.p));
+    MF_K(launch_pdl(k_lb_push_seed, lb_grid(c, k_lb_push_seed), kTB, 0, s, g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk_extra + 0));
+    MF_K(launch_pdl(k_self_push, grid_for(ns), kTB, 0, s, c->seeds.p, ns, ep, c->bval.p, c->wval.p));
+    MF_K(launch_pdl(k_self_push, grid_for(nh), kTB, 0, s, c->hlist.p, nh, ep, c->bval.p, c->wval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedPushers, ns, ep);
     const unsigned long long dbg0 = debug_launches() ? debug_counter(c, wk_extra + 1) : 0;
     sc.emplace(c, kStPushHop);
-    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p,
+    MF_K(launch_pdl(k_lb_push_hop, lb_grid(c, k_lb_push_hop), kTB, 0, s, g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p,
                                                                  c->wval.p, wk_extra + 1));
     sc.emplace(c, kStPush);
     if (debug_launches()) debug_push_hop(c, wk_extra + 1, dbg0);
     row_offsets(c, c->hlist.p, nh, kCntHopPushers, ns, ep);
     const unsigned long long dbg1 = debug_launches() ? debug_counter(c, wk_extra + 1) : 0;
     sc.emplace(c, kStPushHop);
-    MF_K(k_lb_push_hop<<<lb_grid(c, k_lb_push_hop), kTB, 0, s>>>(g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p,
+    MF_K(launch_pdl(k_lb_push_hop, lb_grid(c, k_lb_push_hop), kTB, 0, s, g, c->hlist.p, c->lb_offs.p, nh, ep, c->bval.p,
                                                                  c->wval.p, wk_extra + 1));
     sc.emplace(c, kStPush);
     if (debug_launches()) debug_push_hop(c, wk_extra + 1, dbg1);
@@ -2823,16 +2889,16 @@ void process_batch(mf_ctx* c, int64_t m) {
       MF_CUDA(cudaMemsetAsync(c->ncbits.p, 0, sizeof(uint32_t) * (size_t)nwords, s));
       MF_CUDA(cudaMemsetAsync(cnt + 36, 0, sizeof(int64_t), s));
       if (nct > 0)
-        MF_K(k_cand_bits<<<grid_for(nct), kTB, 0, s>>>(c->cands.p, nct, ns, c->rowcid.p, c->ncbits.p));
+        MF_K(launch_pdl(k_cand_bits, grid_for(nct), kTB, 0, s, c->cands.p, nct, ns, c->rowcid.p, c->ncbits.p));
       const PullArgs pa{g,  c->v2i.p, c->rowcid.p, c->ncbits.p, ns, c->wval.p, ep, c->cid.p, c->pull_long.p,
                         ucnt + 36, wk_extra + 2, c->tune.pull_long};
-      MF_K(k_pull_cand<<<grid_for(n), kTB, 0, s>>>(pa));
-      MF_K(k_pull_cand_long<<<lb_grid(c, k_pull_cand_long), kTB, 0, s>>>(pa));
+      MF_K(launch_pdl(k_pull_cand, grid_for(n), kTB, 0, s, pa));
+      MF_K(launch_pdl(k_pull_cand_long, lb_grid(c, k_pull_cand_long), kTB, 0, s, pa));
     } else {
       row_offsets(c, c->cands.p, nct, kCntCandRows, ns, ep);
-      MF_K(k_lb_push_cand<<<lb_grid(c, k_lb_push_cand), kTB, 0, s>>>(g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
+      MF_K(launch_pdl(k_lb_push_cand, lb_grid(c, k_lb_push_cand), kTB, 0, s, g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
                                                      wk_extra + 2));
-      MF_K(k_finalize_all<<<grid_for(((int64_t)n + 3) / 4), kTB, 0, s>>>(c->wval.p, n, ep, c->rowcid.p, c->cid.p));
+      MF_K(launch_pdl(k_finalize_all, grid_for(((int64_t)n + 3) / 4), kTB, 0, s, c->wval.p, n, ep, c->rowcid.p, c->cid.p));
     }
     c->touched_total += n;
     MF_CUDA(cudaGetLastError());
@@ -2853,7 +2919,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     // ---- assignment + order (cluster ascending, index descending)
     sc.emplace(c, kStAssign);
     MF_CUDA(cudaMemsetAsync(cnt + 9, 0, sizeof(int64_t), s));
-    MF_K(k_assign<<<grid_for(q - p), kTB, 0, s>>>(c->bu.p, c->bv.p, p, q - p, c->cid.p, c->i64b.p + rows, c->keys.p,
+    MF_K(launch_pdl(k_assign, grid_for(q - p), kTB, 0, s, c->bu.p, c->bv.p, p, q - p, c->cid.p, c->i64b.p + rows, c->keys.p,
                                                   c->vals.p, ucnt + 9));
     MF_CUDA(cudaMemcpyAsync(h + 9, cnt + 9, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
@@ -2877,7 +2943,7 @@ void process_batch(mf_ctx* c, int64_t m) {
 
     // ---- clear (mapped vertices only)
     sc.emplace(c, kStClear);
-    MF_K(k_clear<<<grid_for(rows), kTB, 0, s>>>(c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->v2i.p));
+    MF_K(launch_pdl(k_clear, grid_for(rows), kTB, 0, s, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->v2i.p));
     MF_CUDA(cudaGetLastError());
 
     sc.reset();

@@ -65,6 +65,8 @@ __device__ __forceinline__ int64_t block_exclusive(int64_t v, int64_t* smem_warp
 // One block scans the whole (small) input tile by tile with a carry.
 template <typename L>
 __global__ void k_scan_single(L load, int64_t n, int64_t* out) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ int64_t sw[33];
   int64_t carry = 0;
   for (int64_t base = 0; base < n; base += kTile) {
@@ -104,6 +106,8 @@ constexpr int64_t kLookbackSpin = (int64_t)1 << 22;
 template <typename L>
 __global__ void __launch_bounds__(kThreads) k_scan_lookback(L load, int64_t n, int64_t* out,
                                                             unsigned long long* st, unsigned long long seq) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ int64_t tile[kTile];
   __shared__ int64_t sw[33];
   __shared__ int64_t s_excl;
@@ -190,7 +194,7 @@ void scan_exclusive(L load, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s
     return;
   }
   if (n <= kSingleScanMax) {
-    MF_K(k_scan_single<<<1, kThreads, 0, s>>>(load, n, out));
+    MF_K(launch_pdl(k_scan_single<L>, 1, kThreads, 0, s, load, n, out));
     MF_CUDA(cudaGetLastError());
     return;
   }
@@ -201,7 +205,7 @@ void scan_exclusive(L load, int64_t* out, int64_t n, Scratch& ws, cudaStream_t s
     MF_CUDA(cudaMemsetAsync(ws.scan_status.p, 0, sizeof(unsigned long long) * (size_t)ws.scan_status.cap, s));
   }
   const unsigned long long seq = ++ws.scan_seq;
-  MF_K(k_scan_lookback<<<(unsigned)nb, kThreads, 0, s>>>(load, n, out, ws.scan_status.p, seq));
+  MF_K(launch_pdl(k_scan_lookback<L>, (unsigned)nb, kThreads, 0, s, load, n, out, ws.scan_status.p, seq));
   MF_CUDA(cudaGetLastError());
 }
 
