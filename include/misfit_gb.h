@@ -196,6 +196,10 @@ typedef struct mf_tuning {
   int64_t cand_push;      /* 0: on graphs with symmetric sorted rows, the candidate rows' cluster ids
                              are pulled by every vertex (default); 1: always pushed from the
                              candidate rows, then finalised per vertex */
+  int64_t pull_sizes;     /* exact 2-hop sizes on symmetric graphs: 0 always by the push form (bit
+                             atomics per element of every member's row); 1 (default) the seeds whose
+                             neighbourhood volume pays for it by passes over every row, up to 256
+                             seeds per pass; 2 every seed to size by those passes */
 } mf_tuning;
 int mf_get_tuning(mf_ctx* ctx, mf_tuning* out);
 int mf_set_tuning(mf_ctx* ctx, const mf_tuning* in);

@@ -170,6 +170,13 @@ mf_ctx* new_ctx(int gpu) {
   try {
     mf::noalloc_refresh(gpu);
     if (const char* e = std::getenv("MISFIT_GB_BIG_THRESHOLD")) c->tune.big_threshold = std::max<long long>(0, std::atoll(e));
+    if (const char* e = std::getenv("MISFIT_GB_EXACT_CAPS")) {
+      long long dn = 0, pr = 0;
+      if (std::sscanf(e, "%lld,%lld", &dn, &pr) == 2) {
+        c->exact_cap_dense = std::max<long long>(0, dn);
+        c->exact_cap_pairs = pr > 0 ? std::max<long long>(4096, pr) : 0;
+      }
+    }
     MF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     mf::g_alloc_stream = c->stream;
     // keep freed stream-ordered memory in this process's pool for reuse
@@ -777,9 +784,10 @@ int mf_set_tuning(mf_ctx* c, const mf_tuning* in) {
   return guarded([&] {
     need(c && in, MF_EINVAL, "null argument");
     need(in->pull_long >= 32 && in->heavy_min >= 64 && in->big_threshold >= 0 && in->first_bound >= 8 &&
-             in->first_bound <= ((int64_t)1 << 20) && (in->cand_push == 0 || in->cand_push == 1),
+             in->first_bound <= ((int64_t)1 << 20) && (in->cand_push == 0 || in->cand_push == 1) &&
+             in->pull_sizes >= 0 && in->pull_sizes <= 2,
          MF_EINVAL, "tuning out of range (pull_long >= 32, heavy_min >= 64, big_threshold >= 0, "
-                    "8 <= first_bound <= 2^20, cand_push 0 or 1)");
+                    "8 <= first_bound <= 2^20, cand_push 0 or 1, pull_sizes 0..2)");
     bind(c);
     c->tune = *in;
   });

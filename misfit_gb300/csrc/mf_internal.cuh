@@ -606,6 +606,13 @@ struct mf_ctx {
   mf::DBuf<int64_t> dense_light;      // per dense seed light volume (size bound)
   mf::DBuf<int32_t> pull_long;        // vertices with long rows for the warp pull pass
   mf::DBuf<uint32_t> ncbits;          // non-skipped candidate bits for the pull pass
+  // exact 2-hop sizes by row passes: seed masks per vertex, neighbourhood
+  // volumes, the seed groups, counters, huge rows (chunk counts, prefix,
+  // per-row OR of their chunks)
+  mf::DBuf<uint32_t> p2_mask, p2_filt, p2_racc;
+  mf::DBuf<int64_t> p2_vol, p2_hchunks, p2_hpre;
+  mf::DBuf<int32_t> p2_grp, p2_huge;
+  mf::DBuf<unsigned long long> p2_cnt;
   // sub-batch plan of the current batch: cuts, estimates, seed lists
   mf::DBuf<int64_t> plan_cuts, plan_ests, plan_send, plan_pos;
   mf::DBuf<uint8_t> plan_flags;
@@ -629,6 +636,10 @@ struct mf_ctx {
   mf::DBuf<uint32_t> n2bstamp;         // batch stamp of each cached bound
   uint32_t n2batch = 0;
   mf::DBuf<int32_t> dense_idx, dense_hl, pair_d, pair_h, todo;
+  // per-pass capacities of the push form's dense seeds and light pairs, when
+  // lower than the memory-derived ones (MISFIT_GB_EXACT_CAPS=dense,pairs at
+  // context creation; 0 = not lowered): small graphs then take the retry path
+  int64_t exact_cap_dense = 0, exact_cap_pairs = 0;
   mf::DBuf<unsigned long long> fpos;   // first-hit positions
   mf::DBuf<int32_t> un_idx, un_v, need, needv, live_i, live_v, nlist_need;
   mf::DBuf<uint32_t> nmark;            // epoch marks: neighbours of seeds needing their hop-2 part
@@ -667,7 +678,7 @@ struct mf_ctx {
   bool pending = false;
   // load-balancing settings (mf_set_tuning); they move work between kernels,
   // never a result
-  mf_tuning tune = mf_tuning{2048, 2048, 64, 256, 0};
+  mf_tuning tune = mf_tuning{2048, 2048, 64, 256, 0, 1};
 
   mf::GraphView view() const {
     return mf::GraphView{n, nindex.p, nlist.p, live.p, dead.p, aoff.p, aadj.p};
@@ -698,6 +709,8 @@ void for_each_buffer(mf_ctx* c, F&& f) {
   f(c->xst); f(c->xleave); f(c->cta_vert); f(c->cta_ws);
   f(c->keys); f(c->app_keys); f(c->rp_keys); f(c->rp_keys2);
   f(c->big_best); f(c->fpos); f(c->work);
+  f(c->p2_mask); f(c->p2_filt); f(c->p2_racc); f(c->p2_vol); f(c->p2_hchunks); f(c->p2_hpre); f(c->p2_grp); f(c->p2_huge);
+  f(c->p2_cnt);
   f(c->ws.block_sums); f(c->ws.block_sums2); f(c->ws.hist); f(c->ws.hist_scan); f(c->ws.keys_alt);
   f(c->ws.vals_alt); f(c->ws.scan_status);
   for (auto& fr : c->front) {

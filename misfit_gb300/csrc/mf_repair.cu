@@ -191,7 +191,8 @@ __global__ void k_seed_rows(const int32_t* seeds_all, int64_t ns, int32_t* seeds
 // ---- hop-1 set and candidates ---------------------------------------------------
 
 // Row-position counts for lb_rows; rows that must not be visited count 0.
-enum CountKind : int { kCntAll = 0, kCntSeedRows, kCntCandRows, kCntSeedPushers, kCntHopPushers };
+// kCntMarked: the rows i with marks[i] >= 0 (marks passed as rowcid).
+enum CountKind : int { kCntAll = 0, kCntSeedRows, kCntCandRows, kCntSeedPushers, kCntHopPushers, kCntMarked };
 
 // The count of row i is computed inside the scan's tile load (RowCounts is
 // the scan's loader), so the prefix needs one launch and no count array.
@@ -213,6 +214,8 @@ struct RowCounts {
       use = rowcid[ns + i] != kSkip;
     } else if (kind == kCntSeedPushers) {
       use = (bval[x] >> kRowBits) == epoch;
+    } else if (kind == kCntMarked) {
+      use = rowcid[i] >= 0;
     } else if (kind == kCntHopPushers) {
       use = (bval[x] >> kRowBits) == epoch;
       const int32_t vi = v2i[x];
@@ -592,10 +595,10 @@ __global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32
         const unsigned long long d = atomicAdd(o.ndense, 1ull);
         const unsigned long long hoff = atomicAdd(o.hused, (unsigned long long)nh);
         const unsigned long long pb = atomicAdd(o.npairs, lc);
+        s_pbase = pb;
         if ((int64_t)d < o.dmax && (int64_t)(hoff + nh) <= o.hcap && (int64_t)(pb + lc) <= o.pcap) {
           s_d = (int)d;
           s_hoff = (int)hoff;
-          s_pbase = pb;
           o.dseed[d] = (int32_t)i;
           o.dhoff[d] = (int32_t)hoff;
           o.dnh[d] = nh;
@@ -608,6 +611,15 @@ __global__ void __launch_bounds__(512) k_exact_classify(GraphView g, const int32
       }
       __syncthreads();
       const int d = s_d;
+      if (d < 0) {
+        // retried in the next pass: the pair slots this seed reserved are
+        // marked unused (k_dense_light and its row prefix skip them)
+        const unsigned long long q1 = min(s_pbase + lc, (unsigned long long)o.pcap);
+        for (unsigned long long q = s_pbase + threadIdx.x; q < q1; q += blockDim.x) {
+          o.pair_d[q] = -1;
+          o.pair_h[q] = s;
+        }
+      }
       if (d >= 0) {
         for (int j = threadIdx.x; j < nh; j += blockDim.x) o.hlist[s_hoff + j] = s_h[j];
         // one shared atomic per warp and round: the lanes with a light member
@@ -665,7 +677,7 @@ __global__ void k_dense_light(GraphView g, const int32_t* pair_d, const int32_t*
   });
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < np; k += (int64_t)gridDim.x * blockDim.x) {
     const int32_t h = pair_h[k];
-    atomicOr(dbits + (int64_t)pair_d[k] * words + (h >> 5), 1u << (h & 31));
+    if (pair_d[k] >= 0) atomicOr(dbits + (int64_t)pair_d[k] * words + (h >> 5), 1u << (h & 31));
   }
 }
 
@@ -693,6 +705,308 @@ __global__ void k_todo_retry(const int64_t* lens, const int32_t* todo, int64_t n
                              unsigned long long* cnt) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < ntodo && lens[todo[t]] == -2) out[atomicAdd(cnt, 1ull)] = todo[t];
+}
+
+// ---- exact 2-hop sizes, pull form (symmetric graphs) ----------------------------
+// For a group of up to 32*SW seeds s_j: mask[u] bit j <=> u in N[s_j].  On a
+// symmetric overlay graph, v is in the 2-hop list of s_j iff the OR of mask
+// over {v} u row(v) has bit j:
+//   v in N[s_j]                          <=> mask[v] bit j;
+//   v in row(y) for some y in row(s_j)   <=> y in row(v), and mask[y] bit j;
+// and u = s_j in row(v) means v in row(s_j).  One pass over every row
+// therefore sizes the whole group: it reads each live entry once and gathers
+// one mask per entry, a cost set by the graph, where the push form pays one
+// atomic per element of every member's row (tens of millions per seed next to
+// R-MAT hubs).
+constexpr int kP2MaxWords = 8;          // mask words per vertex: up to 256 seeds per pass
+constexpr int64_t kP2Short = 32;        // rows of up to this many positions: one thread each
+constexpr int64_t kP2Huge = 16384;      // rows longer than this: chunks spread over many warps
+constexpr int64_t kP2Chunk = 4096;      // positions per chunk of a huge row
+constexpr double kP2PassVolume = 4.0;   // cost of a pass, in push-form volume per position
+
+template <int SW>
+__device__ __forceinline__ void p2_or(uint32_t (&m)[SW], const uint32_t* mask, int32_t u) {
+  const uint32_t* p = mask + (int64_t)u * SW;
+  if constexpr (SW >= 4) {
+#pragma unroll
+    for (int h = 0; h < SW / 4; ++h) {
+      const uint4 a = __ldg(reinterpret_cast<const uint4*>(p) + h);
+      m[4 * h] |= a.x;
+      m[4 * h + 1] |= a.y;
+      m[4 * h + 2] |= a.z;
+      m[4 * h + 3] |= a.w;
+    }
+  } else if constexpr (SW == 2) {
+    const uint2 a = __ldg(reinterpret_cast<const uint2*>(p));
+    m[0] |= a.x;
+    m[1] |= a.y;
+  } else {
+    m[0] |= __ldg(p);
+  }
+}
+
+// Bit u of the group's filter: u is in some N[s_j] (mask[u] is not zero).
+// n bits stay in L2 while the masks (up to 32 bytes per vertex) do not, so
+// the pass reads a mask from DRAM only where the filter says it is not zero.
+__device__ __forceinline__ bool p2_in(const uint32_t* filt, int32_t u) {
+  return (__ldg(filt + (u >> 5)) >> (u & 31)) & 1u;
+}
+
+// OR of mask over positions [lo, hi) of row(x), every lane a share (lanes
+// disagree until p2_warp_or).
+template <int SW>
+__device__ __forceinline__ void p2_warp_span(const GraphView& g, const uint32_t* mask, const uint32_t* filt,
+                                             int32_t x, int64_t lo, int64_t hi, uint32_t (&m)[SW]) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = g.nindex[x], nb = g.nindex[x + 1] - b;
+  const bool dead = g.dead[x] != 0;
+  const int64_t ab = g.aoff[x];
+  for (int64_t k0 = lo + lane; k0 < hi; k0 += 128) {
+    int32_t y[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t k = k0 + 32 * q;
+      y[q] = -1;
+      if (k < hi) {
+        if (k < nb) {
+          if (!dead || live_at(g.live, b + k)) y[q] = __ldg(g.nlist + b + k);
+        } else {
+          y[q] = g.aadj[ab + (k - nb)];
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (y[q] >= 0 && !p2_in(filt, y[q])) y[q] = -1;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (y[q] >= 0) p2_or(m, mask, y[q]);
+  }
+}
+
+template <int SW>
+__device__ __forceinline__ void p2_warp_or(uint32_t (&m)[SW]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int w = 0; w < SW; ++w) m[w] |= __shfl_xor_sync(0xffffffffu, m[w], o);
+}
+
+// acc[w] of lane l += number of lanes whose m[w] has bit l (all lanes call).
+template <int SW>
+__device__ __forceinline__ void p2_count_lanes(const uint32_t (&m)[SW], uint32_t (&acc)[SW]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int w = 0; w < SW; ++w) {
+    if (!__any_sync(0xffffffffu, m[w] != 0u)) continue;
+#pragma unroll 8
+    for (int bit = 0; bit < 32; ++bit) {
+      const unsigned bal = __ballot_sync(0xffffffffu, (m[w] >> bit) & 1u);
+      if (lane == bit) acc[w] += (uint32_t)__popc(bal);
+    }
+  }
+}
+
+// Per-lane counts into the group's counters (through shared memory).
+template <int SW>
+__device__ __forceinline__ void p2_flush(const uint32_t (&acc)[SW], unsigned long long* s_cnt,
+                                         unsigned long long* counts) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int w = 0; w < SW; ++w)
+    if (acc[w]) atomicAdd(s_cnt + w * 32 + lane, (unsigned long long)acc[w]);
+  __syncthreads();
+  for (int i = threadIdx.x; i < 32 * SW; i += blockDim.x)
+    if (s_cnt[i]) atomicAdd(counts + i, s_cnt[i]);
+}
+
+// Neighbourhood volume of each seed to size: sum over h in N[s] of
+// (deg(h) + 1).  Grid (seeds, 4 slices of the row); vol pre-zeroed.
+__global__ void k_p2_volume(GraphView g, const int32_t* deg, const int32_t* seeds, const int32_t* todo, int64_t ntodo,
+                            int64_t* vol) {
+  const int64_t t = blockIdx.x;
+  if (t >= ntodo) return;
+  const int32_t s = seeds[todo[t]];
+  const int64_t nb = g.nindex[s + 1] - g.nindex[s];
+  const int64_t total = nb + (g.aoff[s + 1] - g.aoff[s]);
+  unsigned long long sum = 0;
+  for (int64_t k = (int64_t)blockIdx.y * blockDim.x + threadIdx.x - 1; k < total;
+       k += (int64_t)gridDim.y * blockDim.x) {
+    const int32_t h = k < 0 ? s : row_elem(g, s, k, nb);
+    if (h >= 0) sum += (unsigned long long)__ldg(deg + h) + 1ull;
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(reinterpret_cast<unsigned long long*>(vol + t), sum);
+}
+
+// mask[u] bit j for u in N[s_j], j < k.  Grid (k, slices of the row).
+template <int SW>
+__global__ void k_p2_mark(GraphView g, const int32_t* seeds, const int32_t* grp, int k, uint32_t* mask,
+                          uint32_t* filt) {
+  const int j = blockIdx.x;
+  if (j >= k) return;
+  const int32_t s = seeds[grp[j]];
+  const int64_t nb = g.nindex[s + 1] - g.nindex[s];
+  const int64_t total = nb + (g.aoff[s + 1] - g.aoff[s]);
+  const uint32_t bit = 1u << (j & 31);
+  uint32_t* col = mask + (j >> 5);
+  for (int64_t t = (int64_t)blockIdx.y * blockDim.x + threadIdx.x - 1; t < total;
+       t += (int64_t)gridDim.y * blockDim.x) {
+    const int32_t h = t < 0 ? s : row_elem(g, s, t, nb);
+    if (h < 0) continue;
+    uint32_t* p = col + (int64_t)h * SW;
+    if (!(*p & bit)) atomicOr(p, bit);   // a stale read only costs an atomic
+    uint32_t* f = filt + (h >> 5);
+    const uint32_t fb = 1u << (h & 31);
+    if (!(*f & fb)) atomicOr(f, fb);
+  }
+}
+
+// The pass over every vertex, 32 consecutive vertices per warp step: short
+// rows one thread each, rows up to kP2Huge positions by the whole warp, one
+// after another; longer rows go to `huge` (their chunk counts to hchunks)
+// for k_p2_huge.  counts[j] += vertices whose OR has bit j.
+template <int SW>
+__global__ void __launch_bounds__(256) k_p2_rows(GraphView g, const uint32_t* mask, const uint32_t* filt,
+                                                 unsigned long long* counts, int32_t* huge, int64_t* hchunks,
+                                                 unsigned long long* nhuge, int64_t hcap) {
+  __shared__ unsigned long long s_cnt[32 * SW];
+  for (int i = threadIdx.x; i < 32 * SW; i += blockDim.x) s_cnt[i] = 0;
+  __syncthreads();
+  uint32_t acc[SW];
+#pragma unroll
+  for (int w = 0; w < SW; ++w) acc[w] = 0;
+  const int lane = threadIdx.x & 31;
+  const int64_t step = ((int64_t)gridDim.x * blockDim.x);
+  for (int64_t base = warp_id() * 32; base < g.n; base += step) {
+    const int64_t vi = base + lane;
+    uint32_t m[SW];
+#pragma unroll
+    for (int w = 0; w < SW; ++w) m[w] = 0;
+    bool warp_row = false;
+    if (vi < g.n) {
+      const int32_t v = (int32_t)vi;
+      const int64_t b = g.nindex[v], e = g.nindex[v + 1];
+      const int64_t ab = g.aoff[v], ae = g.aoff[v + 1];
+      const int64_t tot = (e - b) + (ae - ab);
+      if (tot > kP2Huge) {
+        const unsigned long long h = atomicAdd(nhuge, 1ull);
+        if ((int64_t)h < hcap) {
+          huge[h] = v;
+          hchunks[h] = (tot + kP2Chunk - 1) / kP2Chunk;
+        }
+      } else {
+        if (p2_in(filt, v)) p2_or(m, mask, v);
+        if (tot > kP2Short) {
+          warp_row = true;
+        } else {
+          // four positions per step: their ids, then their filter bits, then
+          // the masks of those that pass, all loads of a step in flight
+          const bool dead = g.dead[v] != 0;
+          const int64_t nb = e - b;
+          for (int64_t k0 = 0; k0 < tot; k0 += 4) {
+            int32_t y[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int64_t k = k0 + q;
+              y[q] = -1;
+              if (k < nb) {
+                if (!dead || live_at(g.live, b + k)) y[q] = __ldg(g.nlist + b + k);
+              } else if (k < tot) {
+                y[q] = g.aadj[ab + (k - nb)];
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (y[q] >= 0 && !p2_in(filt, y[q])) y[q] = -1;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (y[q] >= 0) p2_or(m, mask, y[q]);
+          }
+        }
+      }
+    }
+    unsigned wl = __ballot_sync(0xffffffffu, warp_row);
+    while (wl) {
+      const int src = __ffs(wl) - 1;
+      wl &= wl - 1;
+      const int32_t x = (int32_t)(base + src);
+      const int64_t tot = (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
+      uint32_t r[SW];
+#pragma unroll
+      for (int w = 0; w < SW; ++w) r[w] = 0;
+      p2_warp_span(g, mask, filt, x, 0, tot, r);
+      p2_warp_or(r);
+      if (lane == src)
+#pragma unroll
+        for (int w = 0; w < SW; ++w) m[w] |= r[w];
+    }
+    p2_count_lanes(m, acc);
+  }
+  p2_flush(acc, s_cnt, counts);
+}
+
+// Chunks of the huge rows: warp per chunk; the chunk's OR goes to racc of its
+// row.  hpre is the exclusive prefix of hchunks over hcap entries.
+template <int SW>
+__global__ void __launch_bounds__(256) k_p2_huge(GraphView g, const uint32_t* mask, const uint32_t* filt,
+                                                 const int32_t* huge, const int64_t* hpre, int64_t hcap,
+                                                 uint32_t* racc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = hpre[hcap];
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = warp_id(); c < total; c += nw) {
+    int64_t lo = 0, hi = hcap;   // last i with hpre[i] <= c
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (hpre[mid] <= c) lo = mid; else hi = mid;
+    }
+    const int64_t i = lo;
+    const int32_t x = huge[i];
+    const int64_t tot = (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
+    const int64_t p0 = (c - hpre[i]) * kP2Chunk;
+    uint32_t r[SW];
+#pragma unroll
+    for (int w = 0; w < SW; ++w) r[w] = 0;
+    p2_warp_span(g, mask, filt, x, p0, min(tot, p0 + kP2Chunk), r);
+    p2_warp_or(r);
+#pragma unroll
+    for (int w = 0; w < SW; ++w)
+      if (lane == w && r[w]) atomicOr(racc + i * SW + w, r[w]);
+  }
+}
+
+// The huge rows' own masks plus their chunks' ORs, counted.
+template <int SW>
+__global__ void __launch_bounds__(256) k_p2_huge_count(const uint32_t* mask, const int32_t* huge,
+                                                       const unsigned long long* nhuge, int64_t hcap,
+                                                       const uint32_t* racc, unsigned long long* counts) {
+  __shared__ unsigned long long s_cnt[32 * SW];
+  for (int i = threadIdx.x; i < 32 * SW; i += blockDim.x) s_cnt[i] = 0;
+  __syncthreads();
+  uint32_t acc[SW];
+#pragma unroll
+  for (int w = 0; w < SW; ++w) acc[w] = 0;
+  const int64_t nh = min((int64_t)*nhuge, hcap);
+  const int64_t step = ((int64_t)gridDim.x * blockDim.x);
+  for (int64_t base = warp_id() * 32; base < nh; base += step) {
+    const int64_t i = base + (threadIdx.x & 31);
+    uint32_t m[SW];
+#pragma unroll
+    for (int w = 0; w < SW; ++w) m[w] = 0;
+    if (i < nh) {
+      p2_or(m, mask, huge[i]);
+#pragma unroll
+      for (int w = 0; w < SW; ++w) m[w] |= racc[i * SW + w];
+    }
+    p2_count_lanes(m, acc);
+  }
+  p2_flush(acc, s_cnt, counts);
+}
+
+__global__ void k_p2_store(const unsigned long long* counts, const int32_t* grp, int k, int64_t* lens) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < k) lens[grp[j]] = (int64_t)counts[j];
 }
 
 
@@ -2220,6 +2534,13 @@ void row_offsets(mf_ctx* c, const int32_t* list, int64_t cnt, int kind, int64_t 
                       c->ws, s);
 }
 
+// Row-position prefix of the rows i of list[0..cnt) with marks[i] >= 0.
+void row_offsets_marked(mf_ctx* c, const int32_t* list, const int32_t* marks, int64_t cnt) {
+  c->lb_offs.reserve(cnt + 1);
+  scan_exclusive_with(RowCounts{c->view(), list, kCntMarked, marks, 0, c->bval.p, 0, c->v2i.p}, c->lb_offs.p, cnt,
+                      c->ws, c->stream);
+}
+
 // row_offsets into caller-given buffers on a given stream (the fronts).
 void row_offsets_into(mf_ctx* c, const int32_t* list, int64_t cnt, DBuf<int64_t>& offs, Scratch& ws,
                       cudaStream_t s) {
@@ -2306,6 +2627,109 @@ void debug_push_hop(mf_ctx* c, const unsigned long long* counter, unsigned long 
                debug_counter(c, counter) - before);
 }
 
+template <int SW>
+void pull_pass(mf_ctx* c, const int32_t* grp, int k, int64_t hcap) {
+  cudaStream_t s = c->stream;
+  const GraphView g = c->view();
+  const int32_t n = c->n;
+  unsigned long long* cnt = c->p2_cnt.p;
+  unsigned long long* nhuge = cnt + 32 * kP2MaxWords;
+  const int64_t fwords = ((int64_t)n + 31) / 32;
+  MF_CUDA(cudaMemsetAsync(c->p2_mask.p, 0, sizeof(uint32_t) * (size_t)n * SW, s));
+  MF_CUDA(cudaMemsetAsync(c->p2_filt.p, 0, sizeof(uint32_t) * (size_t)fwords, s));
+  MF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (32 * kP2MaxWords + 1), s));
+  MF_CUDA(cudaMemsetAsync(c->p2_hchunks.p, 0, sizeof(int64_t) * (size_t)hcap, s));
+  MF_K(k_p2_mark<SW><<<dim3((unsigned)k, 16), kTB, 0, s>>>(g, c->seeds.p, grp, k, c->p2_mask.p, c->p2_filt.p));
+  MF_K(k_p2_rows<SW><<<lb_grid(c, k_p2_rows<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, cnt, c->p2_huge.p,
+                                                                 c->p2_hchunks.p, nhuge, hcap));
+  scan_exclusive_i64(c->p2_hchunks.p, c->p2_hpre.p, hcap, c->ws, s);
+  MF_CUDA(cudaMemsetAsync(c->p2_racc.p, 0, sizeof(uint32_t) * (size_t)hcap * SW, s));
+  MF_K(k_p2_huge<SW><<<lb_grid(c, k_p2_huge<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, c->p2_huge.p,
+                                                                 c->p2_hpre.p, hcap, c->p2_racc.p));
+  MF_K(k_p2_huge_count<SW><<<grid_for(hcap), kTB, 0, s>>>(c->p2_mask.p, c->p2_huge.p, nhuge, hcap, c->p2_racc.p,
+                                                            cnt));
+  MF_K(k_p2_store<<<1, 256, 0, s>>>(cnt, grp, k, c->rowlens.p));
+}
+
+// Exact 2-hop sizes, by one pass over every row per group of up to 256
+// seeds, of the todo seeds whose neighbourhood volume pays for it
+// (tune.pull_sizes 1; 2 takes all of them; symmetric graphs only).  Sizes
+// go to c->rowlens; the seeds left for the push form are written back to
+// todo, and their count is returned.
+int64_t pull_exact(mf_ctx* c, int32_t* todo, int64_t ntodo) {
+  if (c->tune.pull_sizes == 0 || !c->symmetric || ntodo == 0) return ntodo;
+  cudaStream_t s = c->stream;
+  const int32_t n = c->n;
+  // mask words per vertex within 8 GB
+  int max_words = kP2MaxWords;
+  while (max_words > 0 && (int64_t)n * max_words * 4 > ((int64_t)8 << 30)) max_words >>= 1;
+  if (max_words == 0) return ntodo;
+  const GraphView g = c->view();
+  c->p2_vol.reserve(ntodo);
+  MF_CUDA(cudaMemsetAsync(c->p2_vol.p, 0, sizeof(int64_t) * (size_t)ntodo, s));
+  MF_K(k_p2_volume<<<dim3((unsigned)ntodo, 4), kTB, 0, s>>>(g, c->deg.p, c->seeds.p, todo, ntodo, c->p2_vol.p));
+  std::vector<int64_t> vol((size_t)ntodo);
+  std::vector<int32_t> idx((size_t)ntodo);
+  MF_CUDA(cudaMemcpyAsync(vol.data(), c->p2_vol.p, sizeof(int64_t) * (size_t)ntodo, cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaMemcpyAsync(idx.data(), todo, sizeof(int32_t) * (size_t)ntodo, cudaMemcpyDeviceToHost, s));
+  MF_CUDA(cudaStreamSynchronize(s));
+  std::vector<int64_t> order((size_t)ntodo);
+  for (int64_t t = 0; t < ntodo; ++t) order[(size_t)t] = t;
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return vol[(size_t)a] > vol[(size_t)b]; });
+  // Measured on R-MAT scale 26 (2.6e9 positions): a pass takes about as long
+  // as the push form takes for a neighbourhood volume of 4x the positions.
+  const int64_t positions = c->nnz + c->a_total;
+  const double pass_cost = (double)positions * kP2PassVolume + 65536.0;
+  const int64_t gmax = 32 * (int64_t)max_words;
+  std::vector<int32_t> pull, push;
+  std::vector<int> group_sizes;
+  size_t t = 0;
+  while (t < order.size()) {
+    const size_t end = std::min(order.size(), t + (size_t)gmax);
+    double sum = 0;
+    for (size_t u = t; u < end; ++u) sum += (double)vol[(size_t)order[u]];
+    if (c->tune.pull_sizes == 1 && sum < pass_cost) break;
+    for (size_t u = t; u < end; ++u) pull.push_back(idx[(size_t)order[u]]);
+    group_sizes.push_back((int)(end - t));
+    t = end;
+  }
+  if (pull.empty()) return ntodo;
+  double pulled_vol = 0;
+  for (size_t u = 0; u < t; ++u) pulled_vol += (double)vol[(size_t)order[u]];
+  for (; t < order.size(); ++t) push.push_back(idx[(size_t)order[t]]);
+  const bool dbg = debug_counters();
+  const double t0 = dbg ? host_ms() : 0.0;
+  const int64_t hcap = positions / kP2Huge + 1;
+  c->p2_grp.reserve((int64_t)pull.size());
+  const int first = group_sizes.front();
+  c->p2_mask.reserve((int64_t)n * (first <= 32 ? 1 : first <= 64 ? 2 : first <= 128 ? 4 : 8));
+  c->p2_cnt.reserve(32 * kP2MaxWords + 1);
+  c->p2_filt.reserve(((int64_t)n + 31) / 32);
+  c->p2_huge.reserve(hcap);
+  c->p2_hchunks.reserve(hcap);
+  c->p2_hpre.reserve(hcap + 1);
+  c->p2_racc.reserve(hcap * kP2MaxWords);
+  MF_CUDA(cudaMemcpyAsync(c->p2_grp.p, pull.data(), sizeof(int32_t) * pull.size(), cudaMemcpyHostToDevice, s));
+  if (!push.empty())
+    MF_CUDA(cudaMemcpyAsync(todo, push.data(), sizeof(int32_t) * push.size(), cudaMemcpyHostToDevice, s));
+  size_t off = 0;
+  for (const int k : group_sizes) {
+    const int32_t* grp = c->p2_grp.p + off;
+    if (k <= 32) pull_pass<1>(c, grp, k, hcap);
+    else if (k <= 64) pull_pass<2>(c, grp, k, hcap);
+    else if (k <= 128) pull_pass<4>(c, grp, k, hcap);
+    else pull_pass<8>(c, grp, k, hcap);
+    off += (size_t)k;
+  }
+  // the host vectors of the copies above stay alive until the stream reaches them
+  MF_CUDA(cudaStreamSynchronize(s));
+  if (dbg)
+    std::fprintf(stderr, "[misfit_gb] pull sizes: seeds %lld of %lld in %zu passes, volume %.0f, positions %lld, "
+                 "%.3f ms\n", (long long)pull.size(), (long long)ntodo, group_sizes.size(), pulled_vol,
+                 (long long)positions, host_ms() - t0);
+  return (int64_t)push.size();
+}
+
 // Exact 2-hop list sizes of the seeds into c->rowlens[0..ns).
 // With bound_only, dense seeds get an upper bound (k_dense_bound) instead of
 // their exact size, and the results go to the bound cache.
@@ -2361,12 +2785,14 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
   }
   if (ns == 0) return;
   // per-pass capacity of the dense bitmaps: 1 GB, at least one seed
-  const int64_t dmax = std::max<int64_t>(1, std::min<int64_t>(ns, ((int64_t)1 << 30) / (words * 4)));
+  int64_t dmax = std::max<int64_t>(1, std::min<int64_t>(ns, ((int64_t)1 << 30) / (words * 4)));
+  if (c->exact_cap_dense > 0) dmax = std::min<int64_t>(dmax, c->exact_cap_dense);
   c->dense_bits.reserve(dmax * words);
   c->dense_idx.reserve(3 * dmax);
   c->dense_light.reserve(dmax);
   c->dense_hl.reserve(std::max<int64_t>(kMaxHeavyPerSeed, std::min<int64_t>(dmax * 64, (int64_t)1 << 22)));
-  const int64_t pcap = std::max<int64_t>(4096, std::min<int64_t>((int64_t)1 << 26, 2 * c->nnz + 1));
+  int64_t pcap = std::max<int64_t>(4096, std::min<int64_t>((int64_t)1 << 26, 2 * c->nnz + 1));
+  if (c->exact_cap_pairs > 0) pcap = std::min<int64_t>(pcap, c->exact_cap_pairs);
   c->pair_d.reserve(pcap);
   c->pair_h.reserve(pcap);
   c->todo.reserve(3 * ns);
@@ -2383,6 +2809,7 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
   int32_t* todo = c->todo.p;
   int32_t* todo_next = c->todo.p + ns;
   int64_t ntodo = nnew;
+  if (!bound_only) ntodo = pull_exact(c, todo, ntodo);
   unsigned long long* cnts = reinterpret_cast<unsigned long long*>(c->counters.p) + 40;
   while (ntodo > 0) {
     MF_CUDA(cudaMemsetAsync(cnts, 0, sizeof(unsigned long long) * 4, s));
@@ -2401,7 +2828,7 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
       MF_K(k_dense_or<<<grid, 256, 0, s>>>(nd, c->dense_idx.p, c->dense_idx.p + dmax, c->dense_idx.p + 2 * dmax,
                                            c->dense_hl.p, c->heavy_bits.p, words, c->dense_bits.p));
       if (np > 0 && !bound_only) {
-        row_offsets(c, c->pair_h.p, np, kCntAll, ns, ep);
+        row_offsets_marked(c, c->pair_h.p, c->pair_d.p, np);
         MF_K(k_dense_light<<<lb_grid(c, k_dense_light), kTB, 0, s>>>(g, c->pair_d.p, c->pair_h.p, c->lb_offs.p, np, words,
                                                        c->dense_bits.p));
       }

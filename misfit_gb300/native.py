@@ -43,7 +43,8 @@ class BatchStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("pull_long", C.c_int64), ("heavy_min", C.c_int64), ("big_threshold", C.c_int64),
-                ("first_bound", C.c_int64), ("cand_push", C.c_int64)]
+                ("first_bound", C.c_int64), ("cand_push", C.c_int64),
+                ("pull_sizes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -306,8 +307,9 @@ class Graph:
         return t.as_dict()
 
     def set_tuning(self, **kw):
-        """Load-balancing settings (pull_long, heavy_min, big_threshold,
-        first_bound); unnamed ones keep their values.  Results never change."""
+        """Load-balancing settings (mf_tuning: pull_long, heavy_min,
+        big_threshold, first_bound, cand_push, pull_sizes); unnamed ones keep
+        their values.  Results never change."""
         cur = self.tuning()
         cur.update(kw)
         t = Tuning(**cur)

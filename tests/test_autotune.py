@@ -85,7 +85,8 @@ def test_plain_search_keeps_fastest_refuses_disagreement_and_caches(monkeypatch,
     cached by GPU and shape."""
     monkeypatch.setenv(autotune.CACHE_ENV, str(tmp_path / "cache.json"))
     monkeypatch.setattr(autotune, "_gpu_name", lambda: "test-gpu")
-    want = {"pull_long": 8192, "heavy_min": 1024, "big_threshold": 1024, "first_bound": 64, "cand_push": 1}
+    want = {"pull_long": 8192, "heavy_min": 1024, "big_threshold": 1024, "first_bound": 64, "cand_push": 1,
+            "pull_sizes": 2}
     calls = []
 
     def fake_plain(nindex, nlist, mis0, batches, tuning):

@@ -147,12 +147,18 @@ def _stream(kind, seed, batches, size, endpoints="uniform"):
     return n, ni, nl, [ts.next_batch(size, endpoints=endpoints) for _ in range(batches)]
 
 
-@pytest.mark.parametrize("kind,seed,max_csr", [("er", 11, None), ("rmat", 12, None), ("rmat", 13, 3000),
-                                               ("rmat", 14, 40000)])
-def test_stage_parity_live(kind, seed, max_csr, gpu_lib):
+@pytest.mark.parametrize("kind,seed,max_csr,pull", [("er", 11, None, 1), ("rmat", 12, None, 1), ("rmat", 13, 3000, 1),
+                                                    ("rmat", 14, 40000, 1), ("er", 15, 3000, 2), ("rmat", 13, 3000, 2),
+                                                    ("rmat", 14, 40000, 0)])
+def test_stage_parity_live(kind, seed, max_csr, pull, gpu_lib):
+    """Every sub-batch's header, seeds, candidates, exact row lengths (when
+    the size bound reaches the limit), cluster ids, order and membership
+    against the oracle; pull = tuning pull_sizes (exact 2-hop sizes by the
+    push form, the cost model, or row passes for every seed)."""
     n, ni, nl, bs = _stream(kind, seed, 4, 500)
     orc = O.Oracle.from_csr(ni, nl)
     gr = native.Graph.from_csr(ni, nl)
+    gr.set_tuning(pull_sizes=pull)
     if max_csr:
         orc.max_csr = max_csr
         gr.max_csr = max_csr
@@ -173,6 +179,90 @@ def test_stage_parity_live(kind, seed, max_csr, gpu_lib):
         assert np.array_equal(gr.degrees(), orc.degrees())
         assert gr.max_csr == orc.max_csr
         assert gr.check_mis() == orc.check_mis()
+
+
+@pytest.mark.parametrize("caps", ["3,0", "0,4096", "2,4096"])
+def test_exact_sizes_push_form_retries(caps, gpu_lib, monkeypatch):
+    """The push form of the exact 2-hop sizes with its per-pass capacities
+    lowered (dense seeds, light pairs), so that seeds are turned away and
+    retried in later passes, as at R-MAT scale 26 where 128 dense bitmaps
+    fill a pass: row lengths, growths and results equal the oracle's."""
+    monkeypatch.setenv("MISFIT_GB_EXACT_CAPS", caps)
+    n, ni, nl, bs = _stream("rmat", 16, 3, 500, endpoints="preferential")
+    orc = O.Oracle.from_csr(ni, nl)
+    gr = native.Graph.from_csr(ni, nl)
+    gr.set_tuning(pull_sizes=0)
+    orc.max_csr = 3000
+    gr.max_csr = 3000
+    mis = O.greedy_mis(ni, nl)
+    orc.set_mis(mis)
+    gr.set_mis(mis)
+    exact = 0
+    for u, v in bs:
+        ins = orc.flag_updates(u, v)
+        orc.trace(True)
+        gr.trace(True)
+        orc.apply_batch(u, v, ins)
+        gr.apply_batch(u, v, ins)
+        _assert_same_trace(gr.trace_records(), orc.trace_records(), n)
+        exact += gr.stats()["exact_sizes"]
+        assert np.array_equal(gr.get_mis(), orc.get_mis())
+        assert gr.max_csr == orc.max_csr
+    assert exact > 0
+    gr.close()
+
+
+def _with_hubs(n, ni, nl, hubs, seed):
+    """The symmetric graph (ni, nl) plus, for each (hub, degree) of hubs,
+    edges from the hub to `degree` random vertices; sorted, de-duplicated."""
+    rng = np.random.default_rng(seed)
+    src = [np.repeat(np.arange(n, dtype=np.int64), np.diff(ni))]
+    dst = [nl.astype(np.int64)]
+    for h, d in hubs:
+        x = rng.choice(n, size=d, replace=False).astype(np.int64)
+        x = x[x != h]
+        src += [np.full(x.size, h, np.int64), x]
+        dst += [x, np.full(x.size, h, np.int64)]
+    key = np.unique(np.concatenate(src) * n + np.concatenate(dst))
+    s, d = key // n, key % n
+    out = np.zeros(n + 1, np.int64)
+    np.cumsum(np.bincount(s, minlength=n), out=out[1:])
+    return out, d.astype(np.int32)
+
+
+@pytest.mark.parametrize("pull", [0, 2])
+def test_exact_sizes_with_huge_rows(pull, gpu_lib):
+    """Hubs of 20,000 and 17,000 neighbours on a sparse random graph: every
+    seed's 2-hop list is large, so under a small limit the exact sizes decide
+    each growth.  The row passes split the hubs' rows (more than 16,384
+    positions) into chunks over many warps; sizes, growths and results
+    equal the oracle's, and those of the push form."""
+    n = 40000
+    ni, nl = W.er_graph(n, 4, 51)
+    ni, nl = _with_hubs(n, ni, nl, [(7, 20000), (12345, 17000)], 52)
+    ts = W.ToggleStream(n, ni, nl, 53)
+    bs = [ts.next_batch(300) for _ in range(3)]
+    orc = O.Oracle.from_csr(ni, nl)
+    gr = native.Graph.from_csr(ni, nl)
+    gr.set_tuning(pull_sizes=pull)
+    orc.max_csr = 50000
+    gr.max_csr = 50000
+    mis = O.greedy_mis(ni, nl)
+    orc.set_mis(mis)
+    gr.set_mis(mis)
+    exact = 0
+    for u, v in bs:
+        ins = orc.flag_updates(u, v)
+        orc.trace(True)
+        gr.trace(True)
+        orc.apply_batch(u, v, ins)
+        gr.apply_batch(u, v, ins)
+        _assert_same_trace(gr.trace_records(), orc.trace_records(), n)
+        exact += gr.stats()["exact_sizes"]
+        assert np.array_equal(gr.get_mis(), orc.get_mis())
+        assert gr.max_csr == orc.max_csr
+    assert exact > 0
+    gr.close()
 
 
 def test_config1_er10k_ten_batches(gpu_lib, tmp_path):
@@ -405,8 +495,10 @@ def test_tuning_settings_change_no_result(gpu_lib):
     orc = O.Oracle.from_csr(ni, nl)
     flags = [orc.flag_updates(u, v) for u, v in bs]
     results = []
-    for tune in ({}, {"pull_long": 32, "heavy_min": 64, "big_threshold": 0, "first_bound": 8, "cand_push": 1},
-                 {"pull_long": 1 << 20, "heavy_min": 1 << 30, "big_threshold": 1 << 40, "first_bound": 1 << 20}):
+    for tune in ({}, {"pull_long": 32, "heavy_min": 64, "big_threshold": 0, "first_bound": 8, "cand_push": 1,
+                      "pull_sizes": 2},
+                 {"pull_long": 1 << 20, "heavy_min": 1 << 30, "big_threshold": 1 << 40, "first_bound": 1 << 20,
+                  "pull_sizes": 0}):
         g = native.Graph.from_csr(ni, nl)
         if not tune:
             assert g.tuning() == autotune.DEFAULT_TUNING
@@ -418,7 +510,8 @@ def test_tuning_settings_change_no_result(gpu_lib):
             g.apply_batch(u, v, ins)
             out.append((g.get_mis(), g.cluster_ids()))
         results.append(out)
-        for bad in ({"pull_long": 1}, {"first_bound": 4}, {"big_threshold": -1}, {"cand_push": 2}):
+        for bad in ({"pull_long": 1}, {"first_bound": 4}, {"big_threshold": -1}, {"cand_push": 2},
+                    {"pull_sizes": 3}):
             with pytest.raises(native.MisfitError):
                 g.set_tuning(**bad)
         g.close()
