@@ -606,11 +606,11 @@ struct mf_ctx {
   mf::DBuf<int64_t> dense_light;      // per dense seed light volume (size bound)
   mf::DBuf<int32_t> pull_long;        // vertices with long rows for the warp pull pass
   mf::DBuf<uint32_t> ncbits;          // non-skipped candidate bits for the pull pass
-  // exact 2-hop sizes by row passes: seed masks per vertex, neighbourhood
-  // volumes, the seed groups, counters, huge rows (chunk counts, prefix,
-  // per-row OR of their chunks)
+  // exact 2-hop sizes by row passes: seed masks per vertex and their filter
+  // bits, the huge rows' chunk ORs, neighbourhood volumes, chunk tasks, the
+  // seed groups, huge-row slots, counters
   mf::DBuf<uint32_t> p2_mask, p2_filt, p2_racc;
-  mf::DBuf<int64_t> p2_vol, p2_hchunks, p2_hpre;
+  mf::DBuf<int64_t> p2_vol, p2_tasks;
   mf::DBuf<int32_t> p2_grp, p2_huge;
   mf::DBuf<unsigned long long> p2_cnt;
   // sub-batch plan of the current batch: cuts, estimates, seed lists
@@ -709,7 +709,7 @@ void for_each_buffer(mf_ctx* c, F&& f) {
   f(c->xst); f(c->xleave); f(c->cta_vert); f(c->cta_ws);
   f(c->keys); f(c->app_keys); f(c->rp_keys); f(c->rp_keys2);
   f(c->big_best); f(c->fpos); f(c->work);
-  f(c->p2_mask); f(c->p2_filt); f(c->p2_racc); f(c->p2_vol); f(c->p2_hchunks); f(c->p2_hpre); f(c->p2_grp); f(c->p2_huge);
+  f(c->p2_mask); f(c->p2_filt); f(c->p2_racc); f(c->p2_vol); f(c->p2_tasks); f(c->p2_grp); f(c->p2_huge);
   f(c->p2_cnt);
   f(c->ws.block_sums); f(c->ws.block_sums2); f(c->ws.hist); f(c->ws.hist_scan); f(c->ws.keys_alt);
   f(c->ws.vals_alt); f(c->ws.scan_status);

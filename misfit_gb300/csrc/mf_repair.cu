@@ -720,9 +720,10 @@ __global__ void k_todo_retry(const int64_t* lens, const int32_t* todo, int64_t n
 // R-MAT hubs).
 constexpr int kP2MaxWords = 8;          // mask words per vertex: up to 256 seeds per pass
 constexpr int64_t kP2Short = 32;        // rows of up to this many positions: one thread each
-constexpr int64_t kP2Huge = 16384;      // rows longer than this: chunks spread over many warps
-constexpr int64_t kP2Chunk = 4096;      // positions per chunk of a huge row
-constexpr double kP2PassVolume = 4.0;   // cost of a pass, in push-form volume per position
+constexpr int64_t kP2Huge = 1024;       // rows longer than this: chunks spread over many warps
+constexpr int64_t kP2Chunk = 2048;      // positions per chunk of a huge row
+constexpr int64_t kP2Grab = 128;        // vertices per block a warp takes
+constexpr double kP2PassVolume = 0.5;   // cost of a pass, in push-form volume per position
 
 template <int SW>
 __device__ __forceinline__ void p2_or(uint32_t (&m)[SW], const uint32_t* mask, int32_t u) {
@@ -862,14 +863,27 @@ __global__ void k_p2_mark(GraphView g, const int32_t* seeds, const int32_t* grp,
   }
 }
 
-// The pass over every vertex, 32 consecutive vertices per warp step: short
-// rows one thread each, rows up to kP2Huge positions by the whole warp, one
-// after another; longer rows go to `huge` (their chunk counts to hchunks)
-// for k_p2_huge.  counts[j] += vertices whose OR has bit j.
+// The pass over every vertex.  Warps take blocks of kP2Grab consecutive
+// vertices from a counter (the work of a block varies by orders of
+// magnitude on power-law graphs; static assignment left most SMs idle
+// while a few walked the heavy blocks).  In a block, 32 vertices at a time:
+// rows of up to kP2Short positions one thread each, rows up to kP2Huge by
+// the whole warp one after another; longer rows get a slot in `huge` and one
+// task per kP2Chunk positions for k_p2_huge.  counts[j] += vertices whose OR
+// has bit j.
+struct P2Work {
+  unsigned long long* next;      // vertex counter of the block grabs
+  int32_t* huge;                 // slot -> vertex
+  unsigned long long* nhuge;
+  int64_t hcap;
+  int64_t* tasks;                // (slot << 32) | chunk
+  unsigned long long* ntasks;
+  int64_t tcap;
+};
+
 template <int SW>
 __global__ void __launch_bounds__(256) k_p2_rows(GraphView g, const uint32_t* mask, const uint32_t* filt,
-                                                 unsigned long long* counts, int32_t* huge, int64_t* hchunks,
-                                                 unsigned long long* nhuge, int64_t hcap) {
+                                                 unsigned long long* counts, P2Work wk) {
   __shared__ unsigned long long s_cnt[32 * SW];
   for (int i = threadIdx.x; i < 32 * SW; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
@@ -877,94 +891,121 @@ __global__ void __launch_bounds__(256) k_p2_rows(GraphView g, const uint32_t* ma
 #pragma unroll
   for (int w = 0; w < SW; ++w) acc[w] = 0;
   const int lane = threadIdx.x & 31;
-  const int64_t step = ((int64_t)gridDim.x * blockDim.x);
-  for (int64_t base = warp_id() * 32; base < g.n; base += step) {
-    const int64_t vi = base + lane;
-    uint32_t m[SW];
+  for (;;) {
+    unsigned long long grab = 0;
+    if (lane == 0) grab = atomicAdd(wk.next, (unsigned long long)kP2Grab);
+    const int64_t first = (int64_t)__shfl_sync(0xffffffffu, grab, 0);
+    if (first >= g.n) break;
+    const int64_t last = min((int64_t)g.n, first + kP2Grab);
+    for (int64_t base = first; base < last; base += 32) {
+      const int64_t vi = base + lane;
+      uint32_t m[SW];
 #pragma unroll
-    for (int w = 0; w < SW; ++w) m[w] = 0;
-    bool warp_row = false;
-    if (vi < g.n) {
-      const int32_t v = (int32_t)vi;
-      const int64_t b = g.nindex[v], e = g.nindex[v + 1];
-      const int64_t ab = g.aoff[v], ae = g.aoff[v + 1];
-      const int64_t tot = (e - b) + (ae - ab);
-      if (tot > kP2Huge) {
-        const unsigned long long h = atomicAdd(nhuge, 1ull);
-        if ((int64_t)h < hcap) {
-          huge[h] = v;
-          hchunks[h] = (tot + kP2Chunk - 1) / kP2Chunk;
-        }
-      } else {
-        if (p2_in(filt, v)) p2_or(m, mask, v);
-        if (tot > kP2Short) {
-          warp_row = true;
+      for (int w = 0; w < SW; ++w) m[w] = 0;
+      bool warp_row = false;
+      int64_t nch = 0;
+      if (vi < last) {
+        const int32_t v = (int32_t)vi;
+        const int64_t b = g.nindex[v], e = g.nindex[v + 1];
+        const int64_t ab = g.aoff[v], ae = g.aoff[v + 1];
+        const int64_t tot = (e - b) + (ae - ab);
+        if (tot > kP2Huge) {
+          nch = (tot + kP2Chunk - 1) / kP2Chunk;
         } else {
-          // four positions per step: their ids, then their filter bits, then
-          // the masks of those that pass, all loads of a step in flight
-          const bool dead = g.dead[v] != 0;
-          const int64_t nb = e - b;
-          for (int64_t k0 = 0; k0 < tot; k0 += 4) {
-            int32_t y[4];
+          if (p2_in(filt, v)) p2_or(m, mask, v);
+          if (tot > kP2Short) {
+            warp_row = true;
+          } else {
+            // four positions per step: their ids, then their filter bits,
+            // then the masks of those that pass, all loads of a step in flight
+            const bool dead = g.dead[v] != 0;
+            const int64_t nb = e - b;
+            for (int64_t k0 = 0; k0 < tot; k0 += 4) {
+              int32_t y[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const int64_t k = k0 + q;
-              y[q] = -1;
-              if (k < nb) {
-                if (!dead || live_at(g.live, b + k)) y[q] = __ldg(g.nlist + b + k);
-              } else if (k < tot) {
-                y[q] = g.aadj[ab + (k - nb)];
+              for (int q = 0; q < 4; ++q) {
+                const int64_t k = k0 + q;
+                y[q] = -1;
+                if (k < nb) {
+                  if (!dead || live_at(g.live, b + k)) y[q] = __ldg(g.nlist + b + k);
+                } else if (k < tot) {
+                  y[q] = g.aadj[ab + (k - nb)];
+                }
               }
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                if (y[q] >= 0 && !p2_in(filt, y[q])) y[q] = -1;
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                if (y[q] >= 0) p2_or(m, mask, y[q]);
             }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (y[q] >= 0 && !p2_in(filt, y[q])) y[q] = -1;
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (y[q] >= 0) p2_or(m, mask, y[q]);
           }
         }
       }
-    }
-    unsigned wl = __ballot_sync(0xffffffffu, warp_row);
-    while (wl) {
-      const int src = __ffs(wl) - 1;
-      wl &= wl - 1;
-      const int32_t x = (int32_t)(base + src);
-      const int64_t tot = (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
-      uint32_t r[SW];
+      // huge rows of these 32 vertices: one slot each and their chunk
+      // tasks, one atomic per warp for each
+      const unsigned hm = __ballot_sync(0xffffffffu, nch > 0);
+      if (hm) {
+        int64_t incl = nch;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int64_t t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        const int64_t wtot = __shfl_sync(0xffffffffu, incl, 31);
+        unsigned long long sbase = 0, tbase = 0;
+        if (lane == 0) {
+          sbase = atomicAdd(wk.nhuge, (unsigned long long)__popc(hm));
+          tbase = atomicAdd(wk.ntasks, (unsigned long long)wtot);
+        }
+        sbase = __shfl_sync(0xffffffffu, sbase, 0);
+        tbase = __shfl_sync(0xffffffffu, tbase, 0);
+        if (nch > 0) {
+          const int64_t slot = (int64_t)sbase + __popc(hm & ((1u << lane) - 1u));
+          const int64_t t0 = (int64_t)tbase + incl - nch;
+          if (slot < wk.hcap) {
+            wk.huge[slot] = (int32_t)vi;
+            for (int64_t c = 0; c < nch; ++c)
+              if (t0 + c < wk.tcap) wk.tasks[t0 + c] = (slot << 32) | c;
+          }
+        }
+      }
+      unsigned wl = __ballot_sync(0xffffffffu, warp_row);
+      while (wl) {
+        const int src = __ffs(wl) - 1;
+        wl &= wl - 1;
+        const int32_t x = (int32_t)(base + src);
+        const int64_t tot = (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
+        uint32_t r[SW];
 #pragma unroll
-      for (int w = 0; w < SW; ++w) r[w] = 0;
-      p2_warp_span(g, mask, filt, x, 0, tot, r);
-      p2_warp_or(r);
-      if (lane == src)
+        for (int w = 0; w < SW; ++w) r[w] = 0;
+        p2_warp_span(g, mask, filt, x, 0, tot, r);
+        p2_warp_or(r);
+        if (lane == src)
 #pragma unroll
-        for (int w = 0; w < SW; ++w) m[w] |= r[w];
+          for (int w = 0; w < SW; ++w) m[w] |= r[w];
+      }
+      p2_count_lanes(m, acc);
     }
-    p2_count_lanes(m, acc);
   }
   p2_flush(acc, s_cnt, counts);
 }
 
-// Chunks of the huge rows: warp per chunk; the chunk's OR goes to racc of its
-// row.  hpre is the exclusive prefix of hchunks over hcap entries.
+// Chunk tasks of the huge rows, one warp each: the chunk's OR goes to racc
+// of its row's slot.
 template <int SW>
 __global__ void __launch_bounds__(256) k_p2_huge(GraphView g, const uint32_t* mask, const uint32_t* filt,
-                                                 const int32_t* huge, const int64_t* hpre, int64_t hcap,
-                                                 uint32_t* racc) {
+                                                 P2Work wk, uint32_t* racc) {
   const int lane = threadIdx.x & 31;
-  const int64_t total = hpre[hcap];
+  const int64_t total = min((int64_t)*wk.ntasks, wk.tcap);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t c = warp_id(); c < total; c += nw) {
-    int64_t lo = 0, hi = hcap;   // last i with hpre[i] <= c
-    while (hi - lo > 1) {
-      const int64_t mid = (lo + hi) >> 1;
-      if (hpre[mid] <= c) lo = mid; else hi = mid;
-    }
-    const int64_t i = lo;
-    const int32_t x = huge[i];
+  for (int64_t t = warp_id(); t < total; t += nw) {
+    const int64_t task = wk.tasks[t];
+    const int64_t i = task >> 32;
+    const int64_t c = task & 0xffffffffll;
+    if (i >= wk.hcap) continue;   // never: hcap bounds the rows over kP2Huge positions
+    const int32_t x = wk.huge[i];
     const int64_t tot = (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
-    const int64_t p0 = (c - hpre[i]) * kP2Chunk;
+    const int64_t p0 = c * kP2Chunk;
     uint32_t r[SW];
 #pragma unroll
     for (int w = 0; w < SW; ++w) r[w] = 0;
@@ -2628,25 +2669,22 @@ void debug_push_hop(mf_ctx* c, const unsigned long long* counter, unsigned long 
 }
 
 template <int SW>
-void pull_pass(mf_ctx* c, const int32_t* grp, int k, int64_t hcap) {
+void pull_pass(mf_ctx* c, const int32_t* grp, int k, int64_t hcap, int64_t tcap) {
   cudaStream_t s = c->stream;
   const GraphView g = c->view();
   const int32_t n = c->n;
-  unsigned long long* cnt = c->p2_cnt.p;
-  unsigned long long* nhuge = cnt + 32 * kP2MaxWords;
+  unsigned long long* cnt = c->p2_cnt.p;   // 32*kP2MaxWords counts, then next, nhuge, ntasks
+  unsigned long long* ctl = cnt + 32 * kP2MaxWords;
+  const P2Work wk{ctl, c->p2_huge.p, ctl + 1, hcap, c->p2_tasks.p, ctl + 2, tcap};
   const int64_t fwords = ((int64_t)n + 31) / 32;
   MF_CUDA(cudaMemsetAsync(c->p2_mask.p, 0, sizeof(uint32_t) * (size_t)n * SW, s));
   MF_CUDA(cudaMemsetAsync(c->p2_filt.p, 0, sizeof(uint32_t) * (size_t)fwords, s));
-  MF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (32 * kP2MaxWords + 1), s));
-  MF_CUDA(cudaMemsetAsync(c->p2_hchunks.p, 0, sizeof(int64_t) * (size_t)hcap, s));
+  MF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * (32 * kP2MaxWords + 3), s));
   MF_K(k_p2_mark<SW><<<dim3((unsigned)k, 16), kTB, 0, s>>>(g, c->seeds.p, grp, k, c->p2_mask.p, c->p2_filt.p));
-  MF_K(k_p2_rows<SW><<<lb_grid(c, k_p2_rows<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, cnt, c->p2_huge.p,
-                                                                 c->p2_hchunks.p, nhuge, hcap));
-  scan_exclusive_i64(c->p2_hchunks.p, c->p2_hpre.p, hcap, c->ws, s);
+  MF_K(k_p2_rows<SW><<<lb_grid(c, k_p2_rows<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, cnt, wk));
   MF_CUDA(cudaMemsetAsync(c->p2_racc.p, 0, sizeof(uint32_t) * (size_t)hcap * SW, s));
-  MF_K(k_p2_huge<SW><<<lb_grid(c, k_p2_huge<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, c->p2_huge.p,
-                                                                 c->p2_hpre.p, hcap, c->p2_racc.p));
-  MF_K(k_p2_huge_count<SW><<<grid_for(hcap), kTB, 0, s>>>(c->p2_mask.p, c->p2_huge.p, nhuge, hcap, c->p2_racc.p,
+  MF_K(k_p2_huge<SW><<<lb_grid(c, k_p2_huge<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, wk, c->p2_racc.p));
+  MF_K(k_p2_huge_count<SW><<<grid_for(hcap), kTB, 0, s>>>(c->p2_mask.p, c->p2_huge.p, ctl + 1, hcap, c->p2_racc.p,
                                                             cnt));
   MF_K(k_p2_store<<<1, 256, 0, s>>>(cnt, grp, k, c->rowlens.p));
 }
@@ -2676,8 +2714,9 @@ int64_t pull_exact(mf_ctx* c, int32_t* todo, int64_t ntodo) {
   std::vector<int64_t> order((size_t)ntodo);
   for (int64_t t = 0; t < ntodo; ++t) order[(size_t)t] = t;
   std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return vol[(size_t)a] > vol[(size_t)b]; });
-  // Measured on R-MAT scale 26 (2.6e9 positions): a pass takes about as long
-  // as the push form takes for a neighbourhood volume of 4x the positions.
+  // Measured on R-MAT scale 26 (2.6e9 positions): a pass (about 13 ms) takes
+  // as long as the push form takes for a neighbourhood volume of about half
+  // the positions.
   const int64_t positions = c->nnz + c->a_total;
   const double pass_cost = (double)positions * kP2PassVolume + 65536.0;
   const int64_t gmax = 32 * (int64_t)max_words;
@@ -2699,15 +2738,16 @@ int64_t pull_exact(mf_ctx* c, int32_t* todo, int64_t ntodo) {
   for (; t < order.size(); ++t) push.push_back(idx[(size_t)order[t]]);
   const bool dbg = debug_counters();
   const double t0 = dbg ? host_ms() : 0.0;
-  const int64_t hcap = positions / kP2Huge + 1;
+  // rows over kP2Huge positions, and their chunks
+  const int64_t hcap = positions / (kP2Huge + 1) + 1;
+  const int64_t tcap = hcap + positions / kP2Chunk + 1;
   c->p2_grp.reserve((int64_t)pull.size());
   const int first = group_sizes.front();
   c->p2_mask.reserve((int64_t)n * (first <= 32 ? 1 : first <= 64 ? 2 : first <= 128 ? 4 : 8));
-  c->p2_cnt.reserve(32 * kP2MaxWords + 1);
+  c->p2_cnt.reserve(32 * kP2MaxWords + 3);
   c->p2_filt.reserve(((int64_t)n + 31) / 32);
   c->p2_huge.reserve(hcap);
-  c->p2_hchunks.reserve(hcap);
-  c->p2_hpre.reserve(hcap + 1);
+  c->p2_tasks.reserve(tcap);
   c->p2_racc.reserve(hcap * kP2MaxWords);
   MF_CUDA(cudaMemcpyAsync(c->p2_grp.p, pull.data(), sizeof(int32_t) * pull.size(), cudaMemcpyHostToDevice, s));
   if (!push.empty())
@@ -2715,10 +2755,10 @@ int64_t pull_exact(mf_ctx* c, int32_t* todo, int64_t ntodo) {
   size_t off = 0;
   for (const int k : group_sizes) {
     const int32_t* grp = c->p2_grp.p + off;
-    if (k <= 32) pull_pass<1>(c, grp, k, hcap);
-    else if (k <= 64) pull_pass<2>(c, grp, k, hcap);
-    else if (k <= 128) pull_pass<4>(c, grp, k, hcap);
-    else pull_pass<8>(c, grp, k, hcap);
+    if (k <= 32) pull_pass<1>(c, grp, k, hcap, tcap);
+    else if (k <= 64) pull_pass<2>(c, grp, k, hcap, tcap);
+    else if (k <= 128) pull_pass<4>(c, grp, k, hcap, tcap);
+    else pull_pass<8>(c, grp, k, hcap, tcap);
     off += (size_t)k;
   }
   // the host vectors of the copies above stay alive until the stream reaches them
