@@ -86,6 +86,10 @@ def parse_args():
     ap.add_argument("--large-seconds", type=float, default=60.0,
                     help="device-time budget of the large leg's timed sample")
     ap.add_argument("--large-dir", default=None, help="folder for the large .egr file (default: the system temp)")
+    ap.add_argument("--large-max-csr", type=int, default=0,
+                    help="MAX_CSR_ELEMENTS to start the large leg from (default: the reference's initial value)")
+    ap.add_argument("--large-pull-sizes", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="tuning pull_sizes of the large leg (-1: the library default)")
     ap.add_argument("--served-only", action="store_true", help="run only the served leg and print its JSON")
     ap.add_argument("--batched-only", action="store_true",
                     help="run only the batched-form leg and print its JSON (profiling runs)")
@@ -330,6 +334,12 @@ def run_large(args, local):
         t = time.perf_counter()
         g = native.Graph.open_egr(path, gpu=local)
         out["ingest_s"] = time.perf_counter() - t
+        if args.large_max_csr > 0:
+            g.max_csr = args.large_max_csr
+            out["max_csr_start"] = args.large_max_csr
+        if args.large_pull_sizes >= 0:
+            g.set_tuning(pull_sizes=args.large_pull_sizes)
+            out["pull_sizes"] = args.large_pull_sizes
         out["ingest_gbs"] = out["file_bytes"] / out["ingest_s"] / 1e9
         t = time.perf_counter()
         mis0 = g.greedy_mis()
