@@ -45,12 +45,12 @@ VALUE_IS = ("plain per-batch loop (the reference's method, compat mode) on the R
 UNIT = "updates/s"
 
 # DRAM bytes (read + write) per pushed element of k_lb_push_hop, measured by
-# ncu on the R-MAT scale-20, 20,000-update case: dram__bytes_read.sum +
-# dram__bytes_write.sum over launches 6-9 of the kernel (71,991,808 bytes)
-# divided by their pushed elements (3,619,180, printed with
-# MISFIT_GB_DEBUG=2).  ncu flushes the caches before each launch, so this is
-# a cold-L2 figure.
-PUSH_HOP_DRAM_BYTES_PER_ELEMENT = 19.89
+# ncu on this workload (R-MAT scale 22, the bench's first batch):
+# dram__bytes_read.sum + dram__bytes_write.sum over the kernel's launches
+# 200-202 (135,575,040 bytes) divided by their pushed elements (9,720,762,
+# printed with MISFIT_GB_DEBUG=2).  ncu flushes the caches before each
+# launch, so this is a cold-L2 figure; 12 bytes per element are algorithmic.
+PUSH_HOP_DRAM_BYTES_PER_ELEMENT = 13.95
 
 
 def parse_args():
@@ -78,6 +78,9 @@ def parse_args():
     ap.add_argument("--served-budget", type=float, default=0.6, help="HBM budget as a fraction of the footprint")
     ap.add_argument("--served-cta-limit", type=int, default=512,
                     help="largest request the served form's continuous batching gives to the persistent kernel")
+    ap.add_argument("--served-cta-vertices", type=int, default=65536,
+                    help="largest graph whose requests the served form's continuous batching gives to the "
+                         "persistent kernel (one CTA walks every vertex of its graph in some stages)")
     ap.add_argument("--no-large", action="store_true", help="skip the 64-bit-layout leg (R-MAT scale 26)")
     ap.add_argument("--large-only", action="store_true", help="run only the 64-bit-layout leg and print its JSON")
     ap.add_argument("--large-scale", type=int, default=26)
@@ -556,7 +559,8 @@ def run_served(args, graphs, mis0, batching, device):
     p_res = plain_sweep(graphs, mis0, per_rate)
     s_res = pool_sweep(graphs, mis0, per_rate, args.served_workers, args.served_budget)
     lat_opts = native.batched_opts(block=batching.block, ctas_per_sm=batching.ctas_per_sm,
-                                   max_cta_updates=min(int(args.served_cta_limit), batching.max_cta_updates))
+                                   max_cta_updates=min(int(args.served_cta_limit), batching.max_cta_updates),
+                                   max_cta_vertices=min(int(args.served_cta_vertices), batching.max_cta_vertices))
     c_res = pool_sweep(graphs, mis0, per_rate, args.served_workers, args.served_budget, lat_opts)
     same = all(np.array_equal(a, b) for a, b in zip(p_res["mis"], s_res["mis"]))
     same_c = all(np.array_equal(a, b) for a, b in zip(p_res["mis"], c_res["mis"]))
@@ -872,8 +876,9 @@ def main():
             "traffic": traffic, "kernel": "k_lb_push_hop", "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": ms / max(calls, 1),
             "launches": int(calls),
-            "traffic_note": "DRAM bytes per pushed element from an ncu capture of the R-MAT scale-20 case, "
-                            "times this workload's elements per launch"}
+            "traffic_note": "DRAM bytes per pushed element from an ncu capture of three launches of this "
+                            "workload (cold L2, 13.95 B against 12 B algorithmic), times this workload's "
+                            "elements per launch"}
 
     # per-batch roofline: the algorithmic bytes of a whole batch, summed over
     # the reference's sub-batches, against the timed batches' mean time:
