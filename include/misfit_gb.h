@@ -192,7 +192,8 @@ typedef struct mf_tuning {
   int64_t big_threshold;  /* hop-2 volume above which the insertion rule's search for the first
                              eligible vertex goes to the grid-wide kernel (default 64) */
   int64_t first_bound;    /* row positions the warp level of the first-cluster-id search covers
-                             before long rows go to the chunk level (default 256, at least 8) */
+                             before long rows go to the chunk level (default 256, at least 8;
+                             values below 32, the per-thread probe's length, act as 32) */
   int64_t cand_push;      /* 0: on graphs with symmetric sorted rows, the candidate rows' cluster ids
                              are pulled by every vertex (default); 1: always pushed from the
                              candidate rows, then finalised per vertex */

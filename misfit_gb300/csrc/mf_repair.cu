@@ -1129,7 +1129,8 @@ __global__ void k_cid_bits(const int32_t* cid, int32_t n, uint32_t* bits) {
 
 // ---- first-hit searches with device-side counts ---------------------------------
 // Three levels, none of which needs the host to know a count:
-//   1. one thread per row probes the first kProbe positions;
+//   1. one thread per row probes the first kProbe positions, eight at a time
+//      (their loads, then their tests);
 //   2. rows still open go to a queue; a fixed grid of warps scans positions
 //      kProbe .. bound of each (a tuning setting, 256 by default);
 //   3. rows still open get chunks of kFirstChunk positions from one packed
@@ -1137,7 +1138,7 @@ __global__ void k_cid_bits(const int32_t* cid, int32_t n, uint32_t* bits) {
 //      with the row slots; a fixed grid of warps takes chunks, finds the row
 //      by binary search over the bases and keeps the minimum hit position.
 // The same chunk queue drives the marking of the need seeds' neighbours.
-constexpr int kProbe = 8;
+constexpr int kProbe = 32;
 constexpr int64_t kFirstChunk = 256;
 constexpr int kChunkShift = 40;
 constexpr unsigned long long kChunkMask = (1ull << kChunkShift) - 1;
@@ -1237,13 +1238,30 @@ __global__ void k_first_probe(GraphView g, const int32_t* list, const unsigned l
     const int64_t nb = g.nindex[x + 1] - g.nindex[x];
     const int64_t np = nb + (g.aoff[x + 1] - g.aoff[x]);
     const int64_t lim = np < kProbe ? np : kProbe;
+    const int64_t b0 = g.nindex[x];
+    const int64_t a0 = g.aoff[x];
+    const bool filt = g.dead[x] != 0;
     unsigned long long fp = kNoPos;
-    for (int64_t k = 0; k < lim; ++k) {
-      const int32_t y = row_elem(g, x, k, nb);
-      if (y >= 0 && pred(y)) {
-        fp = (unsigned long long)k;
-        break;
+    for (int64_t k0 = 0; k0 < lim && fp == kNoPos; k0 += 8) {
+      int32_t y[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int64_t k = k0 + t;
+        y[t] = -1;
+        if (k < lim) {
+          if (k < nb) {
+            if (!filt || live_at(g.live, b0 + k)) y[t] = __ldg(g.nlist + b0 + k);
+          } else {
+            y[t] = g.aadj[a0 + (k - nb)];
+          }
+        }
       }
+      bool ok[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) ok[t] = y[t] >= 0 && pred(y[t]);
+#pragma unroll
+      for (int t = 7; t >= 0; --t)
+        if (ok[t]) fp = (unsigned long long)(k0 + t);
     }
     firstpos[i] = fp;
     if (fp == kNoPos && np > kProbe) {
