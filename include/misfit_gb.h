@@ -403,13 +403,16 @@ int mf_apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t
                      const uint8_t* const* ins, const int64_t* m, int64_t count, const mf_batched_opts* opts,
                      mf_batched_stats* stats);
 /* Batched dispatch for a pool (continuous batching): with opts non-NULL,
- * every request whose batch mf_apply_batches would give to its persistent
- * kernel (size and vertex limits of opts, compat mode) goes to one
- * dispatcher thread instead of the workers.  The dispatcher takes every such
- * request that is ready -- one per graph, graphs restored under the budget
- * first -- and applies them in one mf_apply_batches step; requests that
- * arrive meanwhile form the next step.  Larger requests stay with the
- * workers.  opts NULL turns it off.  Results per graph are unchanged. */
+ * every request of a resident graph whose batch mf_apply_batches would give
+ * to its persistent kernel (size and vertex limits of opts, compat mode),
+ * on a graph whose current mean degree, added entries included, keeps
+ * lines * (1 + degree)^2 within max_cta_updates * 33^2, goes to one
+ * dispatcher thread instead of the workers.  The dispatcher
+ * takes every such request that is ready -- one per graph -- and applies
+ * them in one mf_apply_batches step; requests that arrive meanwhile form the
+ * next step.  Larger requests, and the requests of graphs evicted to host
+ * memory (restored by the workers), stay with the workers.  opts NULL turns
+ * it off.  Results per graph are unchanged. */
 int mf_pool_set_batching(mf_pool* pool, const mf_batched_opts* opts);
 
 #ifdef __cplusplus

@@ -15,6 +15,9 @@
 // equal mf_apply_batch's, and a graph can alternate between the two paths.
 #include <algorithm>
 #include <chrono>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -446,6 +449,24 @@ void apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t* 
       c->stats.exact_sizes = out[cta::kOutExactSizes];
       c->stats.max_csr = c->max_csr;
       c->stats.device_ms = (double)(out[cta::kOutT1] - out[cta::kOutT0]) / 1e6;
+    }
+    // MISFIT_GB_BATCHED_DEBUG: the kernel's items of over 20 ms, one line each
+    static const bool debug = std::getenv("MISFIT_GB_BATCHED_DEBUG") != nullptr;
+    if (debug) {
+      int64_t t_first = INT64_MAX;
+      for (int64_t j = 0; j < k; ++j) t_first = std::min<int64_t>(t_first, E.h_out[cta::kOutWords * j + cta::kOutT0]);
+      for (int64_t j = 0; j < k; ++j) {
+        const int64_t* out = E.h_out + cta::kOutWords * j;
+        const double ms = (double)(out[cta::kOutT1] - out[cta::kOutT0]) / 1e6;
+        if (ms < 20.0) continue;
+        const mf_ctx* c = ctxs[kitems[j].idx];
+        std::fprintf(stderr, "[misfit_gb] batched item: n %d nnz %lld added %lld lines %lld sub-batches %lld "
+                     "exact %lld seeds %lld cands %lld start-ms %.2f ms %.2f (kernel %.2f, items %lld)\n",
+                     c->n, (long long)c->nnz, (long long)out[cta::kOutATotal], (long long)m[kitems[j].idx],
+                     (long long)out[cta::kOutSubBatches], (long long)out[cta::kOutExactSizes],
+                     (long long)out[cta::kOutSeeds], (long long)out[cta::kOutCands],
+                     (double)(out[cta::kOutT0] - t_first) / 1e6, ms, (double)kms, (long long)k);
+      }
     }
     if (!bad_items.empty()) {
       std::string msg = "batched kernel reported an inconsistent state for batch";

@@ -640,6 +640,10 @@ struct mf_ctx {
   // lower than the memory-derived ones (MISFIT_GB_EXACT_CAPS=dense,pairs at
   // context creation; 0 = not lowered): small graphs then take the retry path
   int64_t exact_cap_dense = 0, exact_cap_pairs = 0;
+  // outcomes of the tighter size bound (bit 0 = last: it settled the
+  // sub-batch), how often it ran, and the sub-batches it was skipped on
+  uint32_t bound_hist = 0;
+  int64_t bound_tries = 0, bound_skips = 0;
   mf::DBuf<unsigned long long> fpos;   // first-hit positions
   mf::DBuf<int32_t> un_idx, un_v, need, needv, live_i, live_v, nlist_need;
   mf::DBuf<uint32_t> nmark;            // epoch marks: neighbours of seeds needing their hop-2 part

@@ -14,6 +14,8 @@
 //     rows), so a graph's results do not depend on how often it moved.
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <condition_variable>
 #include <deque>
 #include <mutex>
@@ -221,17 +223,36 @@ struct mf_pool {
     }
   }
 
+  // Whether a request goes to the batched kernel: within the size and vertex
+  // limits and, since one CTA walks the batch's 2-hop neighbourhoods (about
+  // lines * (1 + mean degree)^2 positions), on a graph whose current mean
+  // degree, overlay included, keeps that walk within the limit's at mean
+  // degree 32.  A small graph that takes many insert-heavy requests grows
+  // dense (added entries accumulate in its overlay); its requests then go to
+  // the workers, whose launches spread the walk over the whole GPU.
   bool small(const Graph& gr, const Request* rq) const {
-    return (int64_t)rq->u.size() <= bopts.max_cta_updates && gr.ctx->n <= bopts.max_cta_vertices &&
-           !gr.ctx->exact;
+    const mf_ctx* c = gr.ctx;
+    const int64_t lines = (int64_t)rq->u.size();
+    if (lines > bopts.max_cta_updates || c->n > bopts.max_cta_vertices || c->exact) return false;
+    const double avg = c->n > 0 ? (double)(c->nnz + c->a_total) / (double)c->n : 0.0;
+    return (double)lines * (1.0 + avg) * (1.0 + avg) <= (double)bopts.max_cta_updates * 33.0 * 33.0;
+  }
+
+  // Whether the dispatcher takes the graph's front request: batching on, the
+  // request small, and the graph resident.  A graph evicted to host memory
+  // goes to the workers, which restore graphs concurrently; restored inside
+  // a step, it would hold up every other graph of the step (and the hot
+  // graphs' queues behind them, one request per step).
+  bool for_dispatcher(const Graph& gr) const {
+    return batching && gr.resident && !gr.queue.empty() && small(gr, gr.queue.front());
   }
 
   // A graph with a queued batch and none running becomes ready: for the
-  // dispatcher when batching is on and its front batch is small, else for
-  // the workers.  Called with the lock held.
+  // dispatcher (for_dispatcher), else for the workers.  Called with the
+  // lock held.
   void enqueue_ready(int32_t gid) {
     const Graph& gr = graphs[(size_t)gid];
-    if (batching && !gr.queue.empty() && small(gr, gr.queue.front())) {
+    if (for_dispatcher(gr)) {
       ready_small.push_back(gid);
       cv_batch.notify_one();
     } else {
@@ -252,7 +273,7 @@ struct mf_pool {
         ready_small.pop_front();
         Graph& x = graphs[(size_t)g];
         if (x.busy || x.queue.empty()) continue;
-        if (!batching || !small(x, x.queue.front())) {
+        if (!for_dispatcher(x)) {
           ready.push_back(g);
           cv_work.notify_one();
           continue;
@@ -266,6 +287,10 @@ struct mf_pool {
 
   // One batched step over the front requests of `group` (graphs marked busy).
   void run_group(std::unique_lock<std::mutex>& lk, const std::vector<int32_t>& group) {
+    // MISFIT_GB_POOL_DEBUG: one line per batched step (sizes and times)
+    static const bool debug = std::getenv("MISFIT_GB_POOL_DEBUG") != nullptr;
+    const double t_begin = mf::now_ms_host();
+    int restored = 0;
     const size_t k = group.size();
     std::vector<int> status(k, MF_OK);
     std::vector<std::string> err(k);
@@ -299,6 +324,7 @@ struct mf_pool {
         x.resident = true;
         resident_bytes += x.bytes;
         st.restores += 1;
+        ++restored;
       }
     }
     std::vector<mf_ctx*> ctxs;
@@ -319,10 +345,18 @@ struct mf_pool {
     lk.unlock();
     int rc = MF_OK;
     std::string rerr;
+    mf_batched_stats bst{};
     if (!ctxs.empty()) {
       rc = mf_apply_batches(ctxs.data(), us.data(), vs.data(), is.data(), ms.data(), (int64_t)ctxs.size(), &opts,
-                            nullptr);
+                            &bst);
       if (rc != MF_OK) rerr = mf_last_error();
+    }
+    if (debug) {
+      int64_t lines = 0;
+      for (const int64_t x : ms) lines += x;
+      std::fprintf(stderr, "[misfit_gb] pool step: graphs %zu lines %lld restored %d prepare-ms %.2f apply-ms %.2f "
+                   "kernel-ms %.2f\n", ctxs.size(), (long long)lines, restored, t0 - t_begin,
+                   mf::now_ms_host() - t0, (double)bst.kernel_ms);
     }
     std::vector<int64_t> bytes(k, -1);
     for (size_t j = 0; j < k; ++j)

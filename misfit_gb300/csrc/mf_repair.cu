@@ -3255,13 +3255,24 @@ void process_batch(mf_ctx* c, int64_t m) {
       // The limit grows only if the packed total reaches it.  A tighter upper
       // bound (exact sizes except for the light part of dense seeds) settles
       // most of these sub-batches; the exact sizes follow only if it does not.
+      // Where the bound has stopped settling them (hub-dominated graphs, whose
+      // packed totals sit at the limit), it is tried on one sub-batch in
+      // eight only, and the exact sizes are computed directly; either way
+      // the growth comes from exact sizes, so results do not depend on it.
       sc.emplace(c, kStExact);
-      exact_sizes(c, ns, ep, true);
       MF_K(k_cand_lens<<<grid_for(nct), kTB, 0, s>>>(g, c->cands.p, nct, c->rowlens.p + ns));
-      scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
-      MF_CUDA(cudaMemcpyAsync(h + 6, c->i64a.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-      MF_CUDA(cudaStreamSynchronize(s));
-      if (h[6] >= c->max_csr) {
+      const bool bound_useful = c->bound_tries < 8 || __builtin_popcount(c->bound_hist & 0xffu) >= 2;
+      bool settled = false;
+      if (bound_useful || (++c->bound_skips & 7) == 0) {
+        exact_sizes(c, ns, ep, true);
+        scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
+        MF_CUDA(cudaMemcpyAsync(h + 6, c->i64a.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        MF_CUDA(cudaStreamSynchronize(s));
+        settled = h[6] < c->max_csr;
+        c->bound_hist = (c->bound_hist << 1) | (settled ? 1u : 0u);
+        ++c->bound_tries;
+      }
+      if (!settled) {
         exact_sizes(c, ns, ep, false);
         scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
         h[5] = c->max_csr;
