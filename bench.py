@@ -51,6 +51,11 @@ UNIT = "updates/s"
 # printed with MISFIT_GB_DEBUG=2).  ncu flushes the caches before each
 # launch, so this is a cold-L2 figure; 12 bytes per element are algorithmic.
 PUSH_HOP_DRAM_BYTES_PER_ELEMENT = 13.95
+# DRAM bytes (read + write) per launch of k_pull_cand on this workload: ncu
+# over the kernel's launches 100-102 of the bench's first batch (cold L2),
+# 699,086,592 bytes in three launches.  Its launches read every vertex's row
+# bounds, so their traffic hardly varies from one sub-batch to the next.
+PULL_DRAM_BYTES_PER_LAUNCH = 233028864
 
 
 def parse_args():
@@ -861,10 +866,12 @@ def main():
                  "violations_after": int(viol), "uncovered_after": int(unc),
                  "timing": "library CUDA events per batch, host-buffer batches"}
 
-    # ---- roofline of the dominant kernel, k_lb_push_hop (the hop-2 reach of
-    # the clustering write): algorithmic bytes = 12 B per pushed element
-    # (4 B row entry read + 4 B state read + 4 B cid write), timed by CUDA
-    # events around each of its launches on the library's stream.
+    # ---- roofline of the two largest kernels, each timed by CUDA events
+    # around its launches on the library's stream inside the timed region:
+    # k_lb_push_hop (the hop-2 reach of the clustering write), 12 B per
+    # pushed element (4 B row entry read + 4 B state read + 4 B cid write),
+    # and the candidates' pull (k_pull_cand), 28 B per vertex + 4 B per row
+    # entry read.  The one with more device time is the line's "roofline".
     peak, peak_kind = measured_peaks()
     ms, calls, nbytes = prof["push_hop"]
     achieved = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
@@ -901,6 +908,24 @@ def main():
                    "mean device time",
     }
     roof["batch_frac"] = roof["batch"]["frac"]
+    ms_p, calls_p, bytes_p = prof.get("pull", (0.0, 0, 0.0))
+    if ms_p > 0:
+        ach_p = bytes_p / (ms_p / 1e3) / 1e9
+        pull = {"bound": "hbm", "achieved": ach_p, "peak": peak, "unit": "GB/s", "frac": ach_p / peak,
+                "traffic": PULL_DRAM_BYTES_PER_LAUNCH, "kernel": "k_pull_cand", "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": bytes_p / max(calls_p, 1), "avg_launch_ms": ms_p / max(calls_p, 1),
+                "launches": int(calls_p),
+                "timed": "per sub-batch: k_cand_bits, k_pull_cand and k_pull_cand_long (the pull step)",
+                "bytes_note": "28 B per vertex (row bounds, tombstone count, tag, id) + 4 B per row entry read "
+                              "(device counter)",
+                "traffic_note": "DRAM bytes per launch of k_pull_cand from an ncu capture of this workload "
+                                "(cold L2)" if PULL_DRAM_BYTES_PER_LAUNCH else "not captured"}
+        push_hop = roof
+        if ms_p > ms:
+            roof = dict(pull, batch=push_hop.pop("batch"), batch_frac=push_hop.pop("batch_frac"))
+            roof["next"] = push_hop
+        else:
+            roof["next"] = pull
 
     line = {
         "metric": METRIC, "value_is": VALUE_IS, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -911,7 +936,8 @@ def main():
         "wall_s_timed": wall, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
         "stage_ms": {k: round(v[0], 3) for k, v in stage_prof.items()}, "slowest_stage": top[0],
         "stage_ms_note": "one untimed batch after the timed ones, every stage timed with CUDA events "
-                         "(the push_hop launches are timed apart from the rest of cluster_write)",
+                         "(the push_hop launches and the pull step are timed apart from the rest of "
+                         "cluster_write)",
     }
     if e2e:
         line["e2e"] = e2e

@@ -271,8 +271,9 @@ void mf_free(void* p);
 const char* mf_stage_name(int stage);
 /* on = 1: every later batch records CUDA events around each stage on the
  * context's stream; times accumulate until mf_profile_reset.  on = 2: only
- * the k_lb_push_hop launches are timed (the "push_hop" stage), which costs
- * four event records per sub-batch instead of about fifty.  on = 0: off.
+ * the k_lb_push_hop launches (the "push_hop" stage) and the candidates'
+ * pull (the "pull" stage: k_cand_bits, k_pull_cand, k_pull_cand_long) are
+ * timed, six event records per sub-batch instead of about fifty.  on = 0: off.
  * Adding 4 (on = 4, 5, 6) also counts each batch's algorithmic work
  * (mf_batch_stats.packed_total / row_degree_total): every sub-batch then
  * computes its exact 2-hop sizes, which costs device time, so a batch timed
@@ -281,7 +282,8 @@ int mf_profile_enable(mf_ctx* ctx, int on);
 int mf_profile_reset(mf_ctx* ctx);
 /* Accumulated device milliseconds, occurrences and algorithmic bytes per
  * stage (cap entries; bytes may be NULL).  Bytes are counted for the stages
- * with a device work counter (hop1, cluster_write) and are 0 elsewhere. */
+ * with a device work counter (hop1, cluster_write, push_hop, pull) and are 0
+ * elsewhere. */
 int mf_profile_read(mf_ctx* ctx, double* ms, int64_t* calls, double* bytes, int cap);
 /* Kernels launched by this library in this process so far. */
 int64_t mf_kernel_launches(void);

@@ -252,8 +252,11 @@ void run_batch(mf_ctx* c, int64_t m) {
     unsigned long long w[2 * mf::kStCount + 8];
     MF_CUDA(cudaMemcpy(w, c->work.p, sizeof(w), cudaMemcpyDeviceToHost));
     const unsigned long long* x = w + 2 * mf::kStCount;
-    // 4 B row entry + 8 B state read and cid write per pushed element
-    c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + x[2]);
+    // 4 B row entry + 8 B state read and cid write per pushed element; in
+    // the pull form the candidates' counter is the row entries the pull read
+    const bool pull_form = c->symmetric && c->rows_sorted && c->tune.cand_push == 0;
+    c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + (pull_form ? 0ull : x[2]));
+    if (pull_form) c->stage_bytes[mf::kStPull] += 4.0 * (double)x[2];
     c->stage_bytes[mf::kStPushHop] += 12.0 * (double)x[1];
     if (debug) {
       std::fprintf(stderr, "[misfit_gb] batch: push elements seed %llu hop %llu cand %llu; sub-batches %lld\n", x[0],

@@ -658,7 +658,7 @@ struct mf_ctx {
   std::vector<SubBatchTrace> traces;
 
   // optional per-stage CUDA-event profiling
-  int profile = 0;                     // 0 off, 1 all stages, 2 the push_hop stage only
+  int profile = 0;                     // 0 off, 1 all stages, 2 the push_hop and pull stages only
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   std::vector<std::pair<int, size_t>> ev_marks;
@@ -782,7 +782,8 @@ struct StageScope {
   size_t first = 0;
   bool on;
   StageScope(mf_ctx* ctx, int st)
-      : c(ctx), stage(st), on((ctx->profile & 3) == 1 || ((ctx->profile & 3) == 2 && st == kStPushHop)) {
+      : c(ctx), stage(st),
+        on((ctx->profile & 3) == 1 || ((ctx->profile & 3) == 2 && (st == kStPushHop || st == kStPull))) {
     if (!on) return;
     if (c->ev_used + 2 > c->ev_pool.size()) {
       for (int k = 0; k < 64; ++k) {

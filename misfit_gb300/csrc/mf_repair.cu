@@ -3390,6 +3390,9 @@ void process_batch(mf_ctx* c, int64_t m) {
                         ucnt + 36, wk_extra + 2, c->tune.pull_long};
       MF_K(launch_pdl(k_pull_cand, grid_for(n), kTB, 0, s, pa));
       MF_K(launch_pdl(k_pull_cand_long, lb_grid(c, k_pull_cand_long), kTB, 0, s, pa));
+      // per vertex: row bounds (8 B of nindex, 8 B of aoff), tombstone count,
+      // tag and id (4 B each); the row entries read are counted on the device
+      if (c->profile) c->stage_bytes[kStPull] += 28.0 * (double)n;
     } else {
       row_offsets(c, c->cands.p, nct, kCntCandRows, ns, ep);
       MF_K(launch_pdl(k_lb_push_cand, lb_grid(c, k_lb_push_cand), kTB, 0, s, g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,

@@ -382,7 +382,8 @@ class Graph:
         _check(_lib().mf_compact(self._h, os.fsencode(path), 1 if rebase else 0), "mf_compact")
 
     def profile(self, on=True):
-        """True/1: all stages; 2: the k_lb_push_hop launches only; False/0: off;
+        """True/1: all stages; 2: the k_lb_push_hop launches and the
+        candidates' pull only; False/0: off;
         adding 4 also counts each batch's algorithmic work (stats packed_total,
         row_degree_total), at the cost of exact 2-hop sizes in every sub-batch."""
         level = 1 if on is True else (0 if on is False else int(on))
