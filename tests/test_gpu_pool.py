@@ -153,3 +153,34 @@ def test_pool_drain_wakes_after_eviction(gpu_lib):
                 assert np.array_equal(pool.get_mis(gid), plans[k][2][b]), (b, k)
         st = pool.stats()
     assert st["errors"] == 0 and st["evictions"] > 0
+
+
+def test_pool_batched_dispatch_leaves_dense_graphs_to_workers(gpu_lib):
+    """Continuous batching gives the dispatcher a request only while one CTA's
+    walk of its 2-hop neighbourhoods stays small: lines * (1 + mean degree)^2
+    within max_cta_updates * 33^2.  On a dense graph (mean degree ~95) the
+    200-line requests go to the workers and the 20-line ones to the
+    dispatcher; memberships equal the dedicated context's either way."""
+    n = 120
+    ni, nl = W.er_graph(n, 95.0, 77)
+    g = native.Graph.from_csr(ni, nl)
+    mis0 = g.greedy_mis()
+    g.set_mis(mis0)
+    ts = W.ToggleStream(n, ni, nl, 78)
+    reqs, after = [], []
+    for size in (200, 20, 200, 20, 200, 20):
+        u, v = ts.next_batch(size)
+        ins = g.flag_updates(u, v)
+        g.apply_batch(u, v, ins)
+        reqs.append((u, v, ins))
+        after.append(g.get_mis())
+    g.close()
+    with native.Pool(1 << 30, workers=2) as pool:
+        pool.set_batching(native.batched_opts(max_cta_updates=512))
+        gid = pool.add_graph(ni, nl, mis0)
+        for k, (u, v, ins) in enumerate(reqs):
+            assert pool.wait(pool.submit(gid, u, v, ins)) >= 0
+            assert np.array_equal(pool.get_mis(gid), after[k]), k
+        st = pool.stats()
+    assert st["completed"] == len(reqs)
+    assert st["batched_requests"] == 3
