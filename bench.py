@@ -310,7 +310,9 @@ def run_large(args, local):
     a batch with hub endpoints packs 2-hop lists of tens of millions of
     entries per seed, so the leg times a bounded sample: consecutive
     prefixes of the first batch (25 lines, then doubling), each applied as a
-    batch, while the next prefix's expected device time fits the budget;
+    batch, until a quarter of the budget of device time is spent; then one
+    last prefix sized to fill the rest, the largest (a batch keeps its
+    exact 2-hop sizes for all its sub-batches, as a full batch would);
     then one more 25-line prefix in exact-MIS mode, after which the
     membership is checked for independence and maximality on the whole
     graph."""
@@ -370,9 +372,14 @@ def run_large(args, local):
         while done < u.size:
             k = min(chunk, u.size - done)
             if samples:
-                # the next prefix's expected time from the last one's per-line time
+                # the next prefix's expected time from the last one's per-line
+                # time; the last prefix takes what fits in the rest of the budget
                 last = samples[-1]
-                if dev_ms + last["device_ms"] / last["lines"] * k > budget_ms:
+                per_line = last["device_ms"] / last["lines"]
+                fit = int(0.85 * (budget_ms - dev_ms) / per_line)
+                # past a quarter of the budget, one last prefix takes the rest
+                k = min(fit if dev_ms >= budget_ms / 4 else min(k, fit), u.size - done)
+                if k < 25:
                     break
             g.apply_batch(u[done:done + k], v[done:done + k], ins[done:done + k])
             st = g.stats()
@@ -390,7 +397,8 @@ def run_large(args, local):
                     "projected_s_per_batch": args.large_batch / rate,
                     "stage_ms": {s: round(x[0], 1) for s, x in prof.items() if x[0] > 0},
                     "timing": "library CUDA events per applied prefix (host-buffer batches); prefixes of 25 "
-                              "lines, doubling, while the next one's expected device time fits the budget"})
+                              "lines, doubling, until a quarter of the budget is spent, then one prefix "
+                              "sized to fill the rest"})
         ms, calls, nbytes = prof["push_hop"]
         peak, peak_kind = measured_peaks()
         if ms > 0:
