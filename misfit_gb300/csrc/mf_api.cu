@@ -491,7 +491,7 @@ mf_ctx* open_egr(const char* path, int gpu) {
     c->header_edges = h.edges;
     // nlist: read through two pinned chunks, copied asynchronously.
     const int64_t nnz = (int64_t)h.edges;
-    c->nlist.reserve(std::max<int64_t>(nnz, 1));
+    c->nlist.reserve(nnz + mf::kNlistPad);
     const size_t chunk = (size_t)64 << 20;
     void* pin[2] = {nullptr, nullptr};
     cudaEvent_t done[2];

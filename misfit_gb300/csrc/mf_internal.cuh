@@ -175,6 +175,11 @@ struct DBuf {
 
 struct AsyncQueue;   // mf_api.cu
 
+// Entries past the end of the row array (nlist): bulk copies start on the
+// 16-byte boundary at or below a span and end on the one at or above it, so
+// they may read up to 12 bytes beyond the last entry.
+constexpr int64_t kNlistPad = 4;
+
 // ---- read-only view of the current graph ----------------------------------
 
 struct GraphView {

@@ -422,7 +422,7 @@ void upload_base(mf_ctx* c, int32_t n, const int64_t* nindex, const int32_t* nli
   c->n = n;
   c->nnz = nnz;
   c->nindex.reserve((int64_t)n + 1);
-  c->nlist.reserve(nnz);
+  c->nlist.reserve(nnz + kNlistPad);
   if (nindex) MF_CUDA(cudaMemcpyAsync(c->nindex.p, nindex, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, s));
   if (nlist && nnz > 0) MF_CUDA(cudaMemcpyAsync(c->nlist.p, nlist, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, s));
   const int64_t words = (nnz + 31) / 32;

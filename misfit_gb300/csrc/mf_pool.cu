@@ -88,6 +88,7 @@ void restore(mf_ctx* c, const PinnedSnapshot& snap) {
   const int64_t n = c->n, words = (c->nnz + 31) / 32;
   size_t part = 0;
   load(snap, part, c->nindex, n + 1, s);
+  c->nlist.reserve(c->nnz + mf::kNlistPad);
   load(snap, part, c->nlist, c->nnz, s);
   load(snap, part, c->live, words, s);
   load(snap, part, c->dead, n, s);

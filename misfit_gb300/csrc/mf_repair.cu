@@ -990,30 +990,186 @@ __global__ void __launch_bounds__(256) k_p2_rows(GraphView g, const uint32_t* ma
   p2_flush(acc, s_cnt, counts);
 }
 
-// Chunk tasks of the huge rows, one warp each: the chunk's OR goes to racc
-// of its row's slot.
+// ---- bulk staging of row spans (cp.async.bulk, completion on an mbarrier) ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// One thread: bytes expected on bar, then the copy global -> shared that
+// completes them.  dst, src and bytes are multiples of 16 (callers check).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+// Wait for the phase of bar with parity `parity`; false after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int64_t limit) {
+  for (int64_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+constexpr int kP2Sub = 512;                  // positions per staged span of a chunk task
+constexpr int kP2SubBuf = kP2Sub + 8;        // room for the 16-byte rounding at both ends
+constexpr int64_t kBulkPolls = (int64_t)1 << 22;
+
+// A staged span: positions [p0, p1) of row x; the base entries in
+// [p0, min(p1, nb)) sit in the buffer from entry `lead` on (copied from the
+// 16-byte boundary at or below their address), the rest are added entries.
+struct P2Span {
+  int64_t slot, p0, p1, b, nb, ab;
+  int32_t x, lead;
+  bool dead, copied, valid;
+};
+
+// Chunk tasks of the huge rows, one warp each, split into spans of kP2Sub
+// positions; the chunk's OR goes to racc of its row's slot.  With `bulk`,
+// the base-row ids of the warp's next span are copied into shared memory by
+// the bulk-copy engine while the current span is processed (two buffers,
+// one mbarrier each); every copy starts on a 16-byte boundary of the row
+// array (rounded down, its length rounded up; the array carries 16 bytes of
+// padding).  Without it the ids are read with plain loads.  (At R-MAT scale
+// 26 both take the same time: the span's filter and mask loads, which
+// depend on the ids, bound the pass.)  A wait that runs out sets *err and
+// the warp stops, after a bounded wait for its copy still in flight.
 template <int SW>
-__global__ void __launch_bounds__(256) k_p2_huge(GraphView g, const uint32_t* mask, const uint32_t* filt,
-                                                 P2Work wk, uint32_t* racc) {
-  const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) k_p2_huge(GraphView g, const uint32_t* mask, const uint32_t* filt, P2Work wk,
+                                                 uint32_t* racc, bool bulk, unsigned long long* err) {
+  extern __shared__ __align__(16) unsigned char p2_smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  int32_t* bufs = reinterpret_cast<int32_t*>(p2_smem) + (int64_t)wib * 2 * kP2SubBuf;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(p2_smem + (size_t)nwb * 2 * kP2SubBuf * 4) + wib * 2;
+  if (lane == 0) {
+    mbar_init(bars, 1);
+    mbar_init(bars + 1, 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  uint32_t parity[2] = {0u, 0u};
   const int64_t total = min((int64_t)*wk.ntasks, wk.tcap);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = warp_id(); t < total; t += nw) {
+  // span after (t, sub) in this warp's sequence: next sub of the task, else
+  // the first of the warp's next task
+  auto describe = [&](int64_t t, int64_t sub) {
+    P2Span sp{};
+    sp.valid = false;
+    if (t >= total) return sp;
     const int64_t task = wk.tasks[t];
-    const int64_t i = task >> 32;
-    const int64_t c = task & 0xffffffffll;
-    if (i >= wk.hcap) continue;   // never: hcap bounds the rows over kP2Huge positions
+    const int64_t i = task >> 32, c = task & 0xffffffffll;
+    if (i >= wk.hcap) return sp;   // never: hcap bounds the rows over kP2Huge positions
     const int32_t x = wk.huge[i];
-    const int64_t tot = (g.nindex[x + 1] - g.nindex[x]) + (g.aoff[x + 1] - g.aoff[x]);
-    const int64_t p0 = c * kP2Chunk;
-    uint32_t r[SW];
+    const int64_t b = g.nindex[x], nb = g.nindex[x + 1] - b;
+    const int64_t ab = g.aoff[x], tot = nb + (g.aoff[x + 1] - ab);
+    const int64_t c0 = c * kP2Chunk, c1 = min(tot, c0 + kP2Chunk);
+    sp.p0 = c0 + sub * kP2Sub;
+    if (sp.p0 >= c1) return sp;
+    sp.p1 = min(c1, sp.p0 + kP2Sub);
+    sp.slot = i;
+    sp.x = x;
+    sp.b = b;
+    sp.nb = nb;
+    sp.ab = ab;
+    sp.dead = g.dead[x] != 0;
+    sp.valid = true;
+    return sp;
+  };
+  auto issue = [&](P2Span& sp, int buf) {
+    sp.copied = false;
+    sp.lead = 0;
+    const int64_t e = min(sp.p1, sp.nb);
+    if (!bulk || sp.p0 >= e) return;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(g.nlist + sp.b + sp.p0);
+    const uintptr_t a0 = a & ~(uintptr_t)15;
+    const uint32_t bytes = (uint32_t)(((a + 4 * (uintptr_t)(e - sp.p0) - a0) + 15) & ~(uintptr_t)15);
+    int32_t* dst = bufs + buf * kP2SubBuf;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) != 0 || bytes > 4u * kP2SubBuf) return;   // never: plain loads then
+    sp.lead = (int32_t)((a - a0) >> 2);
+    sp.copied = true;
+    if (lane == 0) bulk_load(dst, reinterpret_cast<const void*>(a0), bytes, bars + buf);
+  };
+  int64_t t = warp_id(), sub = 0;
+  P2Span cur = describe(t, sub);
+  int slot = 0;
+  if (cur.valid) issue(cur, slot);
+  uint32_t r[SW];
 #pragma unroll
-    for (int w = 0; w < SW; ++w) r[w] = 0;
-    p2_warp_span(g, mask, filt, x, p0, min(tot, p0 + kP2Chunk), r);
-    p2_warp_or(r);
+  for (int w = 0; w < SW; ++w) r[w] = 0;
+  bool failed = false;
+  while (cur.valid) {
+    int64_t nt = t, ns = sub + 1;
+    P2Span nxt = describe(nt, ns);
+    if (!nxt.valid) {
+      nt = t + nw;
+      ns = 0;
+      nxt = describe(nt, ns);
+    }
+    if (nxt.valid) issue(nxt, slot ^ 1);
+    if (cur.copied) {
+      if (!mbar_wait(bars + slot, parity[slot], kBulkPolls)) {
+        failed = true;
+        if (lane == 0) atomicExch(err, 1ull);
+        break;
+      }
+      parity[slot] ^= 1u;
+    }
+    const int32_t* sb = bufs + slot * kP2SubBuf + cur.lead;
+    const int64_t e = min(cur.p1, cur.nb);
+    for (int64_t k0 = cur.p0 + lane; k0 < cur.p1; k0 += 128) {
+      int32_t y[4];
 #pragma unroll
-    for (int w = 0; w < SW; ++w)
-      if (lane == w && r[w]) atomicOr(racc + i * SW + w, r[w]);
+      for (int q = 0; q < 4; ++q) {
+        const int64_t k = k0 + 32 * q;
+        y[q] = -1;
+        if (k < cur.p1) {
+          if (k < e) {
+            if (!cur.dead || live_at(g.live, cur.b + k))
+              y[q] = cur.copied ? sb[k - cur.p0] : __ldg(g.nlist + cur.b + k);
+          } else {
+            y[q] = g.aadj[cur.ab + (k - cur.nb)];
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (y[q] >= 0 && !p2_in(filt, y[q])) y[q] = -1;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (y[q] >= 0) p2_or(r, mask, y[q]);
+    }
+    __syncwarp();
+    // the task's OR goes out after its last span
+    if (!nxt.valid || nt != t) {
+      p2_warp_or(r);
+#pragma unroll
+      for (int w = 0; w < SW; ++w) {
+        if (lane == w && r[w]) atomicOr(racc + cur.slot * SW + w, r[w]);
+        r[w] = 0;
+      }
+    }
+    cur = nxt;
+    t = nt;
+    sub = ns;
+    slot ^= 1;
+  }
+  if (failed && cur.valid) {
+    // the copy of the span after the one that ran out may still be in flight
+    int64_t nt = t, ns = sub + 1;
+    P2Span nxt = describe(nt, ns);
+    if (!nxt.valid) nxt = describe(t + nw, 0);
+    if (nxt.valid && nxt.p0 < min(nxt.p1, nxt.nb)) mbar_wait(bars + (slot ^ 1), parity[slot ^ 1], kBulkPolls);
   }
 }
 
@@ -2662,6 +2818,17 @@ bool debug_counters() {
   return on;
 }
 
+// MISFIT_GB_P2_BULK=0: the row pass's chunk tasks read their row entries
+// with plain loads instead of the bulk-copy staging (same results, same
+// speed where measured; kept for comparisons).
+bool p2_bulk_on() {
+  static const bool on = [] {
+    const char* e = std::getenv("MISFIT_GB_P2_BULK");
+    return !(e != nullptr && std::strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 // MISFIT_GB_DEBUG=2: also the elements of every k_lb_push_hop launch.
 bool debug_launches() {
   static const bool on = [] {
@@ -2691,7 +2858,7 @@ void pull_pass(mf_ctx* c, const int32_t* grp, int k, int64_t hcap, int64_t tcap)
   cudaStream_t s = c->stream;
   const GraphView g = c->view();
   const int32_t n = c->n;
-  unsigned long long* cnt = c->p2_cnt.p;   // 32*kP2MaxWords counts, then next, nhuge, ntasks
+  unsigned long long* cnt = c->p2_cnt.p;   // 32*kP2MaxWords counts, then next, nhuge, ntasks, bulk error
   unsigned long long* ctl = cnt + 32 * kP2MaxWords;
   const P2Work wk{ctl, c->p2_huge.p, ctl + 1, hcap, c->p2_tasks.p, ctl + 2, tcap};
   const int64_t fwords = ((int64_t)n + 31) / 32;
@@ -2701,7 +2868,18 @@ void pull_pass(mf_ctx* c, const int32_t* grp, int k, int64_t hcap, int64_t tcap)
   MF_K(k_p2_mark<SW><<<dim3((unsigned)k, 16), kTB, 0, s>>>(g, c->seeds.p, grp, k, c->p2_mask.p, c->p2_filt.p));
   MF_K(k_p2_rows<SW><<<lb_grid(c, k_p2_rows<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, cnt, wk));
   MF_CUDA(cudaMemsetAsync(c->p2_racc.p, 0, sizeof(uint32_t) * (size_t)hcap * SW, s));
-  MF_K(k_p2_huge<SW><<<lb_grid(c, k_p2_huge<SW>), kTB, 0, s>>>(g, c->p2_mask.p, c->p2_filt.p, wk, c->p2_racc.p));
+  {
+    const size_t smem = (size_t)(kTB / 32) * (2 * kP2SubBuf * 4 + 2 * 8);
+    static int grid_huge[kP2MaxWords + 1] = {};
+    if (grid_huge[SW] == 0) {
+      int sms = 0, per = 0;
+      MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+      MF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_p2_huge<SW>, kTB, smem));
+      grid_huge[SW] = sms * std::max(per, 1);
+    }
+    MF_K(k_p2_huge<SW><<<grid_huge[SW], kTB, smem, s>>>(g, c->p2_mask.p, c->p2_filt.p, wk, c->p2_racc.p,
+                                                        p2_bulk_on(), ctl + 3));
+  }
   MF_K(k_p2_huge_count<SW><<<grid_for(hcap), kTB, 0, s>>>(c->p2_mask.p, c->p2_huge.p, ctl + 1, hcap, c->p2_racc.p,
                                                             cnt));
   MF_K(k_p2_store<<<1, 256, 0, s>>>(cnt, grp, k, c->rowlens.p));
@@ -2762,12 +2940,13 @@ int64_t pull_exact(mf_ctx* c, int32_t* todo, int64_t ntodo) {
   c->p2_grp.reserve((int64_t)pull.size());
   const int first = group_sizes.front();
   c->p2_mask.reserve((int64_t)n * (first <= 32 ? 1 : first <= 64 ? 2 : first <= 128 ? 4 : 8));
-  c->p2_cnt.reserve(32 * kP2MaxWords + 3);
+  c->p2_cnt.reserve(32 * kP2MaxWords + 4);
   c->p2_filt.reserve(((int64_t)n + 31) / 32);
   c->p2_huge.reserve(hcap);
   c->p2_tasks.reserve(tcap);
   c->p2_racc.reserve(hcap * kP2MaxWords);
   MF_CUDA(cudaMemcpyAsync(c->p2_grp.p, pull.data(), sizeof(int32_t) * pull.size(), cudaMemcpyHostToDevice, s));
+  MF_CUDA(cudaMemsetAsync(c->p2_cnt.p + 32 * kP2MaxWords + 3, 0, sizeof(unsigned long long), s));
   if (!push.empty())
     MF_CUDA(cudaMemcpyAsync(todo, push.data(), sizeof(int32_t) * push.size(), cudaMemcpyHostToDevice, s));
   size_t off = 0;
@@ -2780,7 +2959,11 @@ int64_t pull_exact(mf_ctx* c, int32_t* todo, int64_t ntodo) {
     off += (size_t)k;
   }
   // the host vectors of the copies above stay alive until the stream reaches them
+  unsigned long long bulk_err = 0;
+  MF_CUDA(cudaMemcpyAsync(&bulk_err, c->p2_cnt.p + 32 * kP2MaxWords + 3, sizeof(bulk_err), cudaMemcpyDeviceToHost,
+                          s));
   MF_CUDA(cudaStreamSynchronize(s));
+  if (bulk_err) MF_FAIL(MF_ESTATE, "exact 2-hop sizes: a bulk-copy wait of the row pass ran out");
   if (dbg)
     std::fprintf(stderr, "[misfit_gb] pull sizes: seeds %lld of %lld in %zu passes, volume %.0f, positions %lld, "
                  "%.3f ms\n", (long long)pull.size(), (long long)ntodo, group_sizes.size(), pulled_vol,
