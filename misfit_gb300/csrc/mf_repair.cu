@@ -19,6 +19,7 @@
 //   highest row writes last); assignment by ascending sub-batch index (lists
 //   walked descending); clusters processed in ascending id.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -2870,15 +2871,18 @@ void pull_pass(mf_ctx* c, const int32_t* grp, int k, int64_t hcap, int64_t tcap)
   MF_CUDA(cudaMemsetAsync(c->p2_racc.p, 0, sizeof(uint32_t) * (size_t)hcap * SW, s));
   {
     const size_t smem = (size_t)(kTB / 32) * (2 * kP2SubBuf * 4 + 2 * 8);
-    static int grid_huge[kP2MaxWords + 1] = {};
-    if (grid_huge[SW] == 0) {
+    // resident blocks of this kernel (pool workers may get here at once)
+    static std::atomic<int> grid_huge{0};
+    int grid = grid_huge.load(std::memory_order_relaxed);
+    if (grid == 0) {
       int sms = 0, per = 0;
       MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
       MF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_p2_huge<SW>, kTB, smem));
-      grid_huge[SW] = sms * std::max(per, 1);
+      grid = sms * std::max(per, 1);
+      grid_huge.store(grid, std::memory_order_relaxed);
     }
-    MF_K(k_p2_huge<SW><<<grid_huge[SW], kTB, smem, s>>>(g, c->p2_mask.p, c->p2_filt.p, wk, c->p2_racc.p,
-                                                        p2_bulk_on(), ctl + 3));
+    MF_K(k_p2_huge<SW><<<grid, kTB, smem, s>>>(g, c->p2_mask.p, c->p2_filt.p, wk, c->p2_racc.p, p2_bulk_on(),
+                                               ctl + 3));
   }
   MF_K(k_p2_huge_count<SW><<<grid_for(hcap), kTB, 0, s>>>(c->p2_mask.p, c->p2_huge.p, ctl + 1, hcap, c->p2_racc.p,
                                                             cnt));
