@@ -2047,6 +2047,7 @@ __global__ void __launch_bounds__(1024) k_repair_sequential(RepairArgs a) {
 // the sequential kernel.
 
 constexpr int kMaxRounds = 48;
+constexpr int kRoundsPerSync = 2;   // small rounds queued per host read-back
 
 struct View {
   const uint8_t* m;     // bit 0: committed membership; bit 1: pending writes exist
@@ -2090,7 +2091,21 @@ struct SpecArgs {
   int64_t* pre;           // prefix sums of len(h) over row(r), nr + 1 entries per deferred edge
   unsigned long long* pre_used;
   int64_t pre_cap;
+  // rounds queued without a host read-back: [0] first pending position,
+  // [1] entries of the view, [2] 1 once no position changed, [3] rounds run
+  // (k_spec_round keeps them); p0 and view.nkeys above are then ignored
+  int64_t* dyn = nullptr;
 };
+
+// A queued round's start and view from the device; false once the repair
+// is done (the round then does nothing).
+__device__ __forceinline__ bool spec_dyn_load(SpecArgs& a) {
+  if (a.dyn == nullptr) return true;
+  if (a.dyn[2] != 0) return false;
+  a.p0 = a.dyn[0];
+  a.view.nkeys = a.dyn[1];
+  return true;
+}
 
 constexpr int32_t kDeferred = -2;
 
@@ -2295,6 +2310,7 @@ __global__ void k_spec_eval(SpecArgs a, int64_t* chunk_pre, unsigned long long* 
                             unsigned int* done) {
   pdl_wait();
   pdl_trigger();
+  if (!spec_dyn_load(a)) return;
   const int64_t wi = warp_id();
   if (wi < a.cnt - a.p0) {
     const int lane = threadIdx.x & 31;
@@ -2347,6 +2363,7 @@ __global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_
                                                         unsigned long long* best, unsigned long long* queue) {
   pdl_wait();
   pdl_trigger();
+  if (!spec_dyn_load(a)) return;
   const GraphView& g = a.g;
   const int64_t nbig = (int64_t)*a.big_count;
   const int64_t total = chunk_pre[nbig];
@@ -2606,6 +2623,11 @@ __global__ void __launch_bounds__(kRoundThreads) k_spec_round(const int32_t* n0,
                                                               const unsigned long long* best) {
   pdl_wait();
   pdl_trigger();
+  if (!spec_dyn_load(sa)) return;
+  if (sa.dyn != nullptr) {
+    p0 = sa.p0;
+    nview_old = sa.view.nkeys;
+  }
   __shared__ uint64_t s_keys[kRoundWrites];
   __shared__ uint32_t s_vals[kRoundWrites];
   __shared__ int s_warp[33];
@@ -2702,6 +2724,15 @@ __global__ void __launch_bounds__(kRoundThreads) k_spec_round(const int32_t* n0,
   if (tid == 0) {
     out[0] = f;
     out[1] = (unsigned long long)nview;
+    if (sa.dyn != nullptr) {
+      // the next queued round: after the first changed position, with this
+      // round's writes as its view; the per-round counters start over
+      sa.dyn[0] = (int64_t)f + 1;
+      sa.dyn[1] = nview;
+      sa.dyn[2] = (int64_t)f >= cnt ? 1 : 0;
+      sa.dyn[3] += 1;
+      for (int k = 0; k < 6; ++k) sa.big_count[k] = 0;   // deferrals, prefix use, queue (2), spare, done
+    }
   }
 }
 
@@ -3159,6 +3190,16 @@ bool sequential_repair_forced() {
   return forced;
 }
 
+// MISFIT_GB_REPAIR=rounds: every round read back by the host before the next
+// is queued (instead of kRoundsPerSync rounds per read-back).
+bool host_rounds_forced() {
+  static const bool forced = [] {
+    const char* e = std::getenv("MISFIT_GB_REPAIR");
+    return e != nullptr && std::strcmp(e, "rounds") == 0;
+  }();
+  return forced;
+}
+
 // Repair of one sub-batch: c->vals holds the order (sub-batch indices),
 // nproc entries.  Returns the number of speculative rounds.
 int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t ns) {
@@ -3198,6 +3239,55 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
   MF_CUDA(cudaMemsetAsync(c->rp_w1.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
   const int nbits = bits_for(std::max<int32_t>(c->n - 1, 1));
   int64_t p0 = 0, nview = 0, rounds = 0;
+  if (nproc <= kRoundCap && !host_rounds_forced() && !debug_counters()) {
+    // Every round fits one commit block: rounds are queued kRoundsPerSync at
+    // a time and read back once; a queued round finds its start and view on
+    // the device and does nothing once the repair is done.  Round r writes
+    // into one pair of result buffers and compares with the other, in turn.
+    int64_t* dyn = c->counters.p + 58;
+    MF_CUDA(cudaMemsetAsync(dyn, 0, sizeof(int64_t) * 4, s));
+    MF_CUDA(cudaMemsetAsync(c->counters.p + 24, 0, sizeof(int64_t) * 6, s));
+    std::optional<StageScope> dsc;
+    int64_t queued = 0;
+    while (true) {
+      const int64_t k = std::min<int64_t>(kRoundsPerSync, kMaxRounds - queued);
+      for (int64_t j = 0; j < k; ++j, ++queued) {
+        const bool even = (queued & 1) == 0;
+        int32_t* o0 = even ? c->rp_n0.p : c->rp_w0.p;
+        int32_t* o1 = even ? c->rp_n1.p : c->rp_w1.p;
+        int32_t* r0 = even ? c->rp_w0.p : c->rp_n0.p;
+        int32_t* r1 = even ? c->rp_w1.p : c->rp_n1.p;
+        SpecArgs a{g, c->bu.p, c->bv.p, c->bins.p, p, order, 0, nproc, ns, c->v2i.p,
+                   View{c->mis.p, c->rp_keys.p, c->rp_vals.p, 0}, o0, o1, c->tune.big_threshold, ucnt + 24,
+                   c->big_pos.p, c->big_r.p, c->big_off.p, c->big_nr.p, c->big_pre.p, ucnt + 25, c->big_pre.cap,
+                   dyn};
+        dsc.emplace(c, kStRepair);
+        MF_K(launch_pdl(k_spec_eval, warps_grid(nproc), kTB, 0, s, a, c->big_chunks.p, c->big_best.p, ucnt + 26,
+                        reinterpret_cast<unsigned int*>(ucnt + 29)));
+        dsc.emplace(c, kStRepairBig);
+        MF_K(launch_pdl(k_big_scan, (unsigned)c->big_grid, kBigChunk, 0, s, a, c->big_chunks.p, c->big_best.p,
+                        ucnt + 26));
+        dsc.emplace(c, kStRepair);
+        MF_K(launch_pdl(k_spec_round, 1, kRoundThreads, 0, s, o0, o1, r0, r1, (int64_t)0, nproc, c->bins.p, p, order,
+                        c->rp_keys.p, c->rp_vals.p, (int64_t)0, c->mis.p, ucnt + 20, a, c->big_best.p));
+      }
+      MF_CUDA(cudaMemcpyAsync(h + 58, dyn, sizeof(int64_t) * 4, cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaStreamSynchronize(s));
+      dsc.reset();
+      if (h[60] != 0) break;
+      if (queued >= kMaxRounds) {
+        // round limit: the rest in order by the sequential kernel
+        p0 = h[58];
+        nview = h[59];
+        if (nview > 0) MF_K(k_spec_clear_flags<<<grid_for(nview), kTB, 0, s>>>(c->rp_keys.p, nview, c->mis.p));
+        RepairArgs ra{g, c->bu.p, c->bv.p, c->bins.p, p, order + p0, nproc - p0, ns, c->v2i.p, c->mis.p};
+        MF_K(k_repair_sequential<<<1, 1024, 0, s>>>(ra));
+        MF_CUDA(cudaGetLastError());
+        break;
+      }
+    }
+    return h[61];
+  }
   int64_t dbg_big = 0, dbg_chunks = 0, dbg_scanned = 0;
   std::optional<StageScope> rsc;
   rsc.emplace(c, kStRepair);

@@ -398,11 +398,16 @@ print("ok")
 
 
 @pytest.mark.parametrize("mode,env", [("sequential", {"MISFIT_GB_REPAIR": "sequential"}),
-                                      ("grid", {"MISFIT_GB_BIG_THRESHOLD": "0"})])
+                                      ("grid", {"MISFIT_GB_BIG_THRESHOLD": "0"}),
+                                      ("host_rounds", {"MISFIT_GB_REPAIR": "rounds"}),
+                                      ("host_rounds_grid", {"MISFIT_GB_REPAIR": "rounds",
+                                                            "MISFIT_GB_BIG_THRESHOLD": "0"})])
 def test_repair_variants_match(mode, env, gpu_lib, tmp_path):
-    """The single-CTA sequential repair (the fallback after the round limit)
-    and the grid-wide hop-2 search (forced for every long search by a tiny
-    threshold) both give the oracle's results on a whole stream."""
+    """The single-CTA sequential repair (the fallback after the round limit),
+    the grid-wide hop-2 search (forced for every long search by a tiny
+    threshold) and the host-driven rounds (each read back before the next is
+    queued, where every other test queues two per read-back) all give the
+    oracle's results on a whole stream."""
     import os
     import subprocess
     import sys
