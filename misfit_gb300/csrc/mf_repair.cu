@@ -1588,11 +1588,19 @@ __global__ void k_need_decide(GraphView g, const int32_t* need, const int32_t* n
   }
 }
 
-__global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid) {
+// New cluster ids by ascending row index; the seed rows that write (not
+// skipped) also take phase 1 of the clustering write here: bval[s] = max tag
+// of those rows with s = their own vertex (the rest of phase 1 is
+// k_lb_push_seed).  A skipped row stays skipped whatever its id.
+__global__ void k_new_ids(int64_t rows, const int64_t* pos, int32_t* rowcid, const int32_t* seeds, int64_t ns,
+                          uint32_t epoch, uint32_t* bval) {
   pdl_wait();
   pdl_trigger();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < rows && rowcid[i] == -1) rowcid[i] = (int32_t)pos[i];
+  if (i >= rows) return;
+  const int32_t rc = rowcid[i];
+  if (rc == -1) rowcid[i] = (int32_t)pos[i];
+  if (i < ns && rc != kSkip) atomicMax(bval + seeds[i], (epoch << kRowBits) | (uint32_t)i);
 }
 
 // The pushes are reductions whose results are not read back, so they issue
@@ -1605,13 +1613,8 @@ __device__ __forceinline__ void push_w(uint32_t* wval, int32_t y, uint32_t tag) 
   if (wval[y] < tag) atomicMax(wval + y, tag);
 }
 
-// Phase 1: bval[y] = max tag of the non-skipped seed rows with y in {s} u row(s).
-__global__ void k_seed_self(const int32_t* seeds, int64_t ns, const int32_t* rowcid, uint32_t epoch, uint32_t* bval) {
-  pdl_wait();
-  pdl_trigger();
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < ns && rowcid[i] != kSkip) atomicMax(bval + seeds[i], (epoch << kRowBits) | (uint32_t)i);
-}
+// Phase 1: bval[y] = max tag of the non-skipped seed rows with y in {s} u
+// row(s): the seeds themselves in k_new_ids, their rows here.
 
 __global__ void k_lb_push_seed(GraphView g, const int32_t* seeds, const int64_t* offs, int64_t ns, uint32_t epoch,
                                uint32_t* bval, unsigned long long* work) {
@@ -1627,12 +1630,16 @@ __global__ void k_lb_push_seed(GraphView g, const int32_t* seeds, const int64_t*
 
 // Phase 2: wval[y] = max over x with y in {x} u row(x) of bval[x] (the 2-hop
 // reach of the seed rows), and the candidate rows' own tags over row(c).
-__global__ void k_self_push(const int32_t* list, int64_t cnt, uint32_t epoch, const uint32_t* bval, uint32_t* wval) {
+// Every vertex of list a (cnt_a) and list b (cnt_b) pushes its own phase-1
+// tag, when it has one of this epoch, to itself (one launch for the seeds
+// and the hop-1 vertices).
+__global__ void k_self_push(const int32_t* a, int64_t cnt_a, const int32_t* b, int64_t cnt_b, uint32_t epoch,
+                            const uint32_t* bval, uint32_t* wval) {
   pdl_wait();
   pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cnt) return;
-  const int32_t x = list[i];
+  if (i >= cnt_a + cnt_b) return;
+  const int32_t x = i < cnt_a ? a[i] : b[i - cnt_a];
   const uint32_t t = bval[x];
   if ((t >> kRowBits) == epoch) push_w(wval, x, t);
 }
@@ -3631,15 +3638,15 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_K(launch_pdl(k_need_decide, lb_grid(c, k_need_decide), kTB, 0, s, g, c->need.p, c->needv.p, ucnt + 34, c->fpos.p,
                                                                  c->f1.p, c->rowcid.p, c->creates.p));
     scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
-    MF_K(launch_pdl(k_new_ids, grid_for(rows), kTB, 0, s, rows, c->i64b.p, c->rowcid.p));
+    MF_K(launch_pdl(k_new_ids, grid_for(rows), kTB, 0, s, rows, c->i64b.p, c->rowcid.p, c->seeds.p, ns, ep,
+                    c->bval.p));
     MF_CUDA(cudaMemcpyAsync(h + 7, c->i64b.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     sc.emplace(c, kStPush);
     unsigned long long* wk_extra = c->work.p + 2 * kStCount;   // [0] seed, [1] hop, [2] candidate pushes
-    MF_K(launch_pdl(k_seed_self, grid_for(ns), kTB, 0, s, c->seeds.p, ns, c->rowcid.p, ep, c->bval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedRows, ns, ep);
     MF_K(launch_pdl(k_lb_push_seed, lb_grid(c, k_lb_push_seed), kTB, 0, s, g, c->seeds.p, c->lb_offs.p, ns, ep, c->bval.p, wk_extra + 0));
-    MF_K(launch_pdl(k_self_push, grid_for(ns), kTB, 0, s, c->seeds.p, ns, ep, c->bval.p, c->wval.p));
-    MF_K(launch_pdl(k_self_push, grid_for(nh), kTB, 0, s, c->hlist.p, nh, ep, c->bval.p, c->wval.p));
+    MF_K(launch_pdl(k_self_push, grid_for(ns + nh), kTB, 0, s, c->seeds.p, ns, c->hlist.p, nh, ep, c->bval.p,
+                    c->wval.p));
     row_offsets(c, c->seeds.p, ns, kCntSeedPushers, ns, ep);
     const unsigned long long dbg0 = debug_launches() ? debug_counter(c, wk_extra + 1) : 0;
     sc.emplace(c, kStPushHop);
