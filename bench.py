@@ -603,6 +603,7 @@ def run_served(args, graphs, mis0, batching, device):
         "evictions": st["evictions"], "restores": st["restores"], "scratch_trims": st["trims"],
         "continuous_batching": {"steps": c_res["stats"]["batched_steps"],
                                 "requests_in_steps": c_res["stats"]["batched_requests"],
+                                "handed_to_idle_workers": c_res["stats"]["handed_to_workers"],
                                 "settings": {k: getattr(lat_opts, k) for k, _ in lat_opts._fields_}},
         "identical_to_plain_loop": bool(same), "continuous_batching_identical_to_plain_loop": bool(same_c),
         "request_generation_s": gen_s,

@@ -69,7 +69,9 @@ typedef struct mf_batch_stats {
 
 /* Version of this ABI (major*10000 + minor*100 + patch).  1.1 added the
  * batched form (mf_apply_batches, mf_batched_*), mf_pool_set_batching and the
- * two batched_* fields at the end of mf_pool_stats. */
+ * two batched_* fields at the end of mf_pool_stats.  1.2 added
+ * mf_tuning.pull_sizes, mf_batched_opts.pool_idle_first and
+ * mf_pool_stats.handed_to_workers, each at the end of its struct. */
 int mf_version(void);
 const char* mf_status_string(int status);
 /* Last error on the calling thread ("" when none). */
@@ -337,6 +339,7 @@ typedef struct mf_pool_stats {
   int64_t peak_resident_bytes;  /* the largest value seen */
   int64_t batched_steps;        /* mf_apply_batches steps run by the batched dispatch */
   int64_t batched_requests;     /* requests those steps carried */
+  int64_t handed_to_workers;    /* small requests the dispatcher gave to idle workers */
 } mf_pool_stats;
 
 /* A pool on device `gpu` that keeps at most `hbm_budget` bytes of graph state
@@ -384,6 +387,9 @@ typedef struct mf_batched_opts {
   int use_graph;              /* 1: capture the step as a CUDA graph (default), 0: plain launches */
   int path_threads;           /* host threads driving the batches above the kernel's limits, each
                                  graph on its own stream (1..64, default 8) */
+  int pool_idle_first;        /* pools only (mf_pool_set_batching): 1 (default) hands a ready group
+                                 of small requests to the workers when the idle workers can take
+                                 all of it, one request each; 0 always batches it */
 } mf_batched_opts;
 
 typedef struct mf_batched_stats {
@@ -412,7 +418,10 @@ int mf_apply_batches(mf_ctx* const* ctxs, const int32_t* const* u, const int32_t
  * dispatcher thread instead of the workers.  The dispatcher
  * takes every such request that is ready -- one per graph -- and applies
  * them in one mf_apply_batches step; requests that arrive meanwhile form the
- * next step.  Larger requests, and the requests of graphs evicted to host
+ * next step.  With opts->pool_idle_first set, a ready group no larger than
+ * the number of idle workers goes to those workers instead (one step of the
+ * batched kernel costs more than a worker's plain batch when it would hold
+ * only a few requests).  Larger requests, and the requests of graphs evicted to host
  * memory (restored by the workers), stay with the workers.  opts NULL turns
  * it off.  Results per graph are unchanged. */
 int mf_pool_set_batching(mf_pool* pool, const mf_batched_opts* opts);

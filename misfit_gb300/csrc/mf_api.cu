@@ -571,7 +571,7 @@ int write_egr_int64(const std::string& out_path, int32_t n, const std::vector<in
 
 extern "C" {
 
-int mf_version(void) { return 10100; }
+int mf_version(void) { return 10200; }
 
 const char* mf_status_string(int status) {
   switch (status) {

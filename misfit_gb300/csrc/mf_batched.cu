@@ -149,6 +149,7 @@ mf_batched_opts default_opts() {
   o.max_cta_vertices = 1 << 20;
   o.use_graph = 1;
   o.path_threads = 8;
+  o.pool_idle_first = 1;
   return o;
 }
 

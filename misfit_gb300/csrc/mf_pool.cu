@@ -142,6 +142,7 @@ struct mf_pool {
   std::deque<int32_t> ready;   // graphs with queued batches and no running one
   std::unordered_map<int64_t, Request*> reqs;
   std::vector<std::thread> workers;
+  int working = 0;             // workers between taking a request and finishing it
   // batched dispatch (mf_pool_set_batching): small front requests are
   // routed to one dispatcher thread, which applies all of them that are
   // ready in one mf_apply_batches step while later arrivals queue for the
@@ -282,7 +283,21 @@ struct mf_pool {
         x.busy = true;
         group.push_back(g);
       }
-      if (!group.empty()) run_group(lk, group);
+      if (group.empty()) continue;
+      // idle workers (minus the requests already waiting for them) that can
+      // take the whole group, one request each: a worker's plain batch is
+      // cheaper than a batched step over so few requests
+      const int idle = (int)workers.size() - working - (int)ready.size();
+      if (bopts.pool_idle_first && (int)group.size() <= idle) {
+        for (const int32_t g : group) {
+          graphs[(size_t)g].busy = false;
+          ready.push_back(g);
+          cv_work.notify_one();
+        }
+        st.handed_to_workers += (int64_t)group.size();
+        continue;
+      }
+      run_group(lk, group);
     }
   }
 
@@ -383,6 +398,7 @@ struct mf_pool {
       gr.trimmed = false;
       gr.queue.pop_front();
       gr.busy = false;
+      --working;
       gr.last_use = ++tick;
       st.completed += 1;
       st.updates += (int64_t)rq->u.size();
@@ -409,6 +425,7 @@ struct mf_pool {
       Graph& gr = graphs[(size_t)gid];
       if (gr.busy || gr.queue.empty()) continue;
       gr.busy = true;
+      ++working;
       Request* rq = gr.queue.front();
       int status = MF_OK;
       std::string err;
@@ -447,6 +464,7 @@ struct mf_pool {
       gr.trimmed = false;
       gr.queue.pop_front();
       gr.busy = false;
+      --working;
       gr.last_use = ++tick;
       st.completed += 1;
       st.updates += (int64_t)rq->u.size();
@@ -674,7 +692,7 @@ int mf_pool_set_batching(mf_pool* p, const mf_batched_opts* opts) {
       o = *opts;
       need_arg(o.block >= 64 && o.block <= 1024 && o.block % 32 == 0 && o.ctas_per_sm >= 1 && o.ctas_per_sm <= 32 &&
                    o.max_cta_updates >= 0 && o.max_cta_updates <= mf::kMaxBatchEdges && o.path_threads >= 1 &&
-                   o.path_threads <= 64,
+                   o.path_threads <= 64 && (o.pool_idle_first == 0 || o.pool_idle_first == 1),
                "bad batched options");
     }
     std::lock_guard<std::mutex> lk(p->mu);

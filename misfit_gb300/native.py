@@ -55,7 +55,7 @@ class PoolStats(C.Structure):
         ("graphs", C.c_int64), ("completed", C.c_int64), ("updates", C.c_int64), ("errors", C.c_int64),
         ("evictions", C.c_int64), ("restores", C.c_int64), ("trims", C.c_int64), ("over_budget", C.c_int64),
         ("resident_bytes", C.c_int64), ("peak_resident_bytes", C.c_int64),
-        ("batched_steps", C.c_int64), ("batched_requests", C.c_int64),
+        ("batched_steps", C.c_int64), ("batched_requests", C.c_int64), ("handed_to_workers", C.c_int64),
     ]
 
     def as_dict(self):
@@ -66,6 +66,7 @@ class BatchedOpts(C.Structure):
     _fields_ = [
         ("block", C.c_int), ("ctas_per_sm", C.c_int), ("max_cta_updates", C.c_int64),
         ("max_cta_vertices", C.c_int32), ("use_graph", C.c_int), ("path_threads", C.c_int),
+        ("pool_idle_first", C.c_int),
     ]
 
 

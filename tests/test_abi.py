@@ -34,7 +34,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_version_and_status_strings(lib):
-    assert lib.mf_version() == 10100
+    assert lib.mf_version() == 10200
     assert lib.mf_status_string(0) == b"ok"
     assert lib.mf_status_string(-3) == b"malformed input file"
 

@@ -110,7 +110,7 @@ def test_pool_batched_dispatch_matches_dedicated_contexts(gpu_lib):
     plans = _streams(graphs, 3, 700)
     budget = int(3 * max((ni.size - 1) * 200 + nl.size * 8 for ni, nl in graphs))
     with native.Pool(budget, workers=3) as pool:
-        pool.set_batching(native.batched_opts(max_cta_updates=1500))
+        pool.set_batching(native.batched_opts(max_cta_updates=1500, pool_idle_first=0))
         gids = [pool.add_graph(ni, nl, plans[k][0]) for k, (ni, nl) in enumerate(graphs)]
         rids = []
         for b in range(3):
@@ -160,7 +160,9 @@ def test_pool_batched_dispatch_leaves_dense_graphs_to_workers(gpu_lib):
     walk of its 2-hop neighbourhoods stays small: lines * (1 + mean degree)^2
     within max_cta_updates * 33^2.  On a dense graph (mean degree ~95) the
     200-line requests go to the workers and the 20-line ones to the
-    dispatcher; memberships equal the dedicated context's either way."""
+    dispatcher; memberships equal the dedicated context's either way.  With
+    pool_idle_first (the default) a lone small request meets idle workers and
+    goes to them: no batched step at all."""
     n = 120
     ni, nl = W.er_graph(n, 95.0, 77)
     g = native.Graph.from_csr(ni, nl)
@@ -175,12 +177,13 @@ def test_pool_batched_dispatch_leaves_dense_graphs_to_workers(gpu_lib):
         reqs.append((u, v, ins))
         after.append(g.get_mis())
     g.close()
-    with native.Pool(1 << 30, workers=2) as pool:
-        pool.set_batching(native.batched_opts(max_cta_updates=512))
-        gid = pool.add_graph(ni, nl, mis0)
-        for k, (u, v, ins) in enumerate(reqs):
-            assert pool.wait(pool.submit(gid, u, v, ins)) >= 0
-            assert np.array_equal(pool.get_mis(gid), after[k]), k
-        st = pool.stats()
-    assert st["completed"] == len(reqs)
-    assert st["batched_requests"] == 3
+    for idle_first, batched, handed in ((0, 3, 0), (1, 0, 3)):
+        with native.Pool(1 << 30, workers=2) as pool:
+            pool.set_batching(native.batched_opts(max_cta_updates=512, pool_idle_first=idle_first))
+            gid = pool.add_graph(ni, nl, mis0)
+            for k, (u, v, ins) in enumerate(reqs):
+                assert pool.wait(pool.submit(gid, u, v, ins)) >= 0
+                assert np.array_equal(pool.get_mis(gid), after[k]), (idle_first, k)
+            st = pool.stats()
+        assert st["completed"] == len(reqs)
+        assert (st["batched_requests"], st["handed_to_workers"]) == (batched, handed), idle_first
