@@ -72,11 +72,13 @@ __global__ void k_scan_single(L load, int64_t n, int64_t* out) {
   for (int64_t base = 0; base < n; base += kTile) {
     int64_t v[kItems];
     int64_t local = 0;
+#pragma unroll
     for (int k = 0; k < kItems; ++k) {
       const int64_t i = base + (int64_t)threadIdx.x * kItems + k;
       v[k] = i < n ? load(i) : 0;
-      local += v[k];
     }
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) local += v[k];
     int64_t tot;
     int64_t pre = block_exclusive(local, sw, &tot) + carry;
     for (int k = 0; k < kItems; ++k) {
@@ -114,11 +116,17 @@ __global__ void __launch_bounds__(kThreads) k_scan_lookback(L load, int64_t n, i
   __shared__ int s_fallback;
   const int64_t t = blockIdx.x;
   const int64_t base = t * kTile;
+  // all of the thread's items are loaded before any is stored: a loader's
+  // generic loads may not pass a store to shared memory, so interleaved they
+  // would run one dependent chain (list entry -> row bounds) at a time
+  int64_t v[kItems];
+#pragma unroll
   for (int k = 0; k < kItems; ++k) {
-    const int idx = k * kThreads + threadIdx.x;
-    const int64_t i = base + idx;
-    tile[idx] = i < n ? load(i) : 0;
+    const int64_t i = base + k * kThreads + threadIdx.x;
+    v[k] = i < n ? load(i) : 0;
   }
+#pragma unroll
+  for (int k = 0; k < kItems; ++k) tile[k * kThreads + threadIdx.x] = v[k];
   __syncthreads();
   int64_t local = 0;
   for (int k = 0; k < kItems; ++k) local += tile[threadIdx.x * kItems + k];
