@@ -46,6 +46,9 @@ namespace {
 constexpr int kTB = 256;
 static_assert(kTB == kLbThreads, "lb_rows kernels run kLbThreads-thread blocks");
 constexpr int32_t kSkip = -2;
+// host counter slots [kFrontSlot + 2f, +1]: front f's counts, copied on the
+// stream that computed it
+constexpr int kFrontSlot = 10;
 
 inline unsigned grid_for(int64_t n, int per = kTB) {
   int64_t g = (n + per - 1) / per;
@@ -3520,11 +3523,19 @@ void process_batch(mf_ctx* c, int64_t m) {
     std::swap(c->hlist, fr.hlist);
     std::swap(c->cands, fr.cands);
 
-    // ---- packed sizes (upper bound) and MAX_CSR_ELEMENTS growth; one host
-    // round trip for the hop-1 counts and the bound
+    // ---- packed sizes (upper bound) and MAX_CSR_ELEMENTS growth.  The
+    // hop-1 counts and the bound: a front computed on the second stream
+    // copied them to its own host slot there, and by now has long finished,
+    // so this stream keeps its queue; otherwise one round trip here.
     sc.emplace(c, kStSizes);
-    MF_CUDA(cudaMemcpyAsync(h + 2, fr.cnt.p, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
-    MF_CUDA(cudaStreamSynchronize(s));
+    if (front_on_b) {
+      MF_CUDA(cudaEventSynchronize(c->ev_b));
+      h[2] = h[kFrontSlot + 2 * cur];
+      h[3] = h[kFrontSlot + 2 * cur + 1];
+    } else {
+      MF_CUDA(cudaMemcpyAsync(h + 2, fr.cnt.p, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
+      MF_CUDA(cudaStreamSynchronize(s));
+    }
     h[4] = h[3];
     h[3] = h[2] & 0xffffffffll;
     h[2] = h[2] >> 32;
@@ -3600,6 +3611,8 @@ void process_batch(mf_ctx* c, int64_t m) {
         MF_CUDA(cudaStreamWaitEvent(c->stream_b, c->ev_a, 0));
         g_alloc_stream = c->stream_b;   // any scratch the front's scans grow belongs to its stream
         front_compute(c, c->front[cur ^ 1], c->seeds_all.p + seed_base_next, ns_next, c->stream_b);
+        MF_CUDA(cudaMemcpyAsync(h + kFrontSlot + 2 * (cur ^ 1), c->front[cur ^ 1].cnt.p, sizeof(int64_t) * 2,
+                                cudaMemcpyDeviceToHost, c->stream_b));
         g_alloc_stream = s;
         MF_CUDA(cudaEventRecord(c->ev_b, c->stream_b));
         front_on_b = true;
