@@ -1278,13 +1278,40 @@ struct HasCidBit {
   __device__ __forceinline__ bool operator()(int32_t y) const { return (__ldg(bits + (y >> 5)) >> (y & 31)) & 1u; }
 };
 
+// One warp per 1,024 vertices (32 bitmap words): eight coalesced 16-byte
+// loads per lane, four ids each; the eight lanes that share a word OR their
+// nibbles together, and lane L stores the warp's word L.
+constexpr int64_t kCidBitsPerWarp = 1024;
+
 __global__ void k_cid_bits(const int32_t* cid, int32_t n, uint32_t* bits) {
   pdl_wait();
   pdl_trigger();
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool set = i < n && cid[i] != -1;
-  const unsigned m = __ballot_sync(0xffffffffu, set);
-  if ((threadIdx.x & 31) == 0 && i < ((int64_t)n + 31)) bits[i >> 5] = m;
+  const int lane = threadIdx.x & 31;
+  const int64_t v0 = warp_id() * kCidBitsPerWarp;
+  if (v0 >= n) return;   // the whole warp
+  uint32_t mine = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int64_t v = v0 + k * 128 + lane * 4;
+    uint32_t nib = 0;
+    if (v + 3 < n) {
+      const int4 x = *reinterpret_cast<const int4*>(cid + v);
+      nib = (uint32_t)(x.x != -1) | (uint32_t)(x.y != -1) << 1 | (uint32_t)(x.z != -1) << 2 |
+            (uint32_t)(x.w != -1) << 3;
+    } else {
+      for (int t = 0; t < 4; ++t)
+        if (v + t < n && cid[v + t] != -1) nib |= 1u << t;
+    }
+    // word k * 4 + lane / 8 of the warp's span, nibble lane % 8
+    uint32_t part = nib << ((lane & 7) * 4);
+    part |= __shfl_xor_sync(0xffffffffu, part, 1);
+    part |= __shfl_xor_sync(0xffffffffu, part, 2);
+    part |= __shfl_xor_sync(0xffffffffu, part, 4);
+    const uint32_t word = __shfl_sync(0xffffffffu, part, (lane & 3) * 8);
+    if ((lane >> 2) == k) mine = word;
+  }
+  const int64_t wi = (v0 >> 5) + lane;
+  if (wi < ((int64_t)n + 31) / 32) bits[wi] = mine;
 }
 
 // ---- first-hit searches with device-side counts ---------------------------------
@@ -2624,6 +2651,20 @@ __device__ __forceinline__ int round_scan(int x, int* s_warp, int* total) {
   return r;
 }
 
+// Start of a queued repair: both result pairs' first buffers to "no
+// write", the round words and the deferral counters to zero, in one launch.
+__global__ void k_repair_init(int32_t* w0, int32_t* w1, int64_t cnt, int64_t* dyn, int64_t* counts) {
+  pdl_wait();
+  pdl_trigger();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cnt) {
+    w0[i] = -1;
+    w1[i] = -1;
+  }
+  if (i < 4) dyn[i] = 0;
+  if (i < 6) counts[i] = 0;
+}
+
 __global__ void __launch_bounds__(kRoundThreads) k_spec_round(const int32_t* n0, const int32_t* n1, const int32_t* r0,
                                                               const int32_t* r1, int64_t p0, int64_t cnt,
                                                               const uint8_t* ins, int64_t p, const uint32_t* order,
@@ -3245,8 +3286,6 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
     c->big_grid = 4 * sms;
   }
-  MF_CUDA(cudaMemsetAsync(c->rp_w0.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
-  MF_CUDA(cudaMemsetAsync(c->rp_w1.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
   const int nbits = bits_for(std::max<int32_t>(c->n - 1, 1));
   int64_t p0 = 0, nview = 0, rounds = 0;
   if (nproc <= kRoundCap && !host_rounds_forced() && !debug_counters()) {
@@ -3255,8 +3294,8 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     // the device and does nothing once the repair is done.  Round r writes
     // into one pair of result buffers and compares with the other, in turn.
     int64_t* dyn = c->counters.p + 58;
-    MF_CUDA(cudaMemsetAsync(dyn, 0, sizeof(int64_t) * 4, s));
-    MF_CUDA(cudaMemsetAsync(c->counters.p + 24, 0, sizeof(int64_t) * 6, s));
+    MF_K(launch_pdl(k_repair_init, grid_for(std::max<int64_t>(nproc, 6)), kTB, 0, s, c->rp_w0.p, c->rp_w1.p, nproc,
+                    dyn, c->counters.p + 24));
     std::optional<StageScope> dsc;
     int64_t queued = 0;
     while (true) {
@@ -3298,6 +3337,8 @@ int64_t repair(mf_ctx* c, const GraphView& g, int64_t p, int64_t nproc, int64_t 
     }
     return h[61];
   }
+  MF_CUDA(cudaMemsetAsync(c->rp_w0.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
+  MF_CUDA(cudaMemsetAsync(c->rp_w1.p, 0xFF, sizeof(int32_t) * (size_t)nproc, s));
   int64_t dbg_big = 0, dbg_chunks = 0, dbg_scanned = 0;
   std::optional<StageScope> rsc;
   rsc.emplace(c, kStRepair);
@@ -3636,7 +3677,8 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_K(launch_pdl(k_row_skip, grid_for(rows), kTB, 0, s, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->rowcid.p,
                                                     c->creates.p, c->live_i.p, c->live_v.p, ucnt + 33));
     c->cidbits.reserve(((int64_t)n + 31) / 32 + 1);
-    MF_K(launch_pdl(k_cid_bits, grid_for(((int64_t)n + 31) / 32 * 32), kTB, 0, s, c->cid.p, n, c->cidbits.p));
+    MF_K(launch_pdl(k_cid_bits, warps_grid(((int64_t)n + kCidBitsPerWarp - 1) / kCidBitsPerWarp), kTB, 0, s, c->cid.p, n,
+                    c->cidbits.p));
     const HasCidBit has_cid{c->cidbits.p};
     first_hits(c, c->live_v.p, ucnt + 33, rows, has_cid);
     MF_K(launch_pdl(k_live_decide, lb_grid(c, k_live_decide), kTB, 0, s, g, c->live_i.p, c->live_v.p, ucnt + 33, ns,
