@@ -3191,7 +3191,8 @@ void exact_sizes(mf_ctx* c, int64_t ns, uint32_t ep, bool bound_only) {
 // `upper` bounds *dcnt.  No host round trip: every level reads its count on
 // the device.
 template <class P>
-void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, int64_t upper, P pred) {
+void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, int64_t upper, P pred,
+                unsigned long long* qcnt) {
   cudaStream_t s = c->stream;
   const int64_t cap = std::max<int64_t>(upper, 1);
   c->fpos.reserve(cap);
@@ -3200,9 +3201,7 @@ void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, 
   c->un_cnt.reserve(cap);
   c->rq_idx.reserve(cap);
   c->rq_v.reserve(cap);
-  unsigned long long* ucnt = reinterpret_cast<unsigned long long*>(c->counters.p);
-  MF_CUDA(cudaMemsetAsync(ucnt + 48, 0, sizeof(unsigned long long) * 2, s));
-  const FirstQueues q{c->un_idx.p, c->un_v.p, ucnt + 48, ChunkQueue{c->rq_idx.p, c->rq_v.p, c->un_cnt.p, ucnt + 49},
+  const FirstQueues q{c->un_idx.p, c->un_v.p, qcnt, ChunkQueue{c->rq_idx.p, c->rq_v.p, c->un_cnt.p, qcnt + 1},
                       std::max<int64_t>(c->tune.first_bound, kProbe)};
   const GraphView g = c->view();
   MF_K(launch_pdl(k_first_probe<P>, lb_grid(c, k_first_probe<P>), kTB, 0, s, g, list, dcnt, pred, c->fpos.p, q));
@@ -3212,7 +3211,7 @@ void first_hits(mf_ctx* c, const int32_t* list, const unsigned long long* dcnt, 
     unsigned long long v[3] = {0, 0, 0};
     MF_CUDA(cudaStreamSynchronize(s));
     MF_CUDA(cudaMemcpy(v, dcnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    MF_CUDA(cudaMemcpy(v + 1, ucnt + 48, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost));
+    MF_CUDA(cudaMemcpy(v + 1, qcnt, sizeof(unsigned long long) * 2, cudaMemcpyDeviceToHost));
     c->dbg_first[0] += 1;
     c->dbg_first[1] += (int64_t)v[0];
     c->dbg_first[2] += (int64_t)v[1];
@@ -3671,8 +3670,12 @@ void process_batch(mf_ctx* c, int64_t m) {
     c->mq_idx.reserve(std::max<int64_t>(ns, 1));
     c->mq_v.reserve(std::max<int64_t>(ns, 1));
     c->mq_base.reserve(std::max<int64_t>(ns, 1));
-    MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t) * 3, s));   // live rows, need seeds, their neighbours
-    MF_CUDA(cudaMemsetAsync(cnt + 50, 0, sizeof(int64_t), s));       // chunk queue of the need seeds' rows
+    // [33] live rows, [34] need seeds, [35] their neighbours, [36] the pull's
+    // long rows; [48, 49], [51, 52], [53, 54] the queues of the three
+    // first-hit searches, [50] the chunk queue of the need seeds' rows, [55]
+    // the assignment's count
+    MF_CUDA(cudaMemsetAsync(cnt + 33, 0, sizeof(int64_t) * 4, s));
+    MF_CUDA(cudaMemsetAsync(cnt + 48, 0, sizeof(int64_t) * 8, s));
     const ChunkQueue mq{c->mq_idx.p, c->mq_v.p, c->mq_base.p, ucnt + 50};
     MF_K(launch_pdl(k_row_skip, grid_for(rows), kTB, 0, s, c->seeds.p, ns, c->cands.p, nct, c->cid.p, c->rowcid.p,
                                                     c->creates.p, c->live_i.p, c->live_v.p, ucnt + 33));
@@ -3680,16 +3683,16 @@ void process_batch(mf_ctx* c, int64_t m) {
     MF_K(launch_pdl(k_cid_bits, warps_grid(((int64_t)n + kCidBitsPerWarp - 1) / kCidBitsPerWarp), kTB, 0, s, c->cid.p, n,
                     c->cidbits.p));
     const HasCidBit has_cid{c->cidbits.p};
-    first_hits(c, c->live_v.p, ucnt + 33, rows, has_cid);
+    first_hits(c, c->live_v.p, ucnt + 33, rows, has_cid, ucnt + 48);
     MF_K(launch_pdl(k_live_decide, lb_grid(c, k_live_decide), kTB, 0, s, g, c->live_i.p, c->live_v.p, ucnt + 33, ns,
                                                                  c->fpos.p, c->cid.p, c->rowcid.p, c->creates.p,
                                                                  c->seeds.p, c->need.p, c->needv.p, ucnt + 34, mq));
     sc.emplace(c, kStFirstNeed);
     MF_K(launch_pdl(k_mark_need, lb_grid(c, k_mark_need), kTB, 0, s, g, mq, ep, c->nmark.p, c->nlist_need.p, ucnt + 35));
-    first_hits(c, c->nlist_need.p, ucnt + 35, n, has_cid);
+    first_hits(c, c->nlist_need.p, ucnt + 35, n, has_cid, ucnt + 51);
     MF_K(launch_pdl(k_f1_finish, lb_grid(c, k_f1_finish), kTB, 0, s, g, c->nlist_need.p, ucnt + 35, c->fpos.p, c->cid.p,
                                                              c->f1.p));
-    first_hits(c, c->needv.p, ucnt + 34, ns, HasF1{c->f1.p});
+    first_hits(c, c->needv.p, ucnt + 34, ns, HasF1{c->f1.p}, ucnt + 53);
     MF_K(launch_pdl(k_need_decide, lb_grid(c, k_need_decide), kTB, 0, s, g, c->need.p, c->needv.p, ucnt + 34, c->fpos.p,
                                                                  c->f1.p, c->rowcid.p, c->creates.p));
     scan_exclusive_u8(c->creates.p, c->i64b.p, rows, c->ws, s);
@@ -3721,8 +3724,7 @@ void process_batch(mf_ctx* c, int64_t m) {
       c->pull_long.reserve(std::max<int32_t>(n, 1));
       const int64_t nwords = ((int64_t)n + 31) / 32;
       c->ncbits.reserve(std::max<int64_t>(nwords, 1));
-      MF_CUDA(cudaMemsetAsync(c->ncbits.p, 0, sizeof(uint32_t) * (size_t)nwords, s));
-      MF_CUDA(cudaMemsetAsync(cnt + 36, 0, sizeof(int64_t), s));
+      MF_CUDA(cudaMemsetAsync(c->ncbits.p, 0, sizeof(uint32_t) * (size_t)nwords, s));   // [36] zeroed above
       if (nct > 0)
         MF_K(launch_pdl(k_cand_bits, grid_for(nct), kTB, 0, s, c->cands.p, nct, ns, c->rowcid.p, c->ncbits.p));
       const PullArgs pa{g,  c->v2i.p, c->rowcid.p, c->ncbits.p, ns, c->wval.p, ep, c->cid.p, c->pull_long.p,
@@ -3756,10 +3758,9 @@ void process_batch(mf_ctx* c, int64_t m) {
 
     // ---- assignment + order (cluster ascending, index descending)
     sc.emplace(c, kStAssign);
-    MF_CUDA(cudaMemsetAsync(cnt + 9, 0, sizeof(int64_t), s));
     MF_K(launch_pdl(k_assign, grid_for(q - p), kTB, 0, s, c->bu.p, c->bv.p, p, q - p, c->cid.p, c->i64b.p + rows, c->keys.p,
-                                                  c->vals.p, ucnt + 9));
-    MF_CUDA(cudaMemcpyAsync(h + 9, cnt + 9, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                                                  c->vals.p, ucnt + 55));
+    MF_CUDA(cudaMemcpyAsync(h + 9, cnt + 55, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     MF_CUDA(cudaStreamSynchronize(s));
     const int64_t cc = h[7];
     const int64_t limit = std::min<int64_t>(cc, kMaxBatchEdges);
