@@ -2159,6 +2159,54 @@ __device__ __forceinline__ bool spec_seed(const SpecArgs& a, int32_t x) {
   return i >= 0 && (int64_t)i < a.ns;
 }
 
+// Thread: does row(x) hold a member other than `except`?  1 yes, 0 no, -1
+// when `left` ran out first (it is decremented by the live elements read).
+// Eight positions at a time: their ids, then their membership bytes, all
+// loads of a group in flight before any is tested; the rare pending-write
+// lookups (bit 1 of the byte) go through the view.  A group may read past
+// the budget or past the first member; only the answer is defined.
+__device__ __forceinline__ int t_row_any(const GraphView& g, int32_t x, const Member& mem, int32_t except, int& left) {
+  const uint8_t* m = mem.V->m;
+  auto group = [&](const int32_t (&y)[8]) {
+    uint8_t mb[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) mb[q] = y[q] >= 0 ? m[y[q]] : 0;
+    bool hit = false;
+    int cnt = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (y[q] < 0) continue;
+      ++cnt;
+      if (y[q] == except || y[q] == mem.self0) continue;
+      hit |= (mb[q] & 2) ? mem(y[q]) != 0 : (mb[q] & 1) != 0;
+    }
+    left -= cnt;
+    return hit;
+  };
+  const int64_t b = g.nindex[x], e = g.nindex[x + 1];
+  const bool filt = g.dead[x] != 0;
+  for (int64_t k0 = b; k0 < e; k0 += 8) {
+    if (left <= 0) return -1;
+    int32_t y[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int64_t k = k0 + q;
+      y[q] = -1;
+      if (k < e && (!filt || live_at(g.live, k))) y[q] = __ldg(g.nlist + k);
+    }
+    if (group(y)) return 1;
+  }
+  const int64_t ab = g.aoff[x], ae = g.aoff[x + 1];
+  for (int64_t k0 = ab; k0 < ae; k0 += 8) {
+    if (left <= 0) return -1;
+    int32_t y[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) y[q] = k0 + q < ae ? g.aadj[k0 + q] : -1;
+    if (group(y)) return 1;
+  }
+  return 0;
+}
+
 // Warp: does row-of(x) hold a member other than `except`?
 __device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t except) {
   const GraphView& g = a.g;
@@ -2176,8 +2224,12 @@ __device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t e
     const int32_t h = k < nr ? row_elem(g, x, k, nb) : -1;
     bool found = false, longrow = false;
     if (h >= 0) {
-      if (row_len(g, h) <= 64) found = thread_row_until(g, h, hit);
-      else longrow = true;
+      if (row_len(g, h) <= 64) {
+        int unbounded = 1 << 30;
+        found = t_row_any(g, h, mem, except, unbounded) > 0;
+      } else {
+        longrow = true;
+      }
     }
     if (__any_sync(0xffffffffu, found)) return true;
     unsigned lm = __ballot_sync(0xffffffffu, longrow);
@@ -2192,22 +2244,19 @@ __device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t e
 }
 
 // Thread: 1 if row-of(x) holds a member (other than `except`), 0 if it holds
-// none, -1 if `budget` elements were read without an answer.
+// none, -1 if about `budget` elements were read without an answer (up to
+// seven more: the row scans read eight at a time).
 __device__ int t_any_bounded(const SpecArgs& a, const Member& mem, int32_t x, int32_t except, int budget) {
   int left = budget;
-  int res = 0;
-  auto hit = [&](int32_t z) {
-    if (z != except && mem(z) != 0) { res = 1; return true; }
-    if (--left <= 0) { res = -1; return true; }
-    return false;
-  };
-  if (!spec_seed(a, x)) {
-    thread_row_until(a.g, x, hit);
-    return res;
-  }
+  if (!spec_seed(a, x)) return t_row_any(a.g, x, mem, except, left);
   if (x != except && mem(x)) return 1;
-  if (thread_row_until(a.g, x, hit)) return res;
-  thread_row_until(a.g, x, [&](int32_t h) { return thread_row_until(a.g, h, hit); });
+  const int r = t_row_any(a.g, x, mem, except, left);
+  if (r != 0) return r;
+  int res = 0;
+  thread_row_until(a.g, x, [&](int32_t h) {
+    res = t_row_any(a.g, h, mem, except, left);
+    return res != 0;
+  });
   return res;
 }
 
@@ -2396,7 +2445,7 @@ __global__ void k_spec_eval(SpecArgs a, int64_t* chunk_pre, unsigned long long* 
 // row-of without an early member) are settled afterwards by whole warps, so
 // that no single thread walks a hub row alone.  The chunk's answer is the
 // smallest eligible position.
-__global__ void __launch_bounds__(kBigChunk) k_big_scan(SpecArgs a, const int64_t* chunk_pre,
+__global__ void __launch_bounds__(kBigChunk, 4) k_big_scan(SpecArgs a, const int64_t* chunk_pre,
                                                         unsigned long long* best, unsigned long long* queue) {
   pdl_wait();
   pdl_trigger();
