@@ -2207,15 +2207,50 @@ __device__ __forceinline__ int t_row_any(const GraphView& g, int32_t x, const Me
   return 0;
 }
 
+// Warp: does row(x) hold a member other than `except`?  Steps of one, two,
+// then four 32-position windows, the ids and then the membership bytes of a
+// step loaded before any is tested.
+__device__ bool w_row_any(const GraphView& g, int32_t x, const Member& mem, int32_t except) {
+  const int lane = threadIdx.x & 31;
+  const uint8_t* m = mem.V->m;
+  const int64_t b = g.nindex[x], nb = g.nindex[x + 1] - b;
+  const int64_t ab = g.aoff[x];
+  const int64_t np = nb + (g.aoff[x + 1] - ab);
+  const bool filt = g.dead[x] != 0;
+  int nwin = 1;
+  for (int64_t base = 0; base < np; base += 32 * nwin, nwin = nwin < 4 ? 2 * nwin : 4) {
+    int32_t y[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t k = base + 32 * q + lane;
+      y[q] = -1;
+      if (q < nwin && k < np) {
+        if (k < nb) {
+          if (!filt || live_at(g.live, b + k)) y[q] = __ldg(g.nlist + b + k);
+        } else {
+          y[q] = g.aadj[ab + (k - nb)];
+        }
+      }
+    }
+    uint8_t mb[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) mb[q] = y[q] >= 0 ? m[y[q]] : 0;
+    bool hit = false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (y[q] >= 0 && y[q] != except && y[q] != mem.self0) hit |= (mb[q] & 2) ? mem(y[q]) != 0 : (mb[q] & 1) != 0;
+    if (__any_sync(0xffffffffu, hit)) return true;
+  }
+  return false;
+}
+
 // Warp: does row-of(x) hold a member other than `except`?
 __device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t except) {
   const GraphView& g = a.g;
   const int lane = threadIdx.x & 31;
-  auto hit = [&](int32_t z) { return z != except && mem(z) != 0; };
   const bool seed = spec_seed(a, x);
-  if (seed && hit(x)) return true;
-  int32_t dummy;
-  if (warp_row_first(g, x, hit, &dummy)) return true;
+  if (seed && x != except && mem(x) != 0) return true;
+  if (w_row_any(g, x, mem, except)) return true;
   if (!seed) return false;
   const int64_t nb = g.nindex[x + 1] - g.nindex[x];
   const int64_t nr = nb + (g.aoff[x + 1] - g.aoff[x]);
@@ -2237,7 +2272,7 @@ __device__ bool w_any(const SpecArgs& a, const Member& mem, int32_t x, int32_t e
       const int src = __ffs(lm) - 1;
       lm &= lm - 1;
       const int32_t hh = __shfl_sync(0xffffffffu, h, src);
-      if (warp_row_first(g, hh, hit, &dummy)) return true;
+      if (w_row_any(g, hh, mem, except)) return true;
     }
   }
   return false;
@@ -2300,11 +2335,17 @@ __device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_
   if (!seed) return -1;
   const int64_t nb = g.nindex[r + 1] - g.nindex[r];
   const int64_t nr = nb + (g.aoff[r + 1] - g.aoff[r]);
-  // Volume of the hop-2 part; long ones go to the grid-wide search.
+  // Volume of the hop-2 part; long ones go to the grid-wide search.  Four
+  // windows of row(r) per step, their ids and then their row lengths loaded
+  // before any is summed.
   int64_t vol = 0;
-  for (int64_t k = lane; k < nr; k += 32) {
-    const int32_t h = row_elem(g, r, k, nb);
-    if (h >= 0) vol += row_positions(g, h);   // positions, tombstoned ones included
+  for (int64_t k0 = lane; k0 < nr; k0 += 128) {
+    int32_t hq[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) hq[q] = k0 + 32 * q < nr ? row_elem(g, r, k0 + 32 * q, nb) : -1;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (hq[q] >= 0) vol += row_positions(g, hq[q]);   // positions, tombstoned ones included
   }
   for (int o = 16; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
   if (vol > a.big_threshold) {
@@ -2313,20 +2354,26 @@ __device__ int32_t w_first_eligible(const SpecArgs& a, const Member& mem, int32_
     off = __shfl_sync(0xffffffffu, off, 0);
     if ((int64_t)(off + nr + 1) <= a.pre_cap) {
       int64_t carry = 0;
-      for (int64_t k0 = 0; k0 < nr; k0 += 32) {
-        const int64_t k = k0 + lane;
-        int64_t len = 0;
-        if (k < nr) {
-          const int32_t h = row_elem(g, r, k, nb);
-          if (h >= 0) len = row_positions(g, h);
+      for (int64_t k0 = 0; k0 < nr; k0 += 128) {
+        // four windows: every row length loaded before any prefix is stored
+        int64_t len[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int64_t k = k0 + 32 * q + lane;
+          const int32_t h = k < nr ? row_elem(g, r, k, nb) : -1;
+          len[q] = h >= 0 ? row_positions(g, h) : 0;
         }
-        int64_t inc = len;
-        for (int o = 1; o < 32; o <<= 1) {
-          const int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
-          if (lane >= o) inc += t;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int64_t k = k0 + 32 * q + lane;
+          int64_t inc = len[q];
+          for (int o = 1; o < 32; o <<= 1) {
+            const int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+          }
+          if (k < nr) a.pre[off + k] = carry + inc - len[q];
+          carry += __shfl_sync(0xffffffffu, inc, 31);
         }
-        if (k < nr) a.pre[off + k] = carry + inc - len;
-        carry += __shfl_sync(0xffffffffu, inc, 31);
       }
       if (lane == 0) {
         a.pre[off + nr] = carry;
