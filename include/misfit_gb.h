@@ -196,9 +196,11 @@ typedef struct mf_tuning {
   int64_t first_bound;    /* row positions the warp level of the first-cluster-id search covers
                              before long rows go to the chunk level (default 256, at least 8;
                              values below 32, the per-thread probe's length, act as 32) */
-  int64_t cand_push;      /* 0: on graphs with symmetric sorted rows, the candidate rows' cluster ids
-                             are pulled by every vertex (default); 1: always pushed from the
-                             candidate rows, then finalised per vertex */
+  int64_t cand_push;      /* the candidate rows' cluster ids: 1 always pushed from the candidate rows,
+                             then finalised per vertex; 2 pulled by every vertex on graphs with
+                             symmetric sorted rows (pushed on the others); 0 (default) as 2, except
+                             the sub-batches whose candidate rows hold so few entries that the push
+                             costs less than half the pull's estimate */
   int64_t pull_sizes;     /* exact 2-hop sizes on symmetric graphs: 0 always by the push form (bit
                              atomics per element of every member's row); 1 (default) the seeds whose
                              neighbourhood volume pays for it by passes over every row, up to 256

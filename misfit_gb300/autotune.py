@@ -140,7 +140,7 @@ def tune_batched(graphs, mis0, batches, use_cache=True):
 DEFAULT_TUNING = {"pull_long": 2048, "heavy_min": 2048, "big_threshold": 64, "first_bound": 256, "cand_push": 0,
                   "pull_sizes": 1}
 PLAIN_KNOBS = (
-    ("cand_push", (0, 1)),
+    ("cand_push", (0, 1, 2)),
     ("pull_sizes", (1, 0, 2)),
     ("big_threshold", (64, 256, 1024, 4096)),
     ("first_bound", (64, 256, 1024)),

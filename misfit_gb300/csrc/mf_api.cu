@@ -222,6 +222,7 @@ void run_batch(mf_ctx* c, int64_t m) {
   c->traces.clear();
   c->work.reserve(2 * mf::kStCount + 8);
   c->touched_total = 0;
+  c->pull_runs = 0;
   MF_CUDA(cudaMemsetAsync(c->work.p, 0, sizeof(unsigned long long) * (2 * mf::kStCount + 8), s));
   MF_CUDA(cudaEventRecord(c->ev0, s));
   if (m > 0) {
@@ -247,20 +248,28 @@ void run_batch(mf_ctx* c, int64_t m) {
   }
   c->ev_marks.clear();
   c->ev_used = 0;
+  if (c->pull_runs > 0 && c->n >= (1 << 20)) {
+    // row entries the pull read per vertex, for the next batch's pull-or-push choice
+    unsigned long long visited = 0;
+    MF_CUDA(cudaMemcpy(&visited, c->work.p + 2 * mf::kStCount + 2, sizeof(visited), cudaMemcpyDeviceToHost));
+    c->pull_visit_ratio = (double)visited / ((double)c->pull_runs * (double)c->n);
+  }
   static const bool debug = std::getenv("MISFIT_GB_DEBUG") != nullptr;
   if (debug || c->profile) {
     unsigned long long w[2 * mf::kStCount + 8];
     MF_CUDA(cudaMemcpy(w, c->work.p, sizeof(w), cudaMemcpyDeviceToHost));
     const unsigned long long* x = w + 2 * mf::kStCount;
-    // 4 B row entry + 8 B state read and cid write per pushed element; in
-    // the pull form the candidates' counter is the row entries the pull read
-    const bool pull_form = c->symmetric && c->rows_sorted && c->tune.cand_push == 0;
-    c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + (pull_form ? 0ull : x[2]));
-    if (pull_form) c->stage_bytes[mf::kStPull] += 4.0 * (double)x[2];
+    // 4 B row entry + 8 B state read and cid write per pushed element (x[3]:
+    // the candidate rows of the sub-batches that pushed); x[2] the row
+    // entries read by the sub-batches that pulled
+    c->stage_bytes[mf::kStPush] += 12.0 * (double)(x[0] + x[3]);
+    c->stage_bytes[mf::kStPull] += 4.0 * (double)x[2];
     c->stage_bytes[mf::kStPushHop] += 12.0 * (double)x[1];
     if (debug) {
-      std::fprintf(stderr, "[misfit_gb] batch: push elements seed %llu hop %llu cand %llu; sub-batches %lld\n", x[0],
-                   x[1], x[2], (long long)c->stats.sub_batches);
+      std::fprintf(stderr,
+                   "[misfit_gb] batch: push elements seed %llu hop %llu cand %llu; pull entries %llu in %lld of %lld "
+                   "sub-batches\n",
+                   x[0], x[1], x[3], x[2], (long long)c->pull_runs, (long long)c->stats.sub_batches);
       std::fprintf(stderr, "[misfit_gb] first hits: calls %lld rows %lld warp-level %lld chunk-level %lld chunks %lld\n",
                    (long long)c->dbg_first[0], (long long)c->dbg_first[1], (long long)c->dbg_first[2],
                    (long long)c->dbg_first[3], (long long)c->dbg_first[4]);
@@ -787,10 +796,10 @@ int mf_set_tuning(mf_ctx* c, const mf_tuning* in) {
   return guarded([&] {
     need(c && in, MF_EINVAL, "null argument");
     need(in->pull_long >= 32 && in->heavy_min >= 64 && in->big_threshold >= 0 && in->first_bound >= 8 &&
-             in->first_bound <= ((int64_t)1 << 20) && (in->cand_push == 0 || in->cand_push == 1) &&
+             in->first_bound <= ((int64_t)1 << 20) && in->cand_push >= 0 && in->cand_push <= 2 &&
              in->pull_sizes >= 0 && in->pull_sizes <= 2,
          MF_EINVAL, "tuning out of range (pull_long >= 32, heavy_min >= 64, big_threshold >= 0, "
-                    "8 <= first_bound <= 2^20, cand_push 0 or 1, pull_sizes 0..2)");
+                    "8 <= first_bound <= 2^20, cand_push 0..2, pull_sizes 0..2)");
     bind(c);
     c->tune = *in;
   });

@@ -649,6 +649,12 @@ struct mf_ctx {
   // sub-batch), how often it ran, and the sub-batches it was skipped on
   uint32_t bound_hist = 0;
   int64_t bound_tries = 0, bound_skips = 0;
+  // the candidates' cluster ids, pull or push per sub-batch (tuning
+  // cand_push 0): row entries the pull read per vertex in the last batch
+  // that pulled on a graph of 2^20 vertices or more (1 before any), and the
+  // pull sub-batches of the current batch
+  double pull_visit_ratio = 1.0;
+  int64_t pull_runs = 0;
   mf::DBuf<unsigned long long> fpos;   // first-hit positions
   mf::DBuf<int32_t> un_idx, un_v, need, needv, live_i, live_v, nlist_need;
   mf::DBuf<uint32_t> nmark;            // epoch marks: neighbours of seeds needing their hop-2 part

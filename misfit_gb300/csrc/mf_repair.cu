@@ -3681,6 +3681,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     const int64_t rows = ns + nct;
     if (nct > 0) MF_K(launch_pdl(k_cand_v2i, grid_for(nct), kTB, 0, s, c->cands.p, nct, ns, c->v2i.p));
     int64_t packed = -1;
+    int64_t cand_total = h[4];   // entries of the candidate rows: the bound, exact below if sized
     const bool exact = h[4] >= c->max_csr;
     if (exact) {
       // The limit grows only if the packed total reaches it.  A tighter upper
@@ -3698,8 +3699,10 @@ void process_batch(mf_ctx* c, int64_t m) {
         exact_sizes(c, ns, ep, true);
         scan_exclusive_i64(c->rowlens.p, c->i64a.p, rows, c->ws, s);
         MF_CUDA(cudaMemcpyAsync(h + 6, c->i64a.p + rows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        MF_CUDA(cudaMemcpyAsync(h + 8, c->i64a.p + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         MF_CUDA(cudaStreamSynchronize(s));
         settled = h[6] < c->max_csr;
+        cand_total = h[6] - h[8];   // the candidates' lengths are exact in the bound too
         c->bound_hist = (c->bound_hist << 1) | (settled ? 1u : 0u);
         ++c->bound_tries;
       }
@@ -3710,9 +3713,11 @@ void process_batch(mf_ctx* c, int64_t m) {
         MF_CUDA(cudaMemcpyAsync(cnt + 5, h + 5, sizeof(int64_t), cudaMemcpyHostToDevice, s));
         MF_K(k_growth<<<1, 32, 0, s>>>(c->i64a.p, rows, cnt + 5));
         MF_CUDA(cudaMemcpyAsync(h + 5, cnt + 5, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, s));
+        MF_CUDA(cudaMemcpyAsync(h + 8, c->i64a.p + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         MF_CUDA(cudaStreamSynchronize(s));
         c->max_csr = h[5];
         packed = h[6];
+        cand_total = h[6] - h[8];
         c->stats.exact_sizes += 1;
       }
     }
@@ -3815,8 +3820,21 @@ void process_batch(mf_ctx* c, int64_t m) {
                                                                  c->wval.p, wk_extra + 1));
     sc.emplace(c, kStPush);
     if (debug_launches()) debug_push_hop(c, wk_extra + 1, dbg1);
-    sc.emplace(c, kStPull);
-    if (c->symmetric && c->rows_sorted && c->tune.cand_push == 0) {
+    // Pull or push.  The pull costs ~28 B per vertex plus 4 B per row entry
+    // it reads (as many per vertex as in the last batch that pulled); the
+    // push at most 12 B per entry of the candidate rows plus the 8 B per
+    // vertex of its finalising pass.  With cand_push 0 the push is taken
+    // when that bound is under half the pull's estimate (sparse candidate
+    // rows on a large graph, where the pull walks most rows to their end).
+    bool use_pull = c->symmetric && c->rows_sorted && c->tune.cand_push != 1;
+    if (use_pull && c->tune.cand_push == 0) {
+      const double push_b = 12.0 * (double)cand_total + 8.0 * (double)n;
+      const double pull_b = (28.0 + 4.0 * c->pull_visit_ratio) * (double)n;
+      if (2.0 * push_b < pull_b) use_pull = false;
+    }
+    sc.emplace(c, use_pull ? kStPull : kStPush);
+    if (use_pull) {
+      ++c->pull_runs;
       c->pull_long.reserve(std::max<int32_t>(n, 1));
       const int64_t nwords = ((int64_t)n + 31) / 32;
       c->ncbits.reserve(std::max<int64_t>(nwords, 1));
@@ -3833,7 +3851,7 @@ void process_batch(mf_ctx* c, int64_t m) {
     } else {
       row_offsets(c, c->cands.p, nct, kCntCandRows, ns, ep);
       MF_K(launch_pdl(k_lb_push_cand, lb_grid(c, k_lb_push_cand), kTB, 0, s, g, c->cands.p, c->lb_offs.p, nct, ns, ep, c->wval.p,
-                                                     wk_extra + 2));
+                                                     wk_extra + 3));
       MF_K(launch_pdl(k_finalize_all, grid_for(((int64_t)n + 3) / 4), kTB, 0, s, c->wval.p, n, ep, c->rowcid.p, c->cid.p));
     }
     c->touched_total += n;

@@ -503,7 +503,7 @@ def test_tuning_settings_change_no_result(gpu_lib):
     for tune in ({}, {"pull_long": 32, "heavy_min": 64, "big_threshold": 0, "first_bound": 8, "cand_push": 1,
                       "pull_sizes": 2},
                  {"pull_long": 1 << 20, "heavy_min": 1 << 30, "big_threshold": 1 << 40, "first_bound": 1 << 20,
-                  "pull_sizes": 0}):
+                  "cand_push": 2, "pull_sizes": 0}):
         g = native.Graph.from_csr(ni, nl)
         if not tune:
             assert g.tuning() == autotune.DEFAULT_TUNING
@@ -515,7 +515,7 @@ def test_tuning_settings_change_no_result(gpu_lib):
             g.apply_batch(u, v, ins)
             out.append((g.get_mis(), g.cluster_ids()))
         results.append(out)
-        for bad in ({"pull_long": 1}, {"first_bound": 4}, {"big_threshold": -1}, {"cand_push": 2},
+        for bad in ({"pull_long": 1}, {"first_bound": 4}, {"big_threshold": -1}, {"cand_push": 3},
                     {"pull_sizes": 3}):
             with pytest.raises(native.MisfitError):
                 g.set_tuning(**bad)
