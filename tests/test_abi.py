@@ -84,3 +84,39 @@ def test_batch_folder_order(lib, tmp_path):
     (tmp_path / "notes.txt").write_text("x")
     with pytest.raises(native.MisfitError):
         native.list_batch_files(str(tmp_path))
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every public struct of include/misfit_gb.h has the same size and field
+    offsets in C (compiled here with the host compiler) as its ctypes mirror
+    in misfit_gb300/native.py, field for field and in the same order."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"mf_batch_stats": native.BatchStats, "mf_tuning": native.Tuning, "mf_pool_stats": native.PoolStats,
+               "mf_batched_opts": native.BatchedOpts, "mf_batched_stats": native.BatchedStats}
+    header = open(os.path.join(ROOT, "include", "misfit_gb.h")).read()
+    lines = ['#include <stdio.h>', '#include "misfit_gb.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (cname, cname), header, flags=re.S)
+        assert body, cname
+        decl = re.sub(r"/\*.*?\*/", "", body.group(1), flags=re.S)
+        cfields = re.findall(r"\b([a-z_][a-z_0-9]*)\s*;", decl)
+        assert cfields == [f[0] for f in cls._fields_], cname   # same names, same order
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f in cfields:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = dict(line.split() for line in subprocess.check_output([str(exe)], text=True).splitlines())
+    for cname, cls in mirrors.items():
+        assert int(got[cname]) == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert int(got["%s.%s" % (cname, f)]) == getattr(cls, f).offset, (cname, f)
